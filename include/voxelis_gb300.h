@@ -1,0 +1,199 @@
+/*
+ * voxelis_gb300 — C ABI of the GB300-native SVO-DAG edit-and-intern path.
+ *
+ * This header is the drop-in boundary for voxelis' batched edit path. Each entry point names
+ * the reference interface it replaces (paths are relative to the voxelis repository):
+ *
+ *   VoxInterner::<T>::with_memory_budget   voxelis/src/interner/mod.rs:45-164
+ *   VoxTree::new / get / set / fill / clear voxelis/src/spatial/voxtree.rs:116-292
+ *   VoxTree::apply_batch                    voxelis/src/spatial/voxtree.rs:303-328
+ *   Batch::new / just_set / just_fill / just_clear / size / has_patches
+ *                                           voxelis/src/core/batch.rs:63-195
+ *   VoxInterner::get_ref                    voxelis/src/interner/mod.rs:222-233
+ *   collect_stats / to_vec (verification)   voxelis/src/utils/common.rs:158-333
+ *
+ * Conventions
+ *   - Every function returns an int status (VX_OK or a VX_E_* code). Reference panics map to
+ *     status codes; nothing unwinds or aborts across this boundary.
+ *   - The interner's node store, hash-consing tables, reference counts and generations live in
+ *     device memory (HBM). Trees are small integer handles whose root ids also live on the device.
+ *   - Voxel values cross the boundary as uint32_t and must fit the interner's voxel width
+ *     (8 or 16 bits). Value 0 is the empty voxel (T::default()).
+ *   - Functions taking a `vx_mem` argument read/write either host memory (VX_MEM_HOST; copies are
+ *     done inside the call) or device memory (VX_MEM_DEVICE; pointers must be device pointers).
+ *   - All device work is ordered on the interner's stream (vx_interner_set_stream). Calls that
+ *     return results in host memory synchronise that stream before returning; the *_async calls
+ *     do not, and their status is reported by the next vx_interner_sync.
+ *   - One writer at a time per interner, as in the reference (&mut VoxInterner).
+ */
+#ifndef VOXELIS_GB300_H
+#define VOXELIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define VX_OK 0
+#define VX_E_INVALID_ARG 1  /* null/unknown handle, bad voxel width, bad flag                    */
+#define VX_E_OOB 2          /* position outside the tree (voxtree.rs:146-148 assert!)            */
+#define VX_E_OOM 3          /* node capacity exhausted (interner/macros.rs:38 panic!)            */
+#define VX_E_DEPTH 4        /* depth cap (core/max_depth.rs:77-83) or unsupported depth          */
+#define VX_E_TABLE_FULL 5   /* device hash table probe limit reached                             */
+#define VX_E_TIMEOUT 6      /* a bounded device spin-wait gave up; the context stays usable      */
+#define VX_E_CUDA 7         /* CUDA runtime error                                                */
+#define VX_E_REF_PANIC 8    /* the reference panics on this input (assert!, BlockId::types())   */
+#define VX_E_REF_UB 9       /* the reference hits undefined behaviour (refcount underflow,
+                               release-stack overflow, dangling child)                          */
+#define VX_E_BUFFER 10      /* caller buffer too small; the required size is reported            */
+#define VX_E_UNSUPPORTED 11 /* valid request outside this build's supported set                 */
+
+/* ---- reference patches (behaviour switches, all OFF by default) --------------------------- */
+/* P1: a leaf met exactly at depth max-1 during the batch descent is treated as an ancestor leaf
+ *     instead of panicking in BlockId::types() (voxtree.rs:792-834, block_id.rs:273-276).      */
+#define VX_PATCH_P1 (1u << 0)
+/* P2: depths up to 10 with the closed-form sibling masks (voxtree.rs:41-105 covers 0..6).     */
+#define VX_PATCH_P2 (1u << 1)
+/* P3: growable release queue instead of the fixed 32768 entries (interner/mod.rs:99, 431-513). */
+#define VX_PATCH_P3 (1u << 2)
+/* P4: batch clear bits are honoured, as VoxTree::set(pos, 0) applied to every cleared voxel
+ *     after the set phase (voxtree.rs:563-705); without it they are ignored (voxtree.rs:779).  */
+#define VX_PATCH_P4 (1u << 3)
+
+/* ---- memory locations --------------------------------------------------------------------- */
+typedef enum { VX_MEM_HOST = 0, VX_MEM_DEVICE = 1 } vx_mem;
+
+/* ---- special block ids (core/block_id.rs:120-123) ----------------------------------------- */
+#define VX_BLOCK_EMPTY 0ull
+#define VX_BLOCK_INVALID 0xFFFFFFFFFFFFFFFFull
+
+typedef struct vx_interner vx_interner; /* opaque: device-resident VoxInterner<T>          */
+typedef struct vx_batch vx_batch;       /* opaque: host staging buffer mirroring Batch<T>   */
+typedef uint32_t vx_tree;               /* tree handle, scoped to one interner              */
+
+typedef struct {
+    uint64_t capacity;        /* nodes_capacity = budget / node_size (interner/mod.rs:49-53)      */
+    uint64_t node_size;       /* 4 + 2 + 64 + sizeof(T) + 8 bytes (interner/mod.rs:158-164)       */
+    uint64_t next_index;      /* bump pointer (interner/macros.rs:19-35)                          */
+    uint64_t free_count;      /* length of the LIFO free list (interner/mod.rs:608)               */
+    uint64_t alive_nodes;     /* next_index - free_count (includes the EMPTY branch at index 0)   */
+    uint64_t branch_patterns; /* live entries in the branch table                                 */
+    uint64_t leaf_patterns;   /* live entries in the leaf table                                   */
+    uint64_t table_slots;     /* device branch table size (slots), 0 for the oracle               */
+    uint64_t table_tombstones;/* deleted slots awaiting a rehash                                  */
+    uint64_t error_flags;     /* sticky device error bits (see vx_interner_sync)                  */
+} vx_interner_stats;
+
+/* Canonical depth-first export: nodes renumbered in pre-order over the given trees (children
+ * visited in slot order 0..7, EMPTY children skipped), so that two interners holding the same
+ * DAG produce byte-identical arrays whatever their allocation order. */
+typedef struct {
+    uint8_t *kind;      /* [n_nodes] 1 = leaf, 0 = branch                                   */
+    uint8_t *types;     /* [n_nodes] BlockId types bits (0 for leaves)                      */
+    uint8_t *mask;      /* [n_nodes] BlockId mask bits (0 for leaves)                       */
+    uint32_t *value;    /* [n_nodes] leaf value, or the branch LOD value (voxel.rs:96-141)  */
+    uint32_t *refcount; /* [n_nodes]                                                        */
+    int32_t *children;  /* [n_nodes * 8] canonical child ids, -1 for EMPTY                  */
+    int32_t *roots;     /* [n_trees] canonical root id, -1 for an EMPTY tree                */
+    uint64_t capacity;  /* number of node entries the arrays above can hold                 */
+} vx_canonical;
+
+/* ---- interner ----------------------------------------------------------------------------- */
+/* VoxInterner::<T>::with_memory_budget(budget) (interner/mod.rs:45). voxel_bits is 8 or 16.
+ * patch_flags is a VX_PATCH_* mask. table_log2 = 0 sizes the device branch table
+ * automatically (2 x capacity slots, rounded up to a power of two). */
+int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_flags,
+                       int table_log2, vx_interner **out);
+int vx_interner_destroy(vx_interner *it);
+/* Orders all later work of this interner on `cuda_stream` (a cudaStream_t; NULL = the
+ * interner's own stream). */
+int vx_interner_set_stream(vx_interner *it, void *cuda_stream);
+/* Waits for the interner's stream and returns the first sticky device error as a status. */
+int vx_interner_sync(vx_interner *it);
+int vx_interner_stats_get(vx_interner *it, vx_interner_stats *out);
+/* VoxInterner::get_ref (interner/mod.rs:222-233); VX_E_INVALID_ARG for a stale id. */
+int vx_get_ref(vx_interner *it, uint64_t block_id, uint32_t *out);
+/* Copies of the value stored for a node (leaf value or branch LOD value). */
+int vx_get_value(vx_interner *it, uint64_t block_id, uint32_t *out);
+/* Human-readable text of the last error reported by this interner (never NULL). */
+const char *vx_last_error(vx_interner *it);
+
+/* ---- trees (VoxTree, voxtree.rs:108-142) -------------------------------------------------- */
+int vx_tree_create(vx_interner *it, int max_depth, vx_tree *out);
+/* Creates n trees at once; depths[i] per tree. */
+int vx_trees_create(vx_interner *it, uint32_t n, const uint8_t *depths, vx_tree *out);
+/* Releases the tree's root (dec_ref_recursive) and frees the handle. The reference has no Drop
+ * on VoxTree; this is VoxTree::clear followed by forgetting the tree. */
+int vx_tree_destroy(vx_interner *it, vx_tree tree);
+int vx_tree_root(vx_interner *it, vx_tree tree, uint64_t *out_root);
+int vx_tree_max_depth(vx_interner *it, vx_tree tree, int *out);
+/* VoxOpsRead::get (voxtree.rs:145-159). *found = 0 for an empty voxel. */
+int vx_tree_get(vx_interner *it, vx_tree tree, int32_t x, int32_t y, int32_t z, int *found,
+                uint32_t *value);
+/* VoxOpsWrite::set (voxtree.rs:163-260): single-voxel set; value 0 removes the voxel. */
+int vx_tree_set(vx_interner *it, vx_tree tree, int32_t x, int32_t y, int32_t z,
+                uint32_t value, int *changed);
+/* VoxOpsBulkWrite::fill / clear (voxtree.rs:264-292). */
+int vx_tree_fill(vx_interner *it, vx_tree tree, uint32_t value);
+int vx_tree_clear(vx_interner *it, vx_tree tree);
+
+/* ---- batches (Batch<T>, core/batch.rs) ----------------------------------------------------- */
+/* Batch::new(MaxDepth) (batch.rs:63-81); the depth cap follows patch_flags (P2) like the
+ * interner's. */
+int vx_batch_create(int max_depth, int voxel_bits, uint32_t patch_flags, vx_batch **out);
+int vx_batch_destroy(vx_batch *b);
+/* Batch::just_set (batch.rs:145-172): last write to a voxel wins; value 0 records a clear. */
+int vx_batch_set(vx_batch *b, int32_t x, int32_t y, int32_t z, uint32_t value);
+/* Batch::just_fill (batch.rs:178-184). */
+int vx_batch_fill(vx_batch *b, uint32_t value);
+/* Batch::just_clear (batch.rs:187-195). */
+int vx_batch_clear(vx_batch *b);
+/* just_set over every voxel of a dense grid laid out [y][z][x] (utils/common.rs:229-230),
+ * elements of the batch's voxel width. */
+int vx_batch_set_dense(vx_batch *b, const void *grid);
+/* Batch::size (batch.rs:115-123) and Batch::has_patches (batch.rs:126-132). */
+int vx_batch_size(const vx_batch *b, uint64_t *out);
+int vx_batch_has_patches(const vx_batch *b, int *out);
+
+/* ---- the hot path ---------------------------------------------------------------------- */
+/* VoxOpsBatch::apply_batch (voxtree.rs:303-328). *changed mirrors its bool result. */
+int vx_apply_batch(vx_interner *it, vx_tree tree, const vx_batch *batch, int *changed);
+/* n independent apply_batch calls on distinct trees sharing the interner, in one batched device
+ * pass; the result equals applying them one after the other in index order. */
+int vx_apply_batches(vx_interner *it, uint32_t n, const vx_tree *trees,
+                     const vx_batch *const *batches, uint8_t *changed);
+/* Dense-chunk construction: for each i, a Batch filled by just_set from grids[i] (a dense
+ * [y][z][x] grid of 2^(3*max_depth) voxels of the interner's width, grids packed back to back)
+ * applied to trees[i]. All trees must share one max_depth. `changed` (n bytes) may be NULL.
+ * trees/grids/changed live in `mem`. */
+int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void *grids,
+                   uint8_t *changed, vx_mem mem);
+/* Asynchronous form of vx_build_dense with all arguments in device memory. */
+int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
+                         const void *grids_dev, uint8_t *changed_dev);
+/* Batched VoxOpsRead::get: query i reads tree trees[i] at xyz[3i..3i+2]. found[i] = 0/1,
+ * values[i] has the interner's voxel width (uint8_t or uint16_t elements). Out-of-bounds
+ * positions report VX_E_OOB (and found = 0). */
+int vx_get_many(vx_interner *it, uint64_t n, const vx_tree *trees, const int32_t *xyz,
+                uint8_t *found, void *values, vx_mem mem);
+int vx_get_many_async(vx_interner *it, uint64_t n, const vx_tree *trees_dev,
+                      const int32_t *xyz_dev, uint8_t *found_dev, void *values_dev);
+
+/* ---- verification helpers (not on the timed path) ---------------------------------------- */
+/* Canonical DFS export of the DAG reachable from `trees` (see vx_canonical). On VX_E_BUFFER
+ * *n_nodes holds the required capacity. */
+int vx_export_canonical(vx_interner *it, uint32_t n_trees, const vx_tree *trees,
+                        vx_canonical *out, uint64_t *n_nodes);
+/* to_vec (utils/common.rs:158-246): dense [y][z][x] grid of the tree, voxel-width elements. */
+int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid);
+/* Checks every child reachable from the given trees: generation matches its slot and the
+ * refcount is positive. VX_E_REF_UB when a dangling child is found. */
+int vx_validate(vx_interner *it, uint32_t n_trees, const vx_tree *trees);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VOXELIS_GB300_H */
