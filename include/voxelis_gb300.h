@@ -171,9 +171,12 @@ int vx_apply_batches(vx_interner *it, uint32_t n, const vx_tree *trees,
  * trees/grids/changed live in `mem`. */
 int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void *grids,
                    uint8_t *changed, vx_mem mem);
-/* Asynchronous form of vx_build_dense with all arguments in device memory. */
+/* Asynchronous form of vx_build_dense for trees that are EMPTY (freshly created, cleared or after
+ * vx_interner_reset), all arguments in device memory and every tree of depth max_depth (checked on
+ * the device: a mismatch reports VX_E_INVALID_ARG at the next sync). No host synchronisation, so
+ * the call can be captured in a CUDA graph. */
 int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
-                         const void *grids_dev, uint8_t *changed_dev);
+                         const void *grids_dev, uint8_t *changed_dev, int max_depth);
 /* Batched VoxOpsRead::get: query i reads tree trees[i] at xyz[3i..3i+2]. found[i] = 0/1,
  * values[i] has the interner's voxel width (uint8_t or uint16_t elements). Out-of-bounds
  * positions report VX_E_OOB (and found = 0). */
@@ -192,6 +195,27 @@ int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid);
 /* Checks every child reachable from the given trees: generation matches its slot and the
  * refcount is positive. VX_E_REF_UB when a dangling child is found. */
 int vx_validate(vx_interner *it, uint32_t n_trees, const vx_tree *trees);
+
+/* ---- instrumentation and maintenance (no counterpart in the reference) ------------------- */
+/* Phases timed with CUDA events on the interner's stream while profiling is enabled. */
+#define VX_PROF_DENSE 0    /* fused dense-chunk kernel (blocks of up to 32^3 voxels)          */
+#define VX_PROF_LEVELS 1   /* fresh levels above 32^3 blocks (depth > 5)                       */
+#define VX_PROF_REFCOUNT 2 /* end-of-epoch refcount pass and allocator update                  */
+#define VX_PROF_APPLY 3    /* batched apply: bottom groups and level passes                    */
+#define VX_PROF_RELEASE 4  /* breadth-first release of replaced roots                          */
+#define VX_PROF_GET 5      /* batched gets                                                     */
+#define VX_PROF_COPY 6     /* host<->device copies made inside an entry point                  */
+#define VX_PROF_N 8
+int vx_profile_enable(vx_interner *it, int on);
+/* Waits for the stream and returns, per phase, the summed milliseconds and the number of timed
+ * intervals since the last collect; then starts a new collection. */
+int vx_profile_collect(vx_interner *it, double *ms, uint64_t *count);
+/* Number of kernels this library has launched in this process. */
+uint64_t vx_kernel_launches(void);
+/* Returns the interner to its freshly created state (no nodes, empty tables); tree handles stay
+ * valid and their roots become EMPTY. Same result as destroying it and creating a new interner with
+ * the same budget, without reallocating device memory. */
+int vx_interner_reset(vx_interner *it);
 
 #ifdef __cplusplus
 }

@@ -5,8 +5,10 @@
 // Reference panics become VX_E_REF_PANIC / VX_E_OOM / VX_E_OOB, reference undefined behaviour
 // becomes VX_E_REF_UB; the message is available from vxo_last_error.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <memory>
+#include <thread>
 #include <unordered_map>
 
 #include "../include/voxelis_gb300.h"
@@ -500,6 +502,52 @@ int vxo_time_build_dense(void *h, uint32_t n, const uint32_t *trees, const void 
     auto t1 = std::chrono::steady_clock::now();
     *seconds = std::chrono::duration<double>(t1 - t0).count();
     return st;
+}
+
+// The reference's many-chunks pattern on all host threads (voxelis-voxelize src/lib.rs:284-361):
+// per-chunk Batches are filled in parallel, then applied one after another to the shared interner
+// (apply_batch needs &mut VoxInterner). Returns the seconds of both phases.
+int vxo_build_dense_mt(void *h, uint32_t n, const uint32_t *trees, const void *grids, int threads,
+                       double *fill_seconds, double *apply_seconds) {
+    return with_interner(h, [&](auto &o) {
+        using T = std::decay_t<decltype(o.it.get_value(0))>;
+        if (n == 0) return VX_OK;
+        const int d = o.tree(trees[0])->max_depth();
+        const size_t per = (size_t)1 << (3 * d);
+        const int32_t side = 1 << d;
+        const T *g = static_cast<const T *>(grids);
+        std::vector<std::unique_ptr<vxo::Batch<T>>> batches(n);
+        auto t0 = std::chrono::steady_clock::now();
+        std::atomic<uint32_t> next{0};
+        std::atomic<int> failed{0};
+        auto worker = [&]() {
+            for (;;) {
+                uint32_t i = next.fetch_add(1);
+                if (i >= n) break;
+                try {
+                    auto b = std::make_unique<vxo::Batch<T>>(d, o.flags);
+                    const T *grid = g + per * i;
+                    for (int32_t y = 0; y < side; ++y)
+                        for (int32_t z = 0; z < side; ++z)
+                            for (int32_t x = 0; x < side; ++x)
+                                b->just_set(x, y, z, grid[((size_t)y * side + z) * side + x]);
+                    batches[i] = std::move(b);
+                } catch (...) {
+                    failed = 1;
+                }
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int k = 0; k < std::max(1, threads); ++k) pool.emplace_back(worker);
+        for (auto &t : pool) t.join();
+        if (failed) return VX_E_REF_PANIC;
+        auto t1 = std::chrono::steady_clock::now();
+        for (uint32_t i = 0; i < n; ++i) o.tree(trees[i])->apply_batch(o.it, *batches[i]);
+        auto t2 = std::chrono::steady_clock::now();
+        *fill_seconds = std::chrono::duration<double>(t1 - t0).count();
+        *apply_seconds = std::chrono::duration<double>(t2 - t1).count();
+        return VX_OK;
+    });
 }
 
 }  // extern "C"

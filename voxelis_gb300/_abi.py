@@ -36,6 +36,9 @@ VX_PATCH_P4 = 1 << 3
 VX_MEM_HOST = 0
 VX_MEM_DEVICE = 1
 
+VX_PROF_NAMES = ["dense", "levels", "refcount", "apply", "release", "get", "copy", "unused"]
+VX_PROF_N = 8
+
 VX_BLOCK_EMPTY = 0
 VX_BLOCK_INVALID = 0xFFFFFFFFFFFFFFFF
 
@@ -126,10 +129,13 @@ SIGNATURES = {
 
 # entry points only the GPU library has
 GPU_SIGNATURES = {
+    "profile_enable": [_P, _I],
+    "profile_collect": [_P, C.POINTER(C.c_double), _PU64],
+    "interner_reset": [_P],
     "interner_set_stream": [_P, _P],
     "interner_sync": [_P],
     "trees_create": [_P, _U32, _P, _P],
-    "build_dense_async": [_P, _U32, _P, _P, _P],
+    "build_dense_async": [_P, _U32, _P, _P, _P, _I],
     "get_many_async": [_P, _U64, _P, _P, _P, _P],
 }
 
@@ -150,6 +156,11 @@ class NativeLib:
             f.argtypes = argtypes
             f.restype = C.c_int
             self._fns[name] = f
+        if hasattr(self.lib, prefix + "kernel_launches"):
+            kl = getattr(self.lib, prefix + "kernel_launches")
+            kl.argtypes = []
+            kl.restype = C.c_uint64
+            self.kernel_launches = kl
         le = getattr(self.lib, prefix + "last_error")
         le.argtypes = [_P]
         le.restype = C.c_char_p

@@ -1,0 +1,571 @@
+// Batched VoxTree::apply_batch over many trees sharing one interner, level-synchronous on the GPU.
+//
+// Restates set_batch_at_depth_iterative (spatial/voxtree.rs:724-1118) for n trees at once:
+//   prep     Phase 0 fill (voxtree.rs:742-758): the fill leaf replaces the old root as the
+//            starting node; without patches it is the new root.
+//   bottom   Phase 1 (voxtree.rs:770-897), one thread per touched bottom group: descend the old
+//            tree to depth d-1, collapse a full uniform group to a leaf, otherwise merge the set
+//            voxels into the existing children (or into 8 copies of an ancestor leaf) and
+//            hash-cons the branch. Groups that change nothing drop out, as in the reference.
+//   levels   Phase 2 (voxtree.rs:905-1106), one step per level for all trees together: entries
+//            are kept sorted by (tree, path), so the siblings of one parent form a run; run heads
+//            are found by comparing sibling prefixes (PATH_MASKS), numbered by a prefix scan,
+//            and each parent gathers its run, clones the untouched children of the old parent or
+//            replicates an ancestor leaf, collapses 8 equal leaves, and hash-conses the result.
+//   finish   apply_batch (voxtree.rs:303-328): commit the new root, queue the old root for
+//            release, report assert_ne!(new_root, old_root) as a reference panic.
+// Clear pass (P4). The reference ignores Batch clear bits (voxtree.rs:779). With P4 they are
+// honoured as VoxTree::set(pos, 0) for every cleared voxel after the set phase (remove_at_depth,
+// voxtree.rs:542-706). Those removals commute, so the same level-synchronous machinery applies them
+// in one pass (mode 1): a touched group drops its cleared children (or splits an ancestor leaf into
+// 8 copies minus the cleared ones), a parent takes the new children over the old node's children
+// (or over 8 copies of an ancestor leaf), clears their types bits, drops children that became
+// EMPTY from its mask, and becomes EMPTY itself when its mask empties. Nothing collapses. The
+// removal path is refcount-exact, so no correction applies.
+// Trees are processed deepest first, so the trees whose root is produced at a step are the tail
+// of that step's list and the next list is a prefix of the parents.
+//
+// Refcounts. After the build every count is the in-degree from newly created nodes plus tree roots
+// (counted once per epoch over the allocation log), plus these corrections, which reproduce where
+// the reference's increments differ from the references its nodes hold:
+//   Q5 (voxtree.rs:835-839, 846-868): an ancestor leaf is charged 8 - |set| references, but only
+//      8 - |modified| slots keep it: + (|modified| - |set|), or + (8 - |set|) when nothing changed.
+//   Q6 (voxtree.rs:1062-1072): a collapse with c cloned children gives back min(c, 7) instead of
+//      7 - c references: + (7 - 2c).
+//   Q7 (voxtree.rs:742-758): the fill leaf's Phase-0 reference is never released when the batch
+//      also has patches: + 1.
+#include "vx_launch.h"
+
+namespace vxg {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kScanPer = 8;
+constexpr int kScanBlock = kThreads * kScanPer;
+
+__device__ __forceinline__ void add_ref_delta(const DevInterner &I, uint64_t id, int delta) {
+    if (delta != 0 && id != EMPTY_ID) atomicAdd(I.refcount + id_index(id), (unsigned)delta);
+}
+
+__global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_items) return;
+    const uint32_t t = a.it_tree[i];
+    const uint64_t old = I.roots[t];
+    const uint8_t f = a.it_flags[i];
+    uint64_t init = old;
+    a.it_old[i] = old;
+    if (a.mode == 1) {  // the clear pass starts from the root the set phase left
+        a.it_init[i] = old;
+        a.it_new[i] = INVALID_ID;
+        return;
+    }
+    a.it_panic[i] = 0;
+    if (f & 1) {
+        bool created;
+        const uint64_t fill = intern_leaf(I, a.it_fill[i], &created);
+        init = fill;
+        if (f & 2) add_ref_delta(I, fill, 1);  // Q7
+    }
+    a.it_init[i] = init;
+    a.it_new[i] = (f & 2) ? INVALID_ID : init;
+}
+
+__global__ void __launch_bounds__(kThreads) bottom_kernel(DevInterner I, ApplyArgs a) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.n_records; base += stride) {
+        const uint64_t r = base + threadIdx.x;
+        bool active = r < a.n_records;
+        uint32_t i = 0, set = 0, changed = 0;
+        int d = 0;
+        uint64_t cur = EMPTY_ID, anc = EMPTY_ID, out = EMPTY_ID;
+        uint32_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        uint64_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        uint32_t cv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        uint32_t types = 0, mask = 0, lod = 0;
+        bool want_branch = false;
+        if (active) {
+            i = a.rec_item[r];
+            d = a.it_depth[i];
+            set = a.mode ? a.rec_clear[r] : a.rec_set[r];
+            if (set == 0 || a.it_panic[i]) active = false;
+        }
+        bool uniform = false;
+        if (active) {
+            const uint32_t path = a.rec_group[r] << 3;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = a.rec_vals[8 * r + k];
+            // descend to depth d-1 (voxtree.rs:792-822)
+            cur = a.it_init[i];
+            for (int cd = 0; cd < d - 1; ++cd) {
+                if (id_is_branch(cur)) {
+                    const uint32_t idx = (path >> (3 * (d - cd - 1))) & 7u;
+                    cur = I.children[8ull * id_index(cur) + idx];
+                } else {
+                    anc = cur;
+                    cur = EMPTY_ID;
+                }
+                if (cur == EMPTY_ID) break;
+            }
+            uniform = set == 0xFF;
+#pragma unroll
+            for (int k = 1; k < 8; ++k) uniform = uniform && v[k] == v[0];
+            if (cur != EMPTY_ID && id_is_leaf(cur)) {
+                if ((I.flags & 1u) || a.mode == 1) {  // P1 (removals always split a leaf)
+                    anc = cur;
+                    cur = EMPTY_ID;
+                } else if (!uniform) {  // the reference panics in BlockId::types()
+                    a.it_panic[i] = 1;
+                    set_error(I, ERR_REF_PANIC, 40);
+                    active = false;
+                }
+            }
+        }
+        if (active && a.mode == 1) {  // remove_at_depth_branch / _leaf at depth d-1
+            uint32_t modified = 0;
+            if (cur != EMPTY_ID) {
+                const uint64_t *src = I.children + 8ull * id_index(cur);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    c[k] = src[k];
+                    cv[k] = c[k] ? node_value(I, id_index(c[k])) : 0;
+                }
+                types = id_types(cur);
+                mask = id_mask(cur);
+                modified = set & mask;
+            } else if (anc != EMPTY_ID) {
+                const uint32_t av = node_value(I, id_index(anc));
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    c[k] = anc;
+                    cv[k] = av;
+                }
+                types = mask = 0xFF;
+                modified = set;
+            }
+            if (modified) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if ((modified >> k) & 1) {
+                        c[k] = EMPTY_ID;
+                        cv[k] = 0;
+                    }
+                types &= ~modified;
+                mask &= ~modified;
+                changed = 1;
+                if (mask) {
+                    want_branch = true;
+                    lod = calc_average8(cv);
+                }
+            }
+        } else if (active && uniform) {  // voxtree.rs:826, 887-896
+            bool created;
+            out = intern_leaf(I, v[0], &created);
+            lod = v[0];
+            changed = 1;
+        } else if (active) {  // voxtree.rs:829-883
+            if (cur != EMPTY_ID) {
+                const uint64_t *src = I.children + 8ull * id_index(cur);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    c[k] = src[k];
+                    cv[k] = c[k] ? node_value(I, id_index(c[k])) : 0;
+                }
+                types = id_types(cur);
+                mask = id_mask(cur);
+            } else if (anc != EMPTY_ID) {
+                const uint32_t av = node_value(I, id_index(anc));
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    c[k] = anc;
+                    cv[k] = av;
+                }
+                types = mask = 0xFF;
+            }
+            uint32_t modified = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!((set >> k) & 1)) continue;
+                if (c[k] != EMPTY_ID && cv[k] == v[k]) continue;
+                bool created;
+                c[k] = intern_leaf(I, v[k], &created);
+                cv[k] = v[k];
+                types |= 1u << k;
+                mask |= 1u << k;
+                modified |= 1u << k;
+            }
+            if (anc != EMPTY_ID && cur == EMPTY_ID) {  // Q5
+                const int ds = __popc(set), dm = __popc(modified);
+                add_ref_delta(I, anc, modified ? dm - ds : 8 - ds);
+            }
+            if (modified) {
+                want_branch = true;
+                lod = calc_average8(cv);
+                changed = 1;
+            }
+        }
+        bool created;
+        const uint64_t id = warp_intern_branch(I, want_branch, c, types, mask, lod, &created);
+        if (want_branch) out = id;
+        if (r < a.n_records) {
+            a.flags[r] = changed;
+            a.rec_id[r] = out;
+            a.rec_val[r] = lod;
+        }
+    }
+}
+
+// Exclusive scan of n flags: per-block scan, scan of block sums, add-back. pos[n] = total.
+__global__ void __launch_bounds__(kThreads) scan_blocks_kernel(const uint32_t *in, uint32_t *out, uint32_t *sums,
+                                                              uint32_t n) {
+    __shared__ uint32_t warp_tot[kThreads / 32];
+    const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanPer;
+    uint32_t x[kScanPer];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        x[k] = (base + k < n) ? in[base + k] : 0u;
+        local += x[k];
+    }
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (unsigned)o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kThreads / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (unsigned)o) w += y;
+        }
+        if (lane < kThreads / 32) warp_tot[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = incl - local + (warp ? warp_tot[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += x[k];
+    }
+    if (threadIdx.x == kThreads - 1) sums[blockIdx.x] = warp_tot[kThreads / 32 - 1];
+}
+
+__global__ void scan_add_kernel(uint32_t *out, const uint32_t *sums, uint32_t n) {
+    const uint32_t b = blockIdx.x;
+    if (b == 0) return;
+    const uint32_t add = sums[b];
+    const uint32_t base = b * kScanBlock;
+    for (uint32_t k = threadIdx.x; k < kScanBlock; k += blockDim.x)
+        if (base + k < n) out[base + k] += add;
+}
+
+__global__ void scan_total_kernel(const uint32_t *in, uint32_t *out, uint32_t n) {
+    out[n] = n ? out[n - 1] + in[n - 1] : 0u;
+}
+
+__global__ void scatter_bottom_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) I.ctr->scratch[SC_ENTRIES] = a.pos[a.n_records];
+    if (r >= a.n_records || !a.flags[r]) return;
+    const uint32_t e = a.pos[r];
+    a.e_item[0][e] = a.rec_item[r];
+    a.e_path[0][e] = a.rec_group[r] << 3;
+    a.e_id[0][e] = a.rec_id[r];
+    a.e_val[0][e] = a.rec_val[r];
+}
+
+__device__ __forceinline__ uint32_t parent_key_path(uint32_t path, int d, int t) {
+    return t == 1 ? 0u : (path & path_mask(d, t - 2));
+}
+
+__global__ void heads_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n_records) return;
+    const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
+    uint32_t head = 0;
+    if (j < count) {
+        const uint32_t i = a.e_item[buf][j];
+        const int d = a.it_depth[i];
+        const int t = d - step;
+        head = 1;
+        if (j > 0) {
+            const uint32_t ip = a.e_item[buf][j - 1];
+            if (ip == i && parent_key_path(a.e_path[buf][j - 1], d, t) == parent_key_path(a.e_path[buf][j], d, t))
+                head = 0;
+        }
+    }
+    a.flags[j] = head;
+}
+
+__global__ void starts_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
+    if (j == 0) {
+        const uint32_t np = a.pos[a.n_records];
+        a.p_start[np] = count;
+        I.ctr->scratch[SC_PARENTS] = np;
+        I.ctr->scratch[SC_ROOTS] = 0;
+    }
+    if (j < count && a.flags[j]) a.p_start[a.pos[j]] = j;
+}
+
+__global__ void __launch_bounds__(kThreads) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    const uint32_t n_par = (uint32_t)I.ctr->scratch[SC_PARENTS];
+    const int nb = buf ^ 1;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_par; base += stride) {
+        const uint64_t p = base + threadIdx.x;
+        const bool in = p < n_par;
+        uint64_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        uint32_t cv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        uint32_t types = 0, mask = 0, lod = 0;
+        uint32_t i = 0, path0 = 0;
+        int d = 0, t = 0;
+        bool want_branch = false;
+        uint64_t out = EMPTY_ID;
+        uint32_t out_val = 0;
+        if (in) {
+            const uint32_t b = a.p_start[p], e = a.p_start[p + 1];
+            i = a.e_item[buf][b];
+            d = a.it_depth[i];
+            t = d - step;
+            path0 = a.e_path[buf][b];
+            // the old node at the parent's place (voxtree.rs:934-952)
+            uint64_t eq = a.it_init[i], leaf = EMPTY_ID;
+            for (int cd = 0; cd + 1 < t; ++cd) {
+                if (id_is_leaf(eq)) {
+                    leaf = eq;
+                    eq = EMPTY_ID;
+                    break;
+                }
+                const uint32_t idx = (path0 >> (3 * (d - cd - 1))) & 7u;
+                eq = I.children[8ull * id_index(eq) + idx];
+                if (eq == EMPTY_ID) break;
+            }
+            if (id_is_leaf(eq)) {
+                leaf = eq;
+                eq = EMPTY_ID;
+            }
+            // gather the run of new children (voxtree.rs:959-1000)
+            for (uint32_t j = b; j < e; ++j) {
+                const uint32_t ti = (a.e_path[buf][j] >> (3 * (d - t))) & 7u;
+                const uint64_t id = a.e_id[buf][j];
+                c[ti] = id;
+                cv[ti] = a.e_val[buf][j];
+                types |= (id_is_leaf(id) ? 1u : 0u) << ti;
+                mask |= 1u << ti;
+            }
+            if (a.mode == 1) {  // remove_at_depth_branch / _leaf one level up (voxtree.rs:559-706)
+                const uint32_t ch = mask;
+                uint64_t nc[8];
+                uint32_t nv[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    nc[k] = c[k];
+                    nv[k] = cv[k];
+                }
+                if (eq != EMPTY_ID) {
+                    const uint64_t *src = I.children + 8ull * id_index(eq);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        c[k] = src[k];
+                        cv[k] = c[k] ? node_value(I, id_index(c[k])) : 0;
+                    }
+                    types = id_types(eq) & ~ch;
+                    mask = id_mask(eq);
+                } else if (leaf != EMPTY_ID) {
+                    const uint32_t lv = node_value(I, id_index(leaf));
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        c[k] = leaf;
+                        cv[k] = lv;
+                    }
+                    types = 0xFFu & ~ch;
+                    mask = 0xFF;
+                } else {
+                    set_error(I, ERR_INTERNAL, 45);
+                    types = 0;
+                    mask = 0;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if ((ch >> k) & 1) {
+                        c[k] = nc[k];
+                        cv[k] = nv[k];
+                        if (nc[k] == EMPTY_ID)
+                            mask &= ~(1u << k);
+                        else
+                            mask |= 1u << k;
+                    }
+                if (mask) {
+                    want_branch = true;
+                    lod = calc_average8(cv);
+                } else {
+                    out = EMPTY_ID;
+                    out_val = 0;
+                }
+            } else {
+                const uint32_t existing_mask = eq != EMPTY_ID ? id_mask(eq) : 0u;
+                const uint32_t inv = (~mask) & 0xFFu;
+                const uint32_t cloned = existing_mask & inv;
+                if (mask != 0xFF) {
+                    if (cloned) {  // voxtree.rs:1017-1031
+                        const uint64_t *src = I.children + 8ull * id_index(eq);
+    #pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            if (!((cloned >> k) & 1)) continue;
+                            c[k] = src[k];
+                            cv[k] = c[k] ? node_value(I, id_index(c[k])) : 0;
+                            types |= (id_is_leaf(c[k]) ? 1u : 0u) << k;
+                            mask |= 1u << k;
+                        }
+                    } else if (leaf != EMPTY_ID) {  // voxtree.rs:1032-1047
+                        const uint32_t lv = node_value(I, id_index(leaf));
+    #pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if ((inv >> k) & 1) {
+                                c[k] = leaf;
+                                cv[k] = lv;
+                            }
+                        types |= inv;
+                        mask |= inv;
+                    }
+                }
+                bool same = types == 0xFF;
+    #pragma unroll
+                for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
+                if (same) {  // voxtree.rs:1062-1075
+                    out = c[0];
+                    out_val = cv[0];
+                    if (cloned) add_ref_delta(I, c[0], 7 - 2 * __popc(cloned));  // Q6
+                } else {
+                    want_branch = true;
+                    lod = calc_average8(cv);
+                }
+            }
+            }
+        bool created;
+        const uint64_t id = warp_intern_branch(I, want_branch, c, types, mask, lod, &created);
+        if (!in) continue;
+        if (want_branch) {
+            out = id;
+            out_val = lod;
+        }
+        if (t == 1) {
+            a.it_new[i] = out;
+            atomicAdd(&I.ctr->scratch[SC_ROOTS], 1ull);
+        } else {
+            a.e_item[nb][p] = i;
+            a.e_path[nb][p] = path0 & path_mask(d, t - 2);
+            a.e_id[nb][p] = out;
+            a.e_val[nb][p] = out_val;
+        }
+    }
+}
+
+__global__ void next_count_kernel(DevInterner I) {
+    I.ctr->scratch[SC_ENTRIES] = I.ctr->scratch[SC_PARENTS] - I.ctr->scratch[SC_ROOTS];
+}
+
+__global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_items) return;
+    if (a.mode == 1) {
+        const uint64_t nw = a.it_new[i], old = a.it_old[i];
+        if (nw == INVALID_ID) return;
+        if (nw != EMPTY_ID) atomicAdd(I.refcount + id_index(nw), 1u);
+        if (old != EMPTY_ID) {
+            const unsigned long long e = atomicAdd(&I.ctr->scratch[SC_RELEASE], 1ull);
+            a.release_list[e] = old;
+        }
+        I.roots[a.it_tree[i]] = nw;
+        a.it_changed[i] = 1;
+        return;
+    }
+    a.it_changed[i] = 0;
+    if (a.it_panic[i]) return;
+    const uint64_t nw = a.it_new[i], old = a.it_old[i];
+    if (nw == INVALID_ID) return;
+    const uint8_t f = a.it_flags[i];
+    if ((f & 3) && nw != EMPTY_ID) atomicAdd(I.refcount + id_index(nw), 1u);  // the tree's root reference
+    if (old != EMPTY_ID) {
+        if (nw == old) {  // assert_ne!(new_root_id, self.root_id) (voxtree.rs:311)
+            set_error(I, ERR_REF_PANIC, 41);
+            return;
+        }
+        const unsigned long long e = atomicAdd(&I.ctr->scratch[SC_RELEASE], 1ull);
+        a.release_list[e] = old;
+    }
+    I.roots[a.it_tree[i]] = nw;
+    a.it_changed[i] = 1;
+}
+
+__global__ void zero_counter_kernel(DevInterner I, int slot) { I.ctr->scratch[slot] = 0; }
+
+}  // namespace
+
+size_t scan_tmp_words(uint32_t n) { return (size_t)(n + kScanBlock - 1) / kScanBlock + 32; }
+
+cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s) {
+    const uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb == 0) {
+        count_launches(1);
+        scan_total_kernel<<<1, 1, 0, s>>>(flags, pos, 0);
+        return cudaGetLastError();
+    }
+    count_launches(1);
+    scan_blocks_kernel<<<nb, kThreads, 0, s>>>(flags, pos, tmp, n);
+    if (nb > 1) {
+        uint32_t *tmp2 = tmp + nb;  // scan of the block sums (recursive)
+        cudaError_t e = launch_scan(tmp, tmp2, tmp2 + nb + 1 + 32, nb, s);
+        if (e != cudaSuccess) return e;
+        count_launches(1);
+        scan_add_kernel<<<nb, kThreads, 0, s>>>(pos, tmp2, n);
+    }
+    count_launches(1);
+    scan_total_kernel<<<1, 1, 0, s>>>(flags, pos, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
+    const unsigned ib = (a.n_items + kThreads - 1) / kThreads;
+    count_launches(1);
+    prep_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
+    const uint32_t R = a.n_records;
+    const unsigned rb = (R + kThreads - 1) / kThreads;
+    if (R) {
+        unsigned g = rb < (unsigned)num_sms * 8 ? rb : (unsigned)num_sms * 8;
+        count_launches(1);
+        bottom_kernel<<<g, kThreads, 0, s>>>(I, a);
+        cudaError_t e = launch_scan(a.flags, a.pos, a.scan_tmp, R, s);
+        if (e != cudaSuccess) return e;
+        count_launches(1);
+        scatter_bottom_kernel<<<rb, kThreads, 0, s>>>(I, a);
+        int buf = 0;
+        for (int step = 1; step <= a.max_depth - 1; ++step) {
+            count_launches(1);
+            heads_kernel<<<rb, kThreads, 0, s>>>(I, a, step, buf);
+            e = launch_scan(a.flags, a.pos, a.scan_tmp, R, s);
+            if (e != cudaSuccess) return e;
+            count_launches(1);
+            starts_kernel<<<rb, kThreads, 0, s>>>(I, a);
+            count_launches(1);
+            parents_kernel<<<g, kThreads, 0, s>>>(I, a, step, buf);
+            count_launches(1);
+            next_count_kernel<<<1, 1, 0, s>>>(I);
+            buf ^= 1;
+        }
+    }
+    count_launches(1);
+    zero_counter_kernel<<<1, 1, 0, s>>>(I, SC_RELEASE);
+    count_launches(1);
+    finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
+    return cudaGetLastError();
+}
+
+}  // namespace vxg

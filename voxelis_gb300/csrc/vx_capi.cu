@@ -1,0 +1,1271 @@
+// Host implementation of the C ABI declared in include/voxelis_gb300.h.
+//
+// Owns the device interner (vx_device.cuh), the device tree table (roots + depths), a growable
+// device workspace for the batched paths, pinned staging for host<->device copies, and the host
+// Batch buffers. Every entry point returns a status; device failures are sticky error bits that are
+// read back at the synchronising calls.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/voxelis_gb300.h"
+#include "vx_launch.h"
+
+using namespace vxg;
+
+namespace vxg {
+size_t dense_smem_bytes(int bdepth, int vbytes);
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}
+
+// ---- host Batch<T> (core/batch.rs:39-240) ------------------------------------------------------
+struct vx_batch {
+    int depth = 0;
+    int vbits = 8;
+    uint32_t flags = 0;
+    uint64_t groups = 0;
+    std::vector<uint8_t> set, clear;
+    std::vector<uint8_t> vals;  // groups * 8 voxels of vbits/8 bytes
+    bool has_fill = false;
+    uint32_t fill = 0;
+    bool has_patches = false;
+};
+
+namespace {
+
+constexpr uint32_t kStickyMask = ERR_OOM | ERR_TABLE_FULL | ERR_TIMEOUT | ERR_INTERNAL | ERR_REF_UB;
+constexpr uint8_t kUnused = TREE_UNUSED;
+
+uint32_t morton_encode(int32_t x, int32_t y, int32_t z) {
+    auto split = [](uint32_t v) {
+        v &= 0x3FF;
+        v = (v | (v << 16)) & 0x30000FF;
+        v = (v | (v << 8)) & 0x300F00F;
+        v = (v | (v << 4)) & 0x30C30C3;
+        v = (v | (v << 2)) & 0x9249249;
+        return v;
+    };
+    return split((uint32_t)x) | (split((uint32_t)y) << 1) | (split((uint32_t)z) << 2);
+}
+
+int depth_limit(uint32_t flags) { return (flags & VX_PATCH_P2) ? 11 : 7; }
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = std::max(n, (size_t)1 << 20);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct Carve {
+    char *base;
+    size_t off = 0;
+    explicit Carve(void *b) : base((char *)b) {}
+    template <class T>
+    T *take(size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T *r = reinterpret_cast<T *>(base + off);
+        off += n * sizeof(T);
+        return r;
+    }
+    static size_t need(std::initializer_list<size_t> bytes) {
+        size_t s = 0;
+        for (size_t b : bytes) s = ((s + 255) & ~(size_t)255) + b;
+        return s + 256;
+    }
+};
+
+}  // namespace
+
+struct vx_interner {
+    int vbits = 8;
+    uint32_t flags = 0;
+    uint64_t capacity = 0;
+    uint64_t node_size = 0;
+    uint64_t table_slots = 0;
+    DevInterner dev{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int num_sms = 148;
+    // tree table
+    uint32_t tree_cap = 0;
+    std::vector<uint8_t> tree_depth, tree_used, tree_maybe_nonempty;
+    std::vector<uint32_t> free_trees;
+    uint32_t tree_count = 0;
+    bool all_trees_unknown = false;
+    // device scratch
+    DevBuf ws;
+    DevBuf staging;  // host-memory arguments copied to the device
+    uint32_t *frontier = nullptr;  // 2 * capacity u32 (the single-thread queue aliases it under P3)
+    uint64_t *seq_queue = nullptr;
+    uint64_t seq_queue_cap = 0;
+    unsigned long long *d_live = nullptr;
+    int *d_status = nullptr;
+    // pinned staging
+    DevCounters *h_ctr = nullptr;
+    int *h_status = nullptr;
+    unsigned long long *h_live = nullptr;
+    std::string last_error;
+    // instrumentation: event pairs recorded around the phases while profiling is on
+    bool profile = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+namespace {
+
+cudaEvent_t take_event(vx_interner *it) {
+    if (!it->event_pool.empty()) {
+        cudaEvent_t e = it->event_pool.back();
+        it->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Records CUDA events around one phase on the interner's stream while profiling is enabled.
+struct Phase {
+    vx_interner *it;
+    int id;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Phase(vx_interner *i, int phase) : it(i), id(phase) {
+        if (!it->profile) return;
+        a = take_event(it);
+        b = take_event(it);
+        cudaEventRecord(a, it->stream);
+    }
+    ~Phase() {
+        if (!a) return;
+        cudaEventRecord(b, it->stream);
+        it->marks.push_back({id, {a, b}});
+    }
+};
+
+int set_err(vx_interner *it, int code, const std::string &msg) {
+    if (it) it->last_error = msg;
+    return code;
+}
+
+int cuda_fail(vx_interner *it, cudaError_t e, const char *where) {
+    return set_err(it, VX_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define VX_CUDA(call)                                    \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return cuda_fail(it, _e, #call); \
+    } while (0)
+
+// Waits for the stream, reads the counters and converts device error bits into a status.
+int sync_and_check(vx_interner *it) {
+    VX_CUDA(cudaMemcpyAsync(it->h_ctr, it->dev.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    const uint32_t err = it->h_ctr->error;
+    if (!err) return VX_OK;
+    const uint32_t keep = err & kStickyMask;  // OOB, INVALID and REF_PANIC leave the state usable
+    if (keep != err) {
+        VX_CUDA(cudaMemcpyAsync(&it->dev.ctr->error, &keep, sizeof(uint32_t), cudaMemcpyHostToDevice, it->stream));
+        VX_CUDA(cudaStreamSynchronize(it->stream));
+    }
+    const uint32_t info = it->h_ctr->error_info;
+    std::string where = " (site " + std::to_string(info) + ")";
+    if (err & ERR_OOM) return set_err(it, VX_E_OOM, "Out of memory: node capacity exhausted" + where);
+    if (err & ERR_TABLE_FULL) return set_err(it, VX_E_TABLE_FULL, "branch table probe limit reached" + where);
+    if (err & ERR_TIMEOUT) return set_err(it, VX_E_TIMEOUT, "bounded device wait gave up" + where);
+    if (err & ERR_INTERNAL) return set_err(it, VX_E_UNSUPPORTED, "internal consistency check failed" + where);
+    if (err & ERR_REF_UB) return set_err(it, VX_E_REF_UB, "reference undefined behaviour (refcount underflow or release-queue overflow)" + where);
+    if (err & ERR_REF_PANIC) return set_err(it, VX_E_REF_PANIC, "the reference panics on this input" + where);
+    if (err & ERR_INVALID) return set_err(it, VX_E_INVALID_ARG, "unknown tree handle or depth mismatch" + where);
+    if (err & ERR_OOB) return set_err(it, VX_E_OOB, "position out of bounds" + where);
+    return set_err(it, VX_E_UNSUPPORTED, "unknown device error" + where);
+}
+
+cudaError_t grow_tree_table(vx_interner *it, uint32_t need) {
+    if (need <= it->tree_cap) return cudaSuccess;
+    uint32_t cap = std::max<uint32_t>(1024, it->tree_cap);
+    while (cap < need) cap *= 2;
+    uint64_t *roots = nullptr;
+    uint8_t *depths = nullptr;
+    cudaError_t e = cudaMalloc(&roots, cap * sizeof(uint64_t));
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc(&depths, cap);
+    if (e != cudaSuccess) {
+        cudaFree(roots);
+        return e;
+    }
+    cudaMemsetAsync(roots, 0, cap * sizeof(uint64_t), it->stream);
+    cudaMemsetAsync(depths, kUnused, cap, it->stream);
+    if (it->dev.roots) {
+        cudaMemcpyAsync(roots, it->dev.roots, it->tree_cap * sizeof(uint64_t), cudaMemcpyDeviceToDevice, it->stream);
+        cudaMemcpyAsync(depths, it->dev.depths, it->tree_cap, cudaMemcpyDeviceToDevice, it->stream);
+        cudaStreamSynchronize(it->stream);
+        cudaFree(it->dev.roots);
+        cudaFree(it->dev.depths);
+    }
+    it->dev.roots = roots;
+    it->dev.depths = depths;
+    it->dev.tree_cap = cap;
+    it->tree_cap = cap;
+    it->tree_depth.resize(cap, kUnused);
+    it->tree_used.resize(cap, 0);
+    it->tree_maybe_nonempty.resize(cap, 0);
+    return cudaSuccess;
+}
+
+bool tree_ok(vx_interner *it, vx_tree t) { return t < it->tree_count && it->tree_used[t]; }
+
+bool value_fits(vx_interner *it, uint32_t v) { return it->vbits == 8 ? v <= 0xFFu : v <= 0xFFFFu; }
+
+// Host-side tree helpers -------------------------------------------------------------------------
+int read_root(vx_interner *it, vx_tree t, uint64_t *out) {
+    VX_CUDA(cudaMemcpyAsync(out, it->dev.roots + t, sizeof(uint64_t), cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    return VX_OK;
+}
+
+void maybe_rehash(vx_interner *it) {
+    if (it->h_ctr->tombstones * 4 > it->table_slots) {
+        launch_rehash(it->dev, it->table_slots, it->num_sms, it->stream);
+        cudaStreamSynchronize(it->stream);
+    }
+}
+
+// Snapshot of the node store for the verification helpers.
+struct Snapshot {
+    uint64_t n = 0;
+    std::vector<uint64_t> ids, children;
+    std::vector<uint32_t> values, refcount;
+    std::vector<uint16_t> generation;
+};
+
+int take_snapshot(vx_interner *it, Snapshot &s) {
+    int st = sync_and_check(it);
+    if (st != VX_OK && st != VX_E_REF_PANIC && st != VX_E_OOB) return st;
+    s.n = it->h_ctr->next_index;
+    s.ids.resize(s.n);
+    s.children.resize(s.n * 8);
+    s.refcount.resize(s.n);
+    s.generation.resize(s.n);
+    s.values.resize(s.n);
+    VX_CUDA(cudaMemcpy(s.ids.data(), it->dev.ids, s.n * 8, cudaMemcpyDeviceToHost));
+    VX_CUDA(cudaMemcpy(s.children.data(), it->dev.children, s.n * 64, cudaMemcpyDeviceToHost));
+    VX_CUDA(cudaMemcpy(s.refcount.data(), it->dev.refcount, s.n * 4, cudaMemcpyDeviceToHost));
+    VX_CUDA(cudaMemcpy(s.generation.data(), it->dev.generation, s.n * 2, cudaMemcpyDeviceToHost));
+    if (it->vbits == 8) {
+        std::vector<uint8_t> v(s.n);
+        VX_CUDA(cudaMemcpy(v.data(), it->dev.values, s.n, cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < s.n; ++i) s.values[i] = v[i];
+    } else {
+        std::vector<uint16_t> v(s.n);
+        VX_CUDA(cudaMemcpy(v.data(), it->dev.values, s.n * 2, cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < s.n; ++i) s.values[i] = v[i];
+    }
+    return VX_OK;
+}
+
+int read_roots(vx_interner *it, uint32_t n, const vx_tree *trees, std::vector<uint64_t> &roots) {
+    roots.resize(n);
+    std::vector<uint64_t> all(it->tree_count);
+    if (it->tree_count)
+        VX_CUDA(cudaMemcpy(all.data(), it->dev.roots, it->tree_count * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!tree_ok(it, trees[i])) return set_err(it, VX_E_INVALID_ARG, "unknown tree handle");
+        roots[i] = all[trees[i]];
+    }
+    return VX_OK;
+}
+
+// ---- the batched apply ---------------------------------------------------------------------------
+struct Item {
+    vx_tree tree;
+    const vx_batch *batch;
+    uint32_t caller_index;
+};
+
+int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
+    const uint32_t n = (uint32_t)items.size();
+    if (n == 0) return VX_OK;
+    std::stable_sort(items.begin(), items.end(),
+                     [&](const Item &a, const Item &b) { return it->tree_depth[a.tree] > it->tree_depth[b.tree]; });
+    int max_depth = 0;
+    uint64_t R = 0;
+    for (auto &x : items) {
+        max_depth = std::max(max_depth, (int)it->tree_depth[x.tree]);
+        const vx_batch *b = x.batch;
+        if (!b->has_patches) continue;
+        for (uint64_t g = 0; g < b->groups; ++g) R += (b->set[g] | b->clear[g]) != 0;
+    }
+    for (auto &x : items)
+        if (x.batch->has_patches && it->tree_depth[x.tree] < 2)
+            return set_err(it, VX_E_REF_PANIC, "batch apply needs max_depth >= 2 (usize underflow in the reference)");
+    if (R >= 0xFFFFFFF0ull) return set_err(it, VX_E_UNSUPPORTED, "too many touched groups in one call");
+    bool any_clear = false;
+
+    // host staging (pinned would be faster; these buffers are O(records))
+    std::vector<uint32_t> it_tree(n), it_fill(n), rec_item(R), rec_group(R);
+    std::vector<uint8_t> it_depth(n), it_flags(n), rec_set(R), rec_clear(R);
+    std::vector<uint16_t> rec_vals(R * 8);
+    uint64_t r = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const vx_batch *b = items[i].batch;
+        it_tree[i] = items[i].tree;
+        it_depth[i] = it->tree_depth[items[i].tree];
+        it_flags[i] = (b->has_fill ? 1 : 0) | (b->has_patches ? 2 : 0);
+        it_fill[i] = b->fill;
+        if (!b->has_patches) continue;
+        for (uint64_t g = 0; g < b->groups; ++g) {
+            if (!(b->set[g] | b->clear[g])) continue;
+            rec_item[r] = i;
+            rec_group[r] = (uint32_t)g;
+            rec_set[r] = b->set[g];
+            rec_clear[r] = b->clear[g];
+            any_clear |= b->clear[g] != 0;
+            for (int k = 0; k < 8; ++k)
+                rec_vals[8 * r + k] = b->vbits == 8 ? b->vals[8 * g + k]
+                                                    : reinterpret_cast<const uint16_t *>(b->vals.data())[8 * g + k];
+            ++r;
+        }
+    }
+
+    const size_t Rp = R + 1;
+    const size_t need = Carve::need({n * 4, n, n, n * 4, n * 8, n * 8, n * 8, n, n, R * 4, R * 4, R, R, R * 16,
+                                     Rp * 4, Rp * 4, scan_tmp_words((uint32_t)Rp) * 4 * 4, R * 4, R * 4, R * 4,
+                                     R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8});
+    VX_CUDA(it->ws.reserve(need));
+    Carve c(it->ws.p);
+    ApplyArgs a{};
+    a.mode = 0;
+    a.n_items = n;
+    a.n_records = (uint32_t)R;
+    a.max_depth = max_depth;
+    uint32_t *d_tree = c.take<uint32_t>(n);
+    uint8_t *d_depth = c.take<uint8_t>(n);
+    uint8_t *d_flags = c.take<uint8_t>(n);
+    uint32_t *d_fill = c.take<uint32_t>(n);
+    a.it_tree = d_tree;
+    a.it_depth = d_depth;
+    a.it_flags = d_flags;
+    a.it_fill = d_fill;
+    a.it_init = c.take<uint64_t>(n);
+    a.it_old = c.take<uint64_t>(n);
+    a.it_new = c.take<uint64_t>(n);
+    a.it_panic = c.take<uint8_t>(n);
+    a.it_changed = c.take<uint8_t>(n);
+    uint32_t *d_ritem = c.take<uint32_t>(R), *d_rgroup = c.take<uint32_t>(R);
+    uint8_t *d_rset = c.take<uint8_t>(R), *d_rclear = c.take<uint8_t>(R);
+    uint16_t *d_rvals = c.take<uint16_t>(R * 8);
+    a.rec_item = d_ritem;
+    a.rec_group = d_rgroup;
+    a.rec_set = d_rset;
+    a.rec_clear = d_rclear;
+    a.rec_vals = d_rvals;
+    a.flags = c.take<uint32_t>(Rp);
+    a.pos = c.take<uint32_t>(Rp);
+    a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
+    a.e_item[0] = c.take<uint32_t>(R);
+    a.e_item[1] = c.take<uint32_t>(R);
+    a.e_path[0] = c.take<uint32_t>(R);
+    a.e_path[1] = c.take<uint32_t>(R);
+    a.e_id[0] = c.take<uint64_t>(R);
+    a.e_id[1] = c.take<uint64_t>(R);
+    a.e_val[0] = c.take<uint32_t>(R);
+    a.e_val[1] = c.take<uint32_t>(R);
+    a.p_start = c.take<uint32_t>(Rp);
+    a.rec_id = c.take<uint64_t>(R);
+    a.rec_val = c.take<uint32_t>(R);
+    a.release_list = c.take<uint64_t>(n);
+
+    cudaStream_t s = it->stream;
+    VX_CUDA(cudaMemcpyAsync(d_tree, it_tree.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_depth, it_depth.data(), n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_flags, it_flags.data(), n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_fill, it_fill.data(), n * 4, cudaMemcpyHostToDevice, s));
+    if (R) {
+        VX_CUDA(cudaMemcpyAsync(d_ritem, rec_item.data(), R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(d_rgroup, rec_group.data(), R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(d_rset, rec_set.data(), R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(d_rclear, rec_clear.data(), R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(d_rvals, rec_vals.data(), R * 16, cudaMemcpyHostToDevice, s));
+    }
+    {
+        Phase ph(it, VX_PROF_APPLY);
+        VX_CUDA(launch_apply(it->dev, a, it->num_sms, s));
+    }
+    {
+        Phase ph(it, VX_PROF_REFCOUNT);
+        VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
+    }
+    {
+        Phase ph(it, VX_PROF_RELEASE);
+        VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity, it->capacity, 11,
+                               it->num_sms, s));
+    }
+    if (any_clear && (it->flags & VX_PATCH_P4)) {
+        // P4: every cleared voxel removed after the set phase, as VoxTree::set(pos, 0) would
+        a.mode = 1;
+        {
+            Phase ph(it, VX_PROF_APPLY);
+            VX_CUDA(launch_apply(it->dev, a, it->num_sms, s));
+        }
+        {
+            Phase ph(it, VX_PROF_REFCOUNT);
+            VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
+        }
+        {
+            Phase ph(it, VX_PROF_RELEASE);
+            VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity,
+                                   it->capacity, 11, it->num_sms, s));
+        }
+    }
+    std::vector<uint8_t> ch(n);
+    VX_CUDA(cudaMemcpyAsync(ch.data(), a.it_changed, n, cudaMemcpyDeviceToHost, s));
+    int st = sync_and_check(it);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (changed_out) changed_out[items[i].caller_index] = ch[i];
+        if (ch[i]) it->tree_maybe_nonempty[items[i].tree] = 1;
+    }
+    if (st == VX_OK) maybe_rehash(it);
+    return st;
+}
+
+// Batch filled from a dense [y][z][x] grid by just_set (batch.rs:145-172), in y, z, x order.
+void batch_from_dense(vx_batch *b, const void *grid) {
+    const int32_t n = 1 << b->depth;
+    const int vb = b->vbits / 8;
+    const uint8_t *g8 = static_cast<const uint8_t *>(grid);
+    const uint16_t *g16 = static_cast<const uint16_t *>(grid);
+    for (int32_t y = 0; y < n; ++y)
+        for (int32_t z = 0; z < n; ++z)
+            for (int32_t x = 0; x < n; ++x) {
+                const size_t o = ((size_t)y * n + z) * n + x;
+                const uint32_t v = vb == 1 ? g8[o] : g16[o];
+                const uint32_t full = morton_encode(x, y, z);
+                const uint64_t gi = full >> 3;
+                const unsigned idx = full & 7;
+                const uint8_t bit = (uint8_t)(1u << idx);
+                if (v) {
+                    b->set[gi] |= bit;
+                    b->clear[gi] &= (uint8_t)~bit;
+                } else {
+                    b->set[gi] &= (uint8_t)~bit;
+                    b->clear[gi] |= bit;
+                }
+                if (vb == 1)
+                    b->vals[8 * gi + idx] = (uint8_t)v;
+                else
+                    reinterpret_cast<uint16_t *>(b->vals.data())[8 * gi + idx] = (uint16_t)v;
+                b->has_patches = true;
+            }
+}
+
+// Fused dense construction on EMPTY trees (vx_build.cu). All arguments in device memory.
+int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void *d_grids, uint8_t *d_changed,
+               int depth) {
+    DenseArgs a{};
+    a.grids = d_grids;
+    a.trees = d_trees;
+    a.n_chunks = n;
+    a.depth = depth;
+    a.bdepth = std::min(depth, 5);
+    a.blocks_per_chunk = 1u << (3 * (depth - a.bdepth));
+    a.changed = d_changed;
+    cudaStream_t s = it->stream;
+    if (depth > 5) {
+        // level buffers: blocks, then each level above
+        size_t total = 0;
+        for (int k = depth - 5; k >= 1; --k) total += (size_t)n << (3 * k);
+        VX_CUDA(it->ws.reserve(Carve::need({total * 8, total * 4}) + 1024));
+        Carve c(it->ws.p);
+        uint64_t *ids = c.take<uint64_t>(total);
+        uint32_t *vals = c.take<uint32_t>(total);
+        a.block_roots = ids;
+        a.block_vals = vals;
+        {
+            Phase ph(it, VX_PROF_DENSE);
+            VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
+        }
+        Phase ph(it, VX_PROF_LEVELS);
+        uint64_t *in_ids = ids;
+        uint32_t *in_vals = vals;
+        size_t off = (size_t)n << (3 * (depth - 5));
+        for (int k = depth - 6; k >= 0; --k) {
+            const uint64_t np = (uint64_t)n << (3 * k);
+            uint64_t *out_ids = k > 0 ? ids + off : nullptr;
+            uint32_t *out_vals = k > 0 ? vals + off : nullptr;
+            VX_CUDA(launch_fresh_level(it->dev, in_ids, in_vals, out_ids, out_vals, np, k == 0, d_trees, d_changed, s));
+            in_ids = out_ids;
+            in_vals = out_vals;
+            off += np;
+        }
+    } else {
+        Phase ph(it, VX_PROF_DENSE);
+        VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
+    }
+    Phase ph(it, VX_PROF_REFCOUNT);
+    VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
+    return VX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- interner ---------------------------------------------------------------------------------
+int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_flags, int table_log2,
+                       vx_interner **out) {
+    if (!out || (voxel_bits != 8 && voxel_bits != 16) || table_log2 < 0 || table_log2 > 34)
+        return VX_E_INVALID_ARG;
+    *out = nullptr;
+    vx_interner *it = new (std::nothrow) vx_interner();
+    if (!it) return VX_E_OOM;
+    it->vbits = voxel_bits;
+    it->flags = patch_flags;
+    it->node_size = 4 + 2 + 64 + (uint64_t)voxel_bits / 8 + 8;  // interner/mod.rs:158-164
+    const uint64_t cap = budget_bytes / it->node_size;
+    if (cap == 0) {
+        delete it;
+        return VX_E_REF_PANIC;  // "Requested budget is too small" (interner/mod.rs:68)
+    }
+    if (cap > 0xFFFFFFF0ull) {
+        delete it;
+        return VX_E_INVALID_ARG;  // "Requested budget is too large" (interner/mod.rs:70-73)
+    }
+    it->capacity = cap;
+    uint64_t slots = 1024;
+    if (table_log2 > 0)
+        slots = 1ull << table_log2;
+    else
+        while (slots < 2 * cap) slots <<= 1;
+    it->table_slots = slots;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&it->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaStreamCreateWithFlags(&it->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete it;
+        return VX_E_CUDA;
+    }
+    it->stream = it->own_stream;
+    DevInterner &D = it->dev;
+    D.capacity = (uint32_t)cap;
+    D.vbits = voxel_bits;
+    D.flags = patch_flags;
+    D.table_mask = slots - 1;
+    D.max_probes = (uint32_t)std::min<uint64_t>(slots, 1u << 16);
+    const size_t vb = voxel_bits / 8;
+    bool ok = true;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (!ok) return;
+        if (cudaMalloc(p, std::max<size_t>(bytes, 256)) != cudaSuccess) ok = false;
+    };
+    alloc((void **)&D.children, cap * 64);
+    alloc(&D.values, cap * vb);
+    alloc((void **)&D.refcount, cap * 4);
+    alloc((void **)&D.generation, cap * 2);
+    alloc((void **)&D.hash, cap * 8);
+    alloc((void **)&D.ids, cap * 8);
+    alloc((void **)&D.free_list, cap * 4);
+    alloc((void **)&D.ctr, sizeof(DevCounters));
+    alloc((void **)&D.table, slots * 8);
+    alloc((void **)&D.leaf_table, ((size_t)1 << voxel_bits) * 8);
+    alloc((void **)&it->frontier, 2 * cap * 4 + 64);
+    alloc((void **)&it->d_live, 2 * sizeof(unsigned long long));
+    alloc((void **)&it->d_status, sizeof(int) * 4);
+    if (patch_flags & VX_PATCH_P3) {
+        it->seq_queue_cap = std::max<uint64_t>(cap + 1, 32768);
+        alloc((void **)&it->seq_queue, it->seq_queue_cap * 8);
+    } else {
+        it->seq_queue_cap = 32768;  // PREALLOCATED_STACK_SIZE (interner/consts.rs:15)
+        alloc((void **)&it->seq_queue, it->seq_queue_cap * 8);
+    }
+    if (ok && cudaMallocHost((void **)&it->h_ctr, sizeof(DevCounters)) != cudaSuccess) ok = false;
+    if (ok && cudaMallocHost((void **)&it->h_status, sizeof(int) * 4) != cudaSuccess) ok = false;
+    if (ok && cudaMallocHost((void **)&it->h_live, 2 * sizeof(unsigned long long)) != cudaSuccess) ok = false;
+    if (!ok || grow_tree_table(it, 1024) != cudaSuccess) {
+        vx_interner_destroy(it);
+        return VX_E_OOM;
+    }
+    cudaStream_t s = it->stream;
+    cudaMemsetAsync(D.children, 0, cap * 64, s);
+    cudaMemsetAsync(D.values, 0, cap * vb, s);
+    cudaMemsetAsync(D.refcount, 0, cap * 4, s);
+    cudaMemsetAsync(D.generation, 0, cap * 2, s);
+    cudaMemsetAsync(D.hash, 0, cap * 8, s);
+    cudaMemsetAsync(D.ids, 0, cap * 8, s);
+    cudaMemsetAsync(D.table, 0xFF, slots * 8, s);
+    cudaMemsetAsync(D.leaf_table, 0, ((size_t)1 << voxel_bits) * 8, s);
+    DevCounters c0{};
+    c0.next_index = 1;  // slot 0 is the EMPTY branch (interner/mod.rs:80-97)
+    *it->h_ctr = c0;
+    cudaMemcpyAsync(D.ctr, it->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        vx_interner_destroy(it);
+        return VX_E_CUDA;
+    }
+    *out = it;
+    return VX_OK;
+}
+
+int vx_interner_destroy(vx_interner *it) {
+    if (!it) return VX_E_INVALID_ARG;
+    if (it->stream) cudaStreamSynchronize(it->stream);
+    DevInterner &D = it->dev;
+    void *ptrs[] = {D.children, D.values, D.refcount, D.generation, D.hash, D.ids, D.free_list, D.ctr, D.table,
+                    D.leaf_table, D.roots, D.depths, it->frontier, it->seq_queue, it->d_live, it->d_status};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    it->ws.release();
+    it->staging.release();
+    if (it->h_ctr) cudaFreeHost(it->h_ctr);
+    if (it->h_status) cudaFreeHost(it->h_status);
+    if (it->h_live) cudaFreeHost(it->h_live);
+    for (auto &m : it->marks) {
+        cudaEventDestroy(m.second.first);
+        cudaEventDestroy(m.second.second);
+    }
+    for (cudaEvent_t e : it->event_pool) cudaEventDestroy(e);
+    if (it->own_stream) cudaStreamDestroy(it->own_stream);
+    delete it;
+    return VX_OK;
+}
+
+int vx_profile_enable(vx_interner *it, int on) {
+    if (!it) return VX_E_INVALID_ARG;
+    it->profile = on != 0;
+    return VX_OK;
+}
+
+int vx_profile_collect(vx_interner *it, double *ms, uint64_t *count) {
+    if (!it) return VX_E_INVALID_ARG;
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    for (int k = 0; k < VX_PROF_N; ++k) {
+        if (ms) ms[k] = 0.0;
+        if (count) count[k] = 0;
+    }
+    for (auto &m : it->marks) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, m.second.first, m.second.second);
+        if (ms) ms[m.first] += t;
+        if (count) count[m.first] += 1;
+        it->event_pool.push_back(m.second.first);
+        it->event_pool.push_back(m.second.second);
+    }
+    it->marks.clear();
+    return VX_OK;
+}
+
+uint64_t vx_kernel_launches(void) { return vxg::g_launches.load(); }
+
+int vx_interner_reset(vx_interner *it) {
+    if (!it) return VX_E_INVALID_ARG;
+    cudaStream_t s = it->stream;
+    VX_CUDA(cudaStreamSynchronize(s));
+    VX_CUDA(cudaMemsetAsync(it->dev.table, 0xFF, it->table_slots * 8, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.leaf_table, 0, ((size_t)1 << it->vbits) * 8, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.roots, 0, (size_t)it->tree_cap * 8, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.ids, 0, it->capacity * 8, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.refcount, 0, it->capacity * 4, s));
+    DevCounters c0{};
+    c0.next_index = 1;
+    *it->h_ctr = c0;
+    VX_CUDA(cudaMemcpyAsync(it->dev.ctr, it->h_ctr, sizeof(DevCounters), cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaStreamSynchronize(s));
+    std::fill(it->tree_maybe_nonempty.begin(), it->tree_maybe_nonempty.end(), 0);
+    it->all_trees_unknown = false;
+    return VX_OK;
+}
+
+int vx_interner_set_stream(vx_interner *it, void *cuda_stream) {
+    if (!it) return VX_E_INVALID_ARG;
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    it->stream = cuda_stream ? (cudaStream_t)cuda_stream : it->own_stream;
+    return VX_OK;
+}
+
+int vx_interner_sync(vx_interner *it) {
+    if (!it) return VX_E_INVALID_ARG;
+    return sync_and_check(it);
+}
+
+int vx_interner_stats_get(vx_interner *it, vx_interner_stats *out) {
+    if (!it || !out) return VX_E_INVALID_ARG;
+    VX_CUDA(launch_count_live(it->dev, it->d_live, it->num_sms, it->stream));
+    VX_CUDA(cudaMemcpyAsync(it->h_live, it->d_live, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, it->stream));
+    int st = sync_and_check(it);
+    *out = vx_interner_stats{};
+    out->capacity = it->capacity;
+    out->node_size = it->node_size;
+    out->next_index = it->h_ctr->next_index;
+    out->free_count = it->h_ctr->free_count;
+    out->alive_nodes = out->next_index - out->free_count;
+    out->branch_patterns = it->h_live[0] + 1;  // the EMPTY branch is a pattern in the reference
+    out->leaf_patterns = it->h_live[1];
+    out->table_slots = it->table_slots;
+    out->table_tombstones = it->h_ctr->tombstones;
+    out->error_flags = it->h_ctr->error;
+    return st == VX_E_OOB || st == VX_E_REF_PANIC ? VX_OK : st;
+}
+
+const char *vx_last_error(vx_interner *it) { return it ? it->last_error.c_str() : "null interner"; }
+
+int vx_get_ref(vx_interner *it, uint64_t block_id, uint32_t *out) {
+    if (!it || !out) return VX_E_INVALID_ARG;
+    const uint32_t idx = id_index(block_id);
+    if (idx >= it->capacity) return VX_E_INVALID_ARG;
+    uint16_t gen = 0;
+    VX_CUDA(cudaMemcpyAsync(&gen, it->dev.generation + idx, 2, cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaMemcpyAsync(out, it->dev.refcount + idx, 4, cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    if (gen != id_generation(block_id)) return set_err(it, VX_E_INVALID_ARG, "stale block id");
+    return VX_OK;
+}
+
+int vx_get_value(vx_interner *it, uint64_t block_id, uint32_t *out) {
+    if (!it || !out) return VX_E_INVALID_ARG;
+    const uint32_t idx = id_index(block_id);
+    if (idx >= it->capacity) return VX_E_INVALID_ARG;
+    uint16_t gen = 0;
+    uint16_t v = 0;
+    VX_CUDA(cudaMemcpyAsync(&gen, it->dev.generation + idx, 2, cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaMemcpyAsync(&v, (char *)it->dev.values + idx * (it->vbits / 8), it->vbits / 8,
+                            cudaMemcpyDeviceToHost, it->stream));
+    VX_CUDA(cudaStreamSynchronize(it->stream));
+    if (gen != id_generation(block_id)) return set_err(it, VX_E_INVALID_ARG, "stale block id");
+    *out = it->vbits == 8 ? (v & 0xFF) : v;
+    return VX_OK;
+}
+
+// ---- trees -----------------------------------------------------------------------------------
+int vx_trees_create(vx_interner *it, uint32_t n, const uint8_t *depths, vx_tree *out) {
+    if (!it || (!out && n)) return VX_E_INVALID_ARG;
+    for (uint32_t i = 0; i < n; ++i)
+        if ((int)depths[i] >= depth_limit(it->flags))
+            return set_err(it, VX_E_DEPTH, "Max depth exceeds allowed limit");
+    std::vector<vx_tree> slots(n);
+    uint32_t fresh_needed = 0;
+    size_t reuse = std::min<size_t>(n, it->free_trees.size());
+    fresh_needed = n - (uint32_t)reuse;
+    VX_CUDA(grow_tree_table(it, it->tree_count + fresh_needed));
+    for (uint32_t i = 0; i < n; ++i) {
+        vx_tree t;
+        if (i < reuse) {
+            t = it->free_trees.back();
+            it->free_trees.pop_back();
+        } else {
+            t = it->tree_count++;
+        }
+        slots[i] = t;
+        it->tree_used[t] = 1;
+        it->tree_depth[t] = depths[i];
+        it->tree_maybe_nonempty[t] = 0;
+    }
+    // upload the depth and EMPTY root of every new handle
+    uint32_t lo = 0xFFFFFFFFu, hi = 0;
+    for (vx_tree t : slots) {
+        lo = std::min(lo, t);
+        hi = std::max(hi, t);
+    }
+    if (n) {
+        std::vector<uint64_t> roots(hi - lo + 1);
+        VX_CUDA(cudaMemcpyAsync(roots.data(), it->dev.roots + lo, roots.size() * 8, cudaMemcpyDeviceToHost, it->stream));
+        VX_CUDA(cudaStreamSynchronize(it->stream));
+        for (vx_tree t : slots) roots[t - lo] = 0;
+        VX_CUDA(cudaMemcpyAsync(it->dev.roots + lo, roots.data(), roots.size() * 8, cudaMemcpyHostToDevice, it->stream));
+        VX_CUDA(cudaMemcpyAsync(it->dev.depths + lo, it->tree_depth.data() + lo, hi - lo + 1, cudaMemcpyHostToDevice,
+                                it->stream));
+        VX_CUDA(cudaStreamSynchronize(it->stream));
+    }
+    for (uint32_t i = 0; i < n; ++i) out[i] = slots[i];
+    return VX_OK;
+}
+
+int vx_tree_create(vx_interner *it, int max_depth, vx_tree *out) {
+    if (!it || !out) return VX_E_INVALID_ARG;
+    if (max_depth < 0 || max_depth >= depth_limit(it->flags))
+        return set_err(it, VX_E_DEPTH, "Max depth exceeds allowed limit");
+    uint8_t d = (uint8_t)max_depth;
+    return vx_trees_create(it, 1, &d, out);
+}
+
+int vx_tree_fill(vx_interner *it, vx_tree tree, uint32_t value) {
+    if (!it || !tree_ok(it, tree) || !value_fits(it, value)) return VX_E_INVALID_ARG;
+    VX_CUDA(launch_tree_fill(it->dev, tree, value, it->seq_queue, it->seq_queue_cap, it->d_status, it->stream));
+    VX_CUDA(cudaMemcpyAsync(it->h_status, it->d_status, sizeof(int), cudaMemcpyDeviceToHost, it->stream));
+    int st = sync_and_check(it);
+    it->tree_maybe_nonempty[tree] = value != 0;
+    if (st == VX_OK) maybe_rehash(it);
+    return st;
+}
+
+int vx_tree_clear(vx_interner *it, vx_tree tree) { return vx_tree_fill(it, tree, 0); }
+
+int vx_tree_destroy(vx_interner *it, vx_tree tree) {
+    if (!it || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
+    int st = vx_tree_clear(it, tree);
+    it->tree_used[tree] = 0;
+    it->tree_depth[tree] = kUnused;
+    const uint8_t u = kUnused;
+    cudaMemcpyAsync(it->dev.depths + tree, &u, 1, cudaMemcpyHostToDevice, it->stream);
+    cudaStreamSynchronize(it->stream);
+    it->free_trees.push_back(tree);
+    return st;
+}
+
+int vx_tree_root(vx_interner *it, vx_tree tree, uint64_t *out_root) {
+    if (!it || !out_root || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
+    return read_root(it, tree, out_root);
+}
+
+int vx_tree_max_depth(vx_interner *it, vx_tree tree, int *out) {
+    if (!it || !out || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
+    *out = it->tree_depth[tree];
+    return VX_OK;
+}
+
+int vx_tree_set(vx_interner *it, vx_tree tree, int32_t x, int32_t y, int32_t z, uint32_t value, int *changed) {
+    if (!it || !tree_ok(it, tree) || !value_fits(it, value)) return VX_E_INVALID_ARG;
+    const int32_t side = 1 << it->tree_depth[tree];
+    if (x < 0 || y < 0 || z < 0 || x >= side || y >= side || z >= side)
+        return set_err(it, VX_E_OOB, "position out of bounds");
+    VX_CUDA(launch_tree_set(it->dev, tree, x, y, z, value, it->seq_queue, it->seq_queue_cap, it->d_status, it->stream));
+    VX_CUDA(cudaMemcpyAsync(it->h_status, it->d_status, sizeof(int), cudaMemcpyDeviceToHost, it->stream));
+    int st = sync_and_check(it);
+    if (changed) *changed = *it->h_status == 1;
+    if (*it->h_status == 1) it->tree_maybe_nonempty[tree] = 1;
+    if (st == VX_OK) maybe_rehash(it);
+    return st;
+}
+
+int vx_tree_get(vx_interner *it, vx_tree tree, int32_t x, int32_t y, int32_t z, int *found, uint32_t *value) {
+    if (!it || !found || !value || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
+    const int32_t side = 1 << it->tree_depth[tree];
+    if (x < 0 || y < 0 || z < 0 || x >= side || y >= side || z >= side)
+        return set_err(it, VX_E_OOB, "position out of bounds");
+    int32_t xyz[3] = {x, y, z};
+    uint8_t f = 0;
+    uint16_t v = 0;
+    int st = vx_get_many(it, 1, &tree, xyz, &f, &v, VX_MEM_HOST);
+    *found = f;
+    *value = f ? (it->vbits == 8 ? (v & 0xFF) : v) : 0;
+    return st;
+}
+
+// ---- batches ---------------------------------------------------------------------------------
+int vx_batch_create(int max_depth, int voxel_bits, uint32_t patch_flags, vx_batch **out) {
+    if (!out || (voxel_bits != 8 && voxel_bits != 16)) return VX_E_INVALID_ARG;
+    if (max_depth < 0 || max_depth >= depth_limit(patch_flags)) return VX_E_DEPTH;
+    vx_batch *b = new (std::nothrow) vx_batch();
+    if (!b) return VX_E_OOM;
+    b->depth = max_depth;
+    b->vbits = voxel_bits;
+    b->flags = patch_flags;
+    const int lower = max_depth > 0 ? max_depth - 1 : 0;
+    b->groups = 1ull << (3 * lower);
+    try {
+        b->set.assign(b->groups, 0);
+        b->clear.assign(b->groups, 0);
+        b->vals.assign(b->groups * 8 * (voxel_bits / 8), 0);
+    } catch (const std::bad_alloc &) {
+        delete b;
+        return VX_E_OOM;
+    }
+    *out = b;
+    return VX_OK;
+}
+
+int vx_batch_destroy(vx_batch *b) {
+    delete b;
+    return VX_OK;
+}
+
+int vx_batch_set(vx_batch *b, int32_t x, int32_t y, int32_t z, uint32_t value) {
+    if (!b) return VX_E_INVALID_ARG;
+    if (value > (b->vbits == 8 ? 0xFFu : 0xFFFFu)) return VX_E_INVALID_ARG;
+    const int32_t n = 1 << b->depth;
+    if (x < 0 || y < 0 || z < 0 || x >= n || y >= n || z >= n) return VX_E_OOB;
+    const uint32_t full = morton_encode(x, y, z);
+    const uint64_t gi = full >> 3;
+    const unsigned idx = full & 7;
+    const uint8_t bit = (uint8_t)(1u << idx);
+    if (value) {
+        b->set[gi] |= bit;
+        b->clear[gi] &= (uint8_t)~bit;
+    } else {
+        b->set[gi] &= (uint8_t)~bit;
+        b->clear[gi] |= bit;
+    }
+    if (b->vbits == 8)
+        b->vals[8 * gi + idx] = (uint8_t)value;
+    else
+        reinterpret_cast<uint16_t *>(b->vals.data())[8 * gi + idx] = (uint16_t)value;
+    b->has_patches = true;
+    return VX_OK;
+}
+
+int vx_batch_clear(vx_batch *b) {
+    if (!b) return VX_E_INVALID_ARG;
+    std::fill(b->set.begin(), b->set.end(), 0);
+    std::fill(b->clear.begin(), b->clear.end(), 0);
+    std::fill(b->vals.begin(), b->vals.end(), 0);
+    b->has_fill = false;
+    b->fill = 0;
+    b->has_patches = false;
+    return VX_OK;
+}
+
+int vx_batch_fill(vx_batch *b, uint32_t value) {
+    if (!b || value > (b->vbits == 8 ? 0xFFu : 0xFFFFu)) return VX_E_INVALID_ARG;
+    vx_batch_clear(b);
+    b->has_fill = true;
+    b->fill = value;
+    return VX_OK;
+}
+
+int vx_batch_set_dense(vx_batch *b, const void *grid) {
+    if (!b || !grid) return VX_E_INVALID_ARG;
+    batch_from_dense(b, grid);
+    return VX_OK;
+}
+
+int vx_batch_size(const vx_batch *b, uint64_t *out) {
+    if (!b || !out) return VX_E_INVALID_ARG;
+    uint64_t n = 0;
+    for (uint64_t g = 0; g < b->groups; ++g) n += (b->set[g] | b->clear[g]) != 0;
+    *out = n;
+    return VX_OK;
+}
+
+int vx_batch_has_patches(const vx_batch *b, int *out) {
+    if (!b || !out) return VX_E_INVALID_ARG;
+    *out = b->has_patches ? 1 : 0;
+    return VX_OK;
+}
+
+// ---- the hot path -----------------------------------------------------------------------------
+int vx_apply_batches(vx_interner *it, uint32_t n, const vx_tree *trees, const vx_batch *const *batches,
+                     uint8_t *changed) {
+    if (!it || (n && (!trees || !batches))) return VX_E_INVALID_ARG;
+    std::vector<Item> items(n);
+    std::unordered_set<vx_tree> seen;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!tree_ok(it, trees[i]) || !batches[i]) return set_err(it, VX_E_INVALID_ARG, "unknown tree or batch");
+        if (batches[i]->vbits != it->vbits) return set_err(it, VX_E_INVALID_ARG, "batch voxel width differs");
+        if (batches[i]->depth != it->tree_depth[trees[i]])
+            return set_err(it, VX_E_REF_PANIC, "batch depth differs from the tree depth");
+        if (!seen.insert(trees[i]).second) return set_err(it, VX_E_INVALID_ARG, "a tree appears twice in one call");
+        items[i] = Item{trees[i], batches[i], i};
+    }
+    return run_apply(it, std::move(items), changed);
+}
+
+int vx_apply_batch(vx_interner *it, vx_tree tree, const vx_batch *batch, int *changed) {
+    uint8_t c = 0;
+    int st = vx_apply_batches(it, 1, &tree, &batch, &c);
+    if (changed) *changed = c;
+    return st;
+}
+
+int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev, const void *grids_dev,
+                         uint8_t *changed_dev, int max_depth) {
+    if (!it || (n && (!trees_dev || !grids_dev))) return VX_E_INVALID_ARG;
+    if (max_depth < 0 || max_depth >= depth_limit(it->flags)) return set_err(it, VX_E_DEPTH, "Max depth exceeds allowed limit");
+    if (max_depth < 2) return set_err(it, VX_E_REF_PANIC, "batch apply needs max_depth >= 2 (usize underflow in the reference)");
+    if ((uintptr_t)grids_dev % 16) return set_err(it, VX_E_INVALID_ARG, "grids must be 16-byte aligned");
+    // the trees are named by device handles the host does not inspect: every tree counts as
+    // possibly non-empty until the next reset.
+    it->all_trees_unknown = true;
+    if (n == 0) return VX_OK;
+    return dense_fast(it, n, trees_dev, grids_dev, changed_dev, max_depth);
+}
+
+int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void *grids, uint8_t *changed,
+                   vx_mem mem) {
+    if (!it || (n && (!trees || !grids))) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    std::vector<vx_tree> htrees(n);
+    if (mem == VX_MEM_DEVICE) {
+        VX_CUDA(cudaMemcpyAsync(htrees.data(), trees, n * sizeof(vx_tree), cudaMemcpyDeviceToHost, it->stream));
+        VX_CUDA(cudaStreamSynchronize(it->stream));
+    } else {
+        std::copy(trees, trees + n, htrees.begin());
+    }
+    std::unordered_set<vx_tree> seen;
+    int d = -1;
+    bool fresh = !it->all_trees_unknown;
+    for (vx_tree t : htrees) {
+        if (!tree_ok(it, t)) return set_err(it, VX_E_INVALID_ARG, "unknown tree handle");
+        if (!seen.insert(t).second) return set_err(it, VX_E_INVALID_ARG, "a tree appears twice in one call");
+        if (d >= 0 && it->tree_depth[t] != d) return set_err(it, VX_E_INVALID_ARG, "trees of one call share a depth");
+        d = it->tree_depth[t];
+        fresh = fresh && !it->tree_maybe_nonempty[t];
+    }
+    if (d < 2) return set_err(it, VX_E_REF_PANIC, "batch apply needs max_depth >= 2 (usize underflow in the reference)");
+    const size_t vb = it->vbits / 8;
+    const size_t per = ((size_t)1 << (3 * d)) * vb;
+    if (!fresh) {
+        // general path: Batch per grid, then the batched apply
+        std::vector<uint8_t> hgrids;
+        const uint8_t *g = static_cast<const uint8_t *>(grids);
+        if (mem == VX_MEM_DEVICE) {
+            hgrids.resize(per * n);
+            VX_CUDA(cudaMemcpy(hgrids.data(), grids, per * n, cudaMemcpyDeviceToHost));
+            g = hgrids.data();
+        }
+        std::vector<vx_batch *> bs(n, nullptr);
+        int st = VX_OK;
+        for (uint32_t i = 0; i < n && st == VX_OK; ++i) {
+            st = vx_batch_create(d, it->vbits, it->flags, &bs[i]);
+            if (st == VX_OK) batch_from_dense(bs[i], g + per * i);
+        }
+        std::vector<uint8_t> ch(n);
+        if (st == VX_OK) st = vx_apply_batches(it, n, htrees.data(), bs.data(), ch.data());
+        for (auto *b : bs) vx_batch_destroy(b);
+        if (changed) {
+            if (mem == VX_MEM_DEVICE)
+                cudaMemcpy(changed, ch.data(), n, cudaMemcpyHostToDevice);
+            else
+                std::copy(ch.begin(), ch.end(), changed);
+        }
+        return st;
+    }
+    const uint32_t *d_trees;
+    const void *d_grids;
+    uint8_t *d_changed;
+    if (mem == VX_MEM_HOST) {
+        VX_CUDA(it->staging.reserve(Carve::need({n * 4, per * n, n})));
+        Carve c(it->staging.p);
+        uint32_t *dt = c.take<uint32_t>(n);
+        uint8_t *dg = c.take<uint8_t>(per * n);
+        uint8_t *dc = c.take<uint8_t>(n);
+        Phase ph(it, VX_PROF_COPY);
+        VX_CUDA(cudaMemcpyAsync(dt, htrees.data(), n * 4, cudaMemcpyHostToDevice, it->stream));
+        VX_CUDA(cudaMemcpyAsync(dg, grids, per * n, cudaMemcpyHostToDevice, it->stream));
+        VX_CUDA(cudaMemsetAsync(dc, 0, n, it->stream));
+        d_trees = dt;
+        d_grids = dg;
+        d_changed = dc;
+    } else {
+        if ((uintptr_t)grids % 16) return set_err(it, VX_E_INVALID_ARG, "grids must be 16-byte aligned");
+        d_trees = trees;
+        d_grids = grids;
+        d_changed = changed;
+    }
+    int st = dense_fast(it, n, d_trees, d_grids, d_changed, d);
+    if (st != VX_OK) return st;
+    if (mem == VX_MEM_HOST && changed) {
+        Phase ph(it, VX_PROF_COPY);
+        VX_CUDA(cudaMemcpyAsync(changed, d_changed, n, cudaMemcpyDeviceToHost, it->stream));
+    }
+    st = sync_and_check(it);
+    for (vx_tree t : htrees) it->tree_maybe_nonempty[t] = 1;
+    return st;
+}
+
+int vx_get_many_async(vx_interner *it, uint64_t n, const vx_tree *trees_dev, const int32_t *xyz_dev,
+                      uint8_t *found_dev, void *values_dev) {
+    if (!it || (n && (!trees_dev || !xyz_dev || !found_dev || !values_dev))) return VX_E_INVALID_ARG;
+    Phase ph(it, VX_PROF_GET);
+    VX_CUDA(launch_get_many(it->dev, n, trees_dev, xyz_dev, found_dev, values_dev, it->num_sms, it->stream));
+    return VX_OK;
+}
+
+int vx_get_many(vx_interner *it, uint64_t n, const vx_tree *trees, const int32_t *xyz, uint8_t *found, void *values,
+                vx_mem mem) {
+    if (!it || (n && (!trees || !xyz || !found || !values))) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    if (mem == VX_MEM_DEVICE) {
+        {
+            Phase ph(it, VX_PROF_GET);
+            VX_CUDA(launch_get_many(it->dev, n, trees, xyz, found, values, it->num_sms, it->stream));
+        }
+        return sync_and_check(it);
+    }
+    const size_t vb = it->vbits / 8;
+    VX_CUDA(it->staging.reserve(Carve::need({n * 4, n * 12, n, n * vb})));
+    Carve c(it->staging.p);
+    uint32_t *dt = c.take<uint32_t>(n);
+    int32_t *dx = c.take<int32_t>(n * 3);
+    uint8_t *df = c.take<uint8_t>(n);
+    uint8_t *dv = c.take<uint8_t>(n * vb);
+    {
+        Phase ph(it, VX_PROF_COPY);
+        VX_CUDA(cudaMemcpyAsync(dt, trees, n * 4, cudaMemcpyHostToDevice, it->stream));
+        VX_CUDA(cudaMemcpyAsync(dx, xyz, n * 12, cudaMemcpyHostToDevice, it->stream));
+    }
+    {
+        Phase ph(it, VX_PROF_GET);
+        VX_CUDA(launch_get_many(it->dev, n, dt, dx, df, dv, it->num_sms, it->stream));
+    }
+    {
+        Phase ph(it, VX_PROF_COPY);
+        VX_CUDA(cudaMemcpyAsync(found, df, n, cudaMemcpyDeviceToHost, it->stream));
+        VX_CUDA(cudaMemcpyAsync(values, dv, n * vb, cudaMemcpyDeviceToHost, it->stream));
+    }
+    return sync_and_check(it);
+}
+
+// ---- verification helpers ----------------------------------------------------------------------
+int vx_export_canonical(vx_interner *it, uint32_t n_trees, const vx_tree *trees, vx_canonical *out,
+                        uint64_t *n_nodes) {
+    if (!it || !n_nodes || (n_trees && !trees)) return VX_E_INVALID_ARG;
+    Snapshot s;
+    int st = take_snapshot(it, s);
+    if (st != VX_OK) return st;
+    std::vector<uint64_t> roots;
+    st = read_roots(it, n_trees, trees, roots);
+    if (st != VX_OK) return st;
+    std::unordered_map<uint32_t, int32_t> ids;
+    std::vector<uint64_t> order, stack;
+    std::vector<int32_t> croots(n_trees, -1);
+    for (uint32_t t = 0; t < n_trees; ++t) {
+        const uint64_t r = roots[t];
+        if (r == 0) continue;
+        stack.push_back(r);
+        while (!stack.empty()) {
+            const uint64_t nd = stack.back();
+            stack.pop_back();
+            const uint32_t idx = id_index(nd);
+            if (idx >= s.n) return set_err(it, VX_E_REF_UB, "child index outside the node store");
+            if (ids.count(idx)) continue;
+            ids[idx] = (int32_t)order.size();
+            order.push_back(nd);
+            if (id_is_branch(nd))
+                for (int k = 7; k >= 0; --k)
+                    if (s.children[8ull * idx + k]) stack.push_back(s.children[8ull * idx + k]);
+        }
+        croots[t] = ids[id_index(r)];
+    }
+    *n_nodes = order.size();
+    if (!out) return VX_OK;
+    if (out->capacity < order.size()) return VX_E_BUFFER;
+    for (size_t k = 0; k < order.size(); ++k) {
+        const uint64_t nd = order[k];
+        const uint32_t idx = id_index(nd);
+        const bool leaf = id_is_leaf(nd);
+        out->kind[k] = leaf ? 1 : 0;
+        out->types[k] = leaf ? 0 : (uint8_t)id_types(nd);
+        out->mask[k] = leaf ? 0 : (uint8_t)id_mask(nd);
+        out->value[k] = s.values[idx];
+        out->refcount[k] = s.refcount[idx];
+        for (int j = 0; j < 8; ++j) {
+            int32_t c = -1;
+            if (!leaf) {
+                const uint64_t cid = s.children[8ull * idx + j];
+                if (cid) c = ids[id_index(cid)];
+            }
+            out->children[k * 8 + j] = c;
+        }
+    }
+    if (out->roots)
+        for (uint32_t t = 0; t < n_trees; ++t) out->roots[t] = croots[t];
+    return VX_OK;
+}
+
+int vx_validate(vx_interner *it, uint32_t n_trees, const vx_tree *trees) {
+    if (!it || (n_trees && !trees)) return VX_E_INVALID_ARG;
+    Snapshot s;
+    int st = take_snapshot(it, s);
+    if (st != VX_OK) return st;
+    std::vector<uint64_t> roots;
+    st = read_roots(it, n_trees, trees, roots);
+    if (st != VX_OK) return st;
+    std::vector<uint8_t> seen(s.n, 0);
+    std::vector<uint64_t> stack;
+    for (uint64_t r : roots) {
+        if (r == 0) continue;
+        stack.push_back(r);
+        while (!stack.empty()) {
+            const uint64_t nd = stack.back();
+            stack.pop_back();
+            const uint32_t idx = id_index(nd);
+            if (idx >= s.n) return set_err(it, VX_E_REF_UB, "child index outside the node store");
+            if (s.generation[idx] != id_generation(nd) || s.ids[idx] != nd)
+                return set_err(it, VX_E_REF_UB, "dangling child: generation mismatch");
+            if (s.refcount[idx] == 0) return set_err(it, VX_E_REF_UB, "reachable node with zero refcount");
+            if (seen[idx]) continue;
+            seen[idx] = 1;
+            if (id_is_branch(nd))
+                for (int k = 0; k < 8; ++k)
+                    if (s.children[8ull * idx + k]) stack.push_back(s.children[8ull * idx + k]);
+        }
+    }
+    return VX_OK;
+}
+
+int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid) {
+    if (!it || !out_grid || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
+    Snapshot s;
+    int st = take_snapshot(it, s);
+    if (st != VX_OK) return st;
+    uint64_t root = 0;
+    st = read_root(it, tree, &root);
+    if (st != VX_OK) return st;
+    const int md = it->tree_depth[tree];
+    const size_t n = (size_t)1 << md, size = n * n * n;
+    const int vb = it->vbits / 8;
+    auto put = [&](size_t i, uint32_t v) {
+        if (vb == 1)
+            static_cast<uint8_t *>(out_grid)[i] = (uint8_t)v;
+        else
+            static_cast<uint16_t *>(out_grid)[i] = (uint16_t)v;
+    };
+    if (!id_is_branch(root)) {  // utils/common.rs:169-171
+        const uint32_t v = s.values[id_index(root)];
+        for (size_t i = 0; i < size; ++i) put(i, v);
+        return VX_OK;
+    }
+    for (size_t i = 0; i < size; ++i) put(i, 0);
+    if (root == 0) return VX_OK;
+    struct E {
+        uint64_t id;
+        int32_t x, y, z;
+        int depth;
+    };
+    std::vector<E> stack{{root, 0, 0, 0, 0}};
+    while (!stack.empty()) {
+        E e = stack.back();
+        stack.pop_back();
+        const uint32_t idx = id_index(e.id);
+        if (id_is_branch(e.id) && e.depth < md) {
+            const int32_t half = 1 << (md - e.depth - 1);
+            for (int i = 7; i >= 0; --i) {
+                const uint64_t c = s.children[8ull * idx + i];
+                if (!c) continue;
+                stack.push_back({c, e.x + (i & 1) * half, e.y + ((i >> 1) & 1) * half, e.z + ((i >> 2) & 1) * half,
+                                 e.depth + 1});
+            }
+        } else {
+            const uint32_t v = s.values[idx];
+            if (!v) continue;
+            const size_t side = (size_t)1 << (md - e.depth);
+            for (size_t yy = e.y; yy < e.y + side; ++yy)
+                for (size_t zz = e.z; zz < e.z + side; ++zz)
+                    for (size_t xx = e.x; xx < e.x + side; ++xx) put((yy * n + zz) * n + xx, v);
+        }
+    }
+    return VX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,384 @@
+// Device-side data structures and primitives of the GB300 interner.
+//
+// The interner (the reference's VoxInterner<T>, interner/mod.rs:25-40) lives in HBM as SoA arrays
+// of `capacity` node records (capacity = budget / node_size, interner/mod.rs:49-53, 158-164):
+//   children[8*i]  u64 BlockIds of the 8 children (zero for leaves)      64 B
+//   values[i]      u8 / u16 voxel value (leaf) or LOD value (branch)      1-2 B
+//   refcount[i]    u32                                                     4 B
+//   generation[i]  u16, bumped when the slot is recycled                  2 B
+//   hash[i]        u64 key fingerprint (branches)                          8 B
+//   ids[i]         u64 live BlockId of the slot, 0 while free            (+8 B, outside the budget)
+// Hash-consing tables (outside the budget, like the reference's HashMaps):
+//   table[]        open-addressed branch table of 64-bit slots: tag (32 bits of the key
+//                  fingerprint) | node index. Inserts claim a slot with atomicCAS and publish the
+//                  index after writing the node; lookups compare the full key (types, mask and the
+//                  8 child ids), so equal keys always dedup and unequal keys never alias.
+//   leaf_table[v]  direct-mapped leaf ids, one slot per voxel value (0 = none, 1 = being created).
+// Allocation pops the LIFO free list first, then bumps next_index (interner/macros.rs:1-41).
+// Every spin-wait is bounded; failures set sticky error bits that the host turns into statuses.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vxg {
+
+constexpr uint64_t EMPTY_ID = 0ull;
+constexpr uint64_t INVALID_ID = ~0ull;
+constexpr uint16_t MAX_GENERATION = 0x7FFE;
+constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
+
+// table slot encoding
+constexpr uint64_t SLOT_EMPTY = ~0ull;
+constexpr uint64_t SLOT_TOMB = 0xFFFFFFFEFFFFFFFEull;
+constexpr uint32_t IDX_BUSY = 0xFFFFFFFFu;
+constexpr uint64_t LEAF_BUSY = 1ull;
+
+// sticky error bits (mapped to VX_E_* by the host)
+enum : uint32_t {
+    ERR_OOM = 1u << 0,
+    ERR_TABLE_FULL = 1u << 1,
+    ERR_TIMEOUT = 1u << 2,
+    ERR_REF_PANIC = 1u << 3,
+    ERR_REF_UB = 1u << 4,
+    ERR_OOB = 1u << 5,
+    ERR_INTERNAL = 1u << 6,
+    ERR_INVALID = 1u << 7,
+};
+
+constexpr uint8_t TREE_UNUSED = 0xFF;  // depth marker of a free tree slot
+
+constexpr uint32_t SPIN_LIMIT = 1u << 22;   // bounded waits (~tens of ms with nanosleep)
+constexpr uint32_t ROUND_LIMIT = 1u << 20;  // bounded warp-intern rounds
+
+struct DevCounters {
+    unsigned long long next_index;   // bump pointer
+    unsigned long long free_count;   // free-list length
+    unsigned long long alloc_count;  // allocations in the current epoch
+    unsigned long long tombstones;   // deleted branch-table slots
+    unsigned int error;              // sticky ERR_* bits
+    unsigned int error_info;         // first error detail
+    unsigned long long scratch[10];  // per-launch counters used by the kernels
+};
+
+struct DevInterner {
+    uint64_t *children;
+    void *values;
+    uint32_t *refcount;
+    uint16_t *generation;
+    uint64_t *hash;
+    uint64_t *ids;
+    uint32_t *free_list;
+    DevCounters *ctr;
+    uint64_t *table;
+    uint64_t table_mask;
+    uint64_t *leaf_table;
+    uint64_t *roots;
+    uint8_t *depths;
+    uint32_t tree_cap;
+    uint32_t capacity;
+    int vbits;
+    uint32_t flags;
+    uint32_t max_probes;
+};
+
+// ---- BlockId (core/block_id.rs:19-418) -------------------------------------------------------
+__host__ __device__ __forceinline__ bool id_is_leaf(uint64_t id) { return (id >> 63) != 0; }
+__host__ __device__ __forceinline__ bool id_is_branch(uint64_t id) { return (id >> 63) == 0; }
+__host__ __device__ __forceinline__ uint32_t id_index(uint64_t id) { return (uint32_t)id; }
+__host__ __device__ __forceinline__ uint32_t id_generation(uint64_t id) { return (uint32_t)((id >> 32) & 0x7FFF); }
+__host__ __device__ __forceinline__ uint32_t id_types(uint64_t id) { return (uint32_t)((id >> 55) & 0xFF); }
+__host__ __device__ __forceinline__ uint32_t id_mask(uint64_t id) { return (uint32_t)((id >> 47) & 0xFF); }
+__host__ __device__ __forceinline__ uint64_t make_leaf_id(uint32_t index, uint32_t gen) {
+    return (1ull << 63) | ((uint64_t)(gen & 0x7FFF) << 32) | index;
+}
+__host__ __device__ __forceinline__ uint64_t make_branch_id(uint32_t index, uint32_t gen, uint32_t types,
+                                                            uint32_t mask) {
+    return ((uint64_t)(types & 0xFF) << 55) | ((uint64_t)(mask & 0xFF) << 47) |
+           ((uint64_t)(gen & 0x7FFF) << 32) | index;
+}
+
+// Sibling-prefix mask PATH_MASKS[d][k] (voxtree.rs:41-105), closed form.
+__host__ __device__ __forceinline__ uint32_t path_mask(int d, int k) {
+    if (d <= 0 || k > d - 1) return 0;
+    return ((1u << (3 * (k + 1))) - 1u) << (3 * (d - 1 - k));
+}
+
+// ---- memory helpers --------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t ld_volatile(const uint64_t *p) { return *(const volatile uint64_t *)p; }
+__device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
+
+__device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
+    unsigned int old = atomicOr(&I.ctr->error, bit);
+    if (old == 0) atomicExch(&I.ctr->error_info, info);
+}
+
+__device__ __forceinline__ uint32_t node_value(const DevInterner &I, uint32_t idx) {
+    return I.vbits == 8 ? (uint32_t)((const uint8_t *)I.values)[idx] : (uint32_t)((const uint16_t *)I.values)[idx];
+}
+__device__ __forceinline__ uint32_t node_value_cg(const DevInterner &I, uint32_t idx) {
+    if (I.vbits == 8) return (uint32_t)__ldcg((const unsigned char *)I.values + idx);
+    return (uint32_t)__ldcg((const unsigned short *)I.values + idx);
+}
+__device__ __forceinline__ void set_node_value(const DevInterner &I, uint32_t idx, uint32_t v) {
+    if (I.vbits == 8)
+        ((uint8_t *)I.values)[idx] = (uint8_t)v;
+    else
+        ((uint16_t *)I.values)[idx] = (uint16_t)v;
+}
+
+// ---- key fingerprint -------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t fmix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+__device__ __forceinline__ uint64_t branch_fingerprint(const uint64_t c[8], uint32_t tm) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ ((uint64_t)tm << 17);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        h ^= c[i] * 0x87C37B91114253D5ull;
+        h = ((h << 31) | (h >> 33)) * 0x4CF5AD432745937Full;
+    }
+    return fmix64(h);
+}
+__device__ __forceinline__ uint32_t slot_tag(uint64_t h) {
+    uint32_t t = (uint32_t)(h >> 32);
+    return t >= 0xFFFFFFFEu ? 0xFFFFFFFDu : t;
+}
+__device__ __forceinline__ uint64_t make_slot(uint32_t tag, uint32_t idx) { return ((uint64_t)tag << 32) | idx; }
+
+// calc_average (core/voxel.rs:96-141): the mode of the 8 values. Distinct values are visited in
+// first-seen order; a later value replaces the current best when it is more frequent, or equally
+// frequent while the best is the default value and it is not. Fully unrolled on registers.
+__device__ __forceinline__ uint32_t calc_average8(const uint32_t v[8]) {
+    uint32_t best = v[0];
+    uint32_t best_cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) best_cnt += v[j] == v[0] ? 1u : 0u;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) {
+        bool first = true;
+#pragma unroll
+        for (int j = 0; j < k; ++j) first = first && v[j] != v[k];
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cnt += v[j] == v[k] ? 1u : 0u;
+        if (first && (cnt > best_cnt || (cnt == best_cnt && best == 0 && v[k] != 0))) {
+            best = v[k];
+            best_cnt = cnt;
+        }
+    }
+    return best;
+}
+
+// ---- allocation --------------------------------------------------------------------------------
+// The t-th allocation of an epoch takes free_list[free_count-1-t] while the free list lasts, then
+// next_index + (t - free_count). free_count and next_index only change between epochs.
+__device__ __forceinline__ uint32_t node_for_ticket(const DevInterner &I, unsigned long long t) {
+    unsigned long long fc = I.ctr->free_count;
+    unsigned long long idx = (t < fc) ? (unsigned long long)I.free_list[fc - 1 - t] : I.ctr->next_index + (t - fc);
+    return idx < I.capacity ? (uint32_t)idx : NO_NODE;
+}
+
+// Writes a new branch record (children, LOD value, fingerprint, live id); rc starts at 0.
+__device__ __forceinline__ uint64_t write_branch(const DevInterner &I, uint32_t idx, const uint64_t c[8],
+                                                 uint32_t types, uint32_t mask, uint64_t h, uint32_t lod) {
+    uint32_t gen = I.generation[idx];
+    uint64_t id = make_branch_id(idx, gen, types, mask);
+    ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(I.children + 8ull * idx);
+    dst[0] = make_ulonglong2(c[0], c[1]);
+    dst[1] = make_ulonglong2(c[2], c[3]);
+    dst[2] = make_ulonglong2(c[4], c[5]);
+    dst[3] = make_ulonglong2(c[6], c[7]);
+    set_node_value(I, idx, lod);
+    I.hash[idx] = h;
+    I.refcount[idx] = 0;
+    I.ids[idx] = id;
+    return id;
+}
+
+__device__ __forceinline__ bool key_equal(const DevInterner &I, uint32_t idx, const uint64_t c[8], uint32_t types,
+                                          uint32_t mask) {
+    uint64_t id = ld_cg(I.ids + idx);
+    if (id == 0 || id_is_leaf(id) || id_types(id) != types || id_mask(id) != mask) return false;
+    const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(I.children + 8ull * idx);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ulonglong2 w = __ldcg(src + k);
+        if (w.x != c[2 * k] || w.y != c[2 * k + 1]) return false;
+    }
+    return true;
+}
+
+// Warp-cooperative find-or-insert of branch keys. Every lane of the warp must call it (converged);
+// lanes with active == false only take part in the ballots. Each round every unfinished lane makes
+// one non-blocking probe step; lanes that claimed an empty slot receive node indices from a single
+// warp-aggregated ticket range, write their node and publish it. A lane that meets a slot still being
+// written retries it next round, so no lane ever waits inside a divergent branch.
+// Returns the BlockId, or INVALID_ID on error; *created tells whether this lane inserted the node.
+__device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, bool active, const uint64_t c[8],
+                                                       uint32_t types, uint32_t mask, uint32_t lod, bool *created,
+                                                       uint64_t h_in = 0) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t tm = (types << 8) | mask;
+    uint64_t h = 0;
+    uint32_t tag = 0;
+    uint64_t pos = 0;
+    uint32_t probes = 0;
+    bool done = !active;
+    uint64_t result = INVALID_ID;
+    *created = false;
+    if (active) {
+        h = h_in ? h_in : branch_fingerprint(c, tm);
+        tag = slot_tag(h);
+        pos = h & I.table_mask;
+    }
+    for (uint32_t round = 0;; ++round) {
+        bool claimed = false;
+        if (!done) {
+            uint64_t s = ld_volatile(I.table + pos);
+            if (s == SLOT_EMPTY) {
+                uint64_t prev = atomicCAS((unsigned long long *)(I.table + pos), SLOT_EMPTY, make_slot(tag, IDX_BUSY));
+                if (prev == SLOT_EMPTY)
+                    claimed = true;
+                else
+                    s = prev;
+            }
+            if (!claimed) {
+                if ((uint32_t)(s >> 32) == tag && s != SLOT_TOMB) {
+                    uint32_t idx = (uint32_t)s;
+                    if (idx != IDX_BUSY) {
+                        __threadfence();
+                        if (key_equal(I, idx, c, types, mask)) {
+                            result = ld_cg(I.ids + idx);
+                            done = true;
+                        } else {
+                            pos = (pos + 1) & I.table_mask;
+                            ++probes;
+                        }
+                    }  // else: retry the same slot next round
+                } else {
+                    pos = (pos + 1) & I.table_mask;
+                    ++probes;
+                }
+                if (!done && probes > I.max_probes) {
+                    set_error(I, ERR_TABLE_FULL, 1);
+                    done = true;
+                }
+            }
+        }
+        const unsigned cm = __ballot_sync(0xFFFFFFFFu, claimed);
+        if (cm) {
+            unsigned long long base = 0;
+            const int leader = __ffs(cm) - 1;
+            if ((int)lane == leader) base = atomicAdd(&I.ctr->alloc_count, (unsigned long long)__popc(cm));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (claimed) {
+                const unsigned rank = __popc(cm & ((1u << lane) - 1u));
+                const uint32_t idx = node_for_ticket(I, base + rank);
+                if (idx == NO_NODE) {
+                    set_error(I, ERR_OOM, 1);
+                    atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
+                } else {
+                    result = write_branch(I, idx, c, types, mask, h, lod);
+                    __threadfence();
+                    atomicExch((unsigned long long *)(I.table + pos), make_slot(tag, idx));
+                    *created = true;
+                }
+                done = true;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, !done)) break;
+        if (round >= ROUND_LIMIT) {
+            if (!done) {
+                set_error(I, ERR_TIMEOUT, 2);
+                done = true;
+            }
+            break;
+        }
+        if (!done && !claimed) __nanosleep(0);
+    }
+    return result;
+}
+
+// Find-or-create of the leaf for value v (v != 0) through the direct-mapped leaf table.
+// *created tells whether this call allocated the leaf (its refcount starts at 0).
+__device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v, bool *created) {
+    *created = false;
+    unsigned long long *slot = (unsigned long long *)(I.leaf_table + v);
+    uint64_t s = ld_volatile(I.leaf_table + v);
+    if (s > LEAF_BUSY) return s;
+    if (s == 0) {
+        uint64_t prev = atomicCAS(slot, 0ull, LEAF_BUSY);
+        if (prev == 0) {
+            unsigned long long t = atomicAdd(&I.ctr->alloc_count, 1ull);
+            uint32_t idx = node_for_ticket(I, t);
+            if (idx == NO_NODE) {
+                set_error(I, ERR_OOM, 2);
+                atomicExch(slot, 0ull);
+                return INVALID_ID;
+            }
+            uint32_t gen = I.generation[idx];
+            uint64_t id = make_leaf_id(idx, gen);
+            set_node_value(I, idx, v);
+            I.hash[idx] = 0;
+            I.refcount[idx] = 0;
+            I.ids[idx] = id;
+            __threadfence();
+            atomicExch(slot, id);
+            *created = true;
+            return id;
+        }
+        if (prev > LEAF_BUSY) return prev;
+    }
+    for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin) {
+        s = ld_volatile(I.leaf_table + v);
+        if (s > LEAF_BUSY) return s;
+        if (s == 0) return intern_leaf(I, v, created);  // creator ran out of memory and backed off
+        __nanosleep(64);
+    }
+    set_error(I, ERR_TIMEOUT, 3);
+    return INVALID_ID;
+}
+
+// Removes a dead node from its table, clears the record, bumps the generation and pushes the slot
+// on the free list (recycle, interner/mod.rs:566-625). `free_pos` is the free-list position.
+__device__ __forceinline__ void recycle_node(const DevInterner &I, uint32_t idx, unsigned long long free_pos) {
+    uint64_t id = I.ids[idx];
+    if (id_is_leaf(id)) {
+        uint32_t v = node_value(I, idx);
+        atomicCAS((unsigned long long *)(I.leaf_table + v), id, 0ull);
+    } else {
+        uint64_t h = I.hash[idx];
+        uint32_t tag = slot_tag(h);
+        uint64_t pos = h & I.table_mask;
+        bool removed = false;
+        for (uint32_t p = 0; p <= I.max_probes; ++p) {
+            uint64_t s = ld_volatile(I.table + pos);
+            if (s == SLOT_EMPTY) break;
+            if (s == make_slot(tag, idx)) {
+                atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
+                removed = true;
+                break;
+            }
+            pos = (pos + 1) & I.table_mask;
+        }
+        if (!removed) set_error(I, ERR_INTERNAL, 10);
+        ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(I.children + 8ull * idx);
+        dst[0] = dst[1] = dst[2] = dst[3] = make_ulonglong2(0ull, 0ull);
+    }
+    set_node_value(I, idx, 0);
+    I.hash[idx] = 0;
+    I.refcount[idx] = 0;
+    I.ids[idx] = 0;
+    uint32_t g = (uint32_t)I.generation[idx] + 1u;
+    if (g >= MAX_GENERATION) g = 0;
+    I.generation[idx] = (uint16_t)g;
+    I.free_list[free_pos] = idx;
+}
+
+}  // namespace vxg

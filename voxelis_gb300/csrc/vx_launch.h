@@ -1,0 +1,95 @@
+// Host-side launchers of the device kernels (one declaration per kernel family).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "vx_device.cuh"
+
+namespace vxg {
+
+// Process-wide count of kernels launched by this library (reported by vx_kernel_launches).
+void count_launches(uint64_t n);
+
+// ---- dense-chunk construction on EMPTY trees (vx_build.cu) -----------------------------------
+struct DenseArgs {
+    const void *grids;           // n_chunks * side^3 voxels, [y][z][x] per chunk
+    const uint32_t *trees;       // tree handle per chunk
+    uint32_t n_chunks;
+    int depth;                   // chunk depth d (2..10)
+    int bdepth;                  // depth of one shared-memory block, min(d, 5)
+    uint32_t blocks_per_chunk;   // 8^(d - bdepth)
+    uint64_t *block_roots;       // [n_chunks * blocks_per_chunk] when d > bdepth
+    uint32_t *block_vals;        // LOD values of block roots
+    uint8_t *changed;            // [n_chunks] or null
+};
+// Builds the level-(d - bdepth) subtrees of every chunk (or the whole tree when d <= 5).
+cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s);
+// One level of fresh parents above the blocks: n_parents = n_chunks * 8^k.
+cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
+                               uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
+                               const uint32_t *trees, uint8_t *changed, cudaStream_t s);
+// In-degree refcounts of the nodes created in the current epoch, then closes the epoch.
+cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s);
+cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
+
+// ---- general batch apply (vx_apply.cu) ---------------------------------------------------------
+struct ApplyArgs {
+    int mode;                    // 0: set phase (set_batch_at_depth_iterative); 1: clear pass (P4)
+    uint32_t n_items;
+    uint32_t n_records;
+    int max_depth;
+    // items (ordered by depth, deepest first)
+    const uint32_t *it_tree;
+    const uint8_t *it_depth;
+    const uint8_t *it_flags;     // bit0 has_fill, bit1 has_patches
+    const uint32_t *it_fill;
+    uint64_t *it_init;           // scratch
+    uint64_t *it_old;
+    uint64_t *it_new;
+    uint8_t *it_panic;
+    uint8_t *it_changed;         // result
+    // records sorted by (item, group)
+    const uint32_t *rec_item;
+    const uint32_t *rec_group;
+    const uint8_t *rec_set;
+    const uint8_t *rec_clear;
+    const uint16_t *rec_vals;    // [n_records * 8]
+    // scratch
+    uint32_t *flags;             // [n_records + 1]
+    uint32_t *pos;               // [n_records + 1]
+    uint32_t *scan_tmp;          // block sums
+    uint32_t *e_item[2];
+    uint32_t *e_path[2];
+    uint64_t *e_id[2];
+    uint32_t *e_val[2];
+    uint32_t *p_start;           // [n_records + 1]
+    uint64_t *rec_id;
+    uint32_t *rec_val;
+    uint64_t *release_list;      // [n_items]
+};
+cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
+// Counter slots used by launch_apply (DevCounters::scratch indices).
+enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5 };
+
+// Inclusive-to-exclusive scan of n u32 flags (n from the host) into pos; pos[n] = total.
+cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s);
+size_t scan_tmp_words(uint32_t n);
+
+// ---- reads, releases, single-voxel operations, maintenance (vx_ops.cu) -------------------------
+cudaError_t launch_get_many(const DevInterner &I, uint64_t n, const uint32_t *trees, const int32_t *xyz,
+                            uint8_t *found, void *values, int num_sms, cudaStream_t s);
+// Releases the roots listed in `list` (count at ctr->scratch[SC_RELEASE]) with `rounds`
+// breadth-first rounds, using two frontier buffers of `frontier_cap` entries.
+cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,
+                           uint64_t frontier_cap, int rounds, int num_sms, cudaStream_t s);
+// Single-voxel VoxTree::set / fill / clear executed by one thread with the reference's own
+// refcount order; the result status word is written to *status_out.
+cudaError_t launch_tree_set(const DevInterner &I, uint32_t tree, int32_t x, int32_t y, int32_t z, uint32_t v,
+                            uint64_t *queue, uint64_t queue_cap, int *status_out, cudaStream_t s);
+cudaError_t launch_tree_fill(const DevInterner &I, uint32_t tree, uint32_t v, uint64_t *queue,
+                             uint64_t queue_cap, int *status_out, cudaStream_t s);
+cudaError_t launch_rehash(const DevInterner &I, uint64_t table_slots, int num_sms, cudaStream_t s);
+cudaError_t launch_count_live(const DevInterner &I, unsigned long long *out2, int num_sms, cudaStream_t s);
+
+}  // namespace vxg

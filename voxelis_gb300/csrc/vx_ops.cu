@@ -1,0 +1,587 @@
+// Batched reads, releases, single-voxel edits and table maintenance.
+//
+//   get_many      VoxTree::get -> get_at_depth (voxtree.rs:145-159, utils/common.rs:122-156), one
+//                 thread per query descending at most d levels through the L2-resident node array.
+//   release       dec_ref_recursive (interner/mod.rs:419-534) for many roots at once, breadth
+//                 first: a round decrements the children of the nodes that died in the previous
+//                 round; a child whose count reaches zero dies in the next round. Dead nodes leave
+//                 their table, are cleared, get a new generation and go on the free list
+//                 (recycle, interner/mod.rs:566-625).
+//   set / fill    VoxTree::set (voxtree.rs:163-260, 393-706) and fill/clear (voxtree.rs:264-292)
+//                 run by a single thread with the reference's own refcount order (hit: give back
+//                 the children's references, interner/mod.rs:767-772), its LIFO free list and its
+//                 32768-entry release queue (P3 lifts the limit).
+//   rehash        rebuilds the branch table from the live nodes once tombstones accumulate.
+#include "vx_launch.h"
+
+namespace vxg {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) get_kernel(DevInterner I, uint64_t n, const uint32_t *trees,
+                                                      const int32_t *xyz, uint8_t *found, T *values) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    bool oob = false, bad = false;
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+        const uint32_t t = __ldg(trees + q);
+        const int d = t < I.tree_cap ? I.depths[t] : TREE_UNUSED;
+        const int32_t x = __ldg(xyz + 3 * q), y = __ldg(xyz + 3 * q + 1), z = __ldg(xyz + 3 * q + 2);
+        uint32_t val = 0;
+        uint8_t f = 0;
+        if (d == TREE_UNUSED) {
+            bad = true;
+        } else if (x < 0 || y < 0 || z < 0 || x >= (1 << d) || y >= (1 << d) || z >= (1 << d)) {
+            oob = true;
+        } else {
+            uint64_t node = I.roots[t];
+            int depth = 0;
+            while (node != EMPTY_ID) {
+                if (depth >= d) {
+                    const uint32_t v = node_value(I, id_index(node));
+                    if (v != 0) {
+                        val = v;
+                        f = 1;
+                    }
+                    break;
+                }
+                if (id_is_branch(node)) {
+                    const int shift = d - depth - 1;
+                    const uint32_t ci = ((x >> shift) & 1) | (((y >> shift) & 1) << 1) | (((z >> shift) & 1) << 2);
+                    node = __ldg(reinterpret_cast<const unsigned long long *>(I.children) + 8ull * id_index(node) + ci);
+                    ++depth;
+                } else {
+                    val = node_value(I, id_index(node));
+                    f = 1;
+                    break;
+                }
+            }
+        }
+        found[q] = f;
+        values[q] = (T)val;
+    }
+    if (oob) set_error(I, ERR_OOB, 50);
+    if (bad) set_error(I, ERR_INVALID, 51);
+}
+
+// ---- release -----------------------------------------------------------------------------------
+__device__ __forceinline__ void push_dying(uint32_t *list, unsigned long long *count, bool push, uint32_t idx) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
+    if (!m) return;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long base = 0;
+    const int leader = __ffs(m) - 1;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (push) list[base + __popc(m & ((1u << lane) - 1u))] = idx;
+}
+
+// Decrements each listed root; roots whose count reaches zero become the first dying set.
+__global__ void __launch_bounds__(kThreads) release_roots_kernel(DevInterner I, const uint64_t *list,
+                                                                uint32_t *out) {
+    const uint64_t n = I.ctr->scratch[SC_RELEASE];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint64_t j = base + threadIdx.x;
+        bool dies = false;
+        uint32_t idx = 0;
+        if (j < n) {
+            const uint64_t id = list[j];
+            if (id != EMPTY_ID) {
+                idx = id_index(id);
+                const unsigned old = atomicSub(I.refcount + idx, 1u);
+                if (old == 0) {
+                    atomicAdd(I.refcount + idx, 1u);
+                    set_error(I, ERR_REF_UB, 60);
+                } else {
+                    dies = old == 1;
+                }
+            }
+        }
+        push_dying(out, &I.ctr->scratch[SC_REL_OUT], dies, idx);
+    }
+}
+
+// Retires the dying nodes of `in`: their children lose one reference each (children reaching zero
+// are the next dying set) and the nodes are recycled.
+__global__ void __launch_bounds__(kThreads) release_round_kernel(DevInterner I, const uint32_t *in, uint32_t *out) {
+    const uint64_t n = I.ctr->scratch[SC_REL_IN];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint64_t j = base + threadIdx.x;
+        const bool in_range = j < n;
+        const uint32_t idx = in_range ? in[j] : 0u;
+        const uint64_t id = in_range ? I.ids[idx] : 0ull;
+        const bool branch = in_range && id != 0 && id_is_branch(id);
+        for (int k = 0; k < 8; ++k) {
+            bool dies = false;
+            uint32_t cidx = 0;
+            if (branch) {
+                const uint64_t c = I.children[8ull * idx + k];
+                if (c != EMPTY_ID) {
+                    cidx = id_index(c);
+                    const unsigned old = atomicSub(I.refcount + cidx, 1u);
+                    if (old == 0) {
+                        atomicAdd(I.refcount + cidx, 1u);
+                        set_error(I, ERR_REF_UB, 61);
+                    } else {
+                        dies = old == 1;
+                    }
+                }
+            }
+            push_dying(out, &I.ctr->scratch[SC_REL_OUT], dies, cidx);
+        }
+        const bool rec = in_range && id != 0;
+        if (in_range && id == 0) set_error(I, ERR_INTERNAL, 62);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, rec);
+        unsigned long long fbase = 0;
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            if ((int)lane == leader) fbase = atomicAdd(&I.ctr->free_count, (unsigned long long)__popc(m));
+            fbase = __shfl_sync(0xFFFFFFFFu, fbase, leader);
+        }
+        unsigned tomb = __ballot_sync(0xFFFFFFFFu, rec && branch);
+        if (lane == 0 && tomb) atomicAdd(&I.ctr->tombstones, (unsigned long long)__popc(tomb));
+        if (rec) recycle_node(I, idx, fbase + __popc(m & ((1u << lane) - 1u)));
+    }
+}
+
+__global__ void release_advance_kernel(DevInterner I) {
+    I.ctr->scratch[SC_REL_IN] = I.ctr->scratch[SC_REL_OUT];
+    I.ctr->scratch[SC_REL_OUT] = 0;
+}
+
+// ---- single-thread reference-order operations ---------------------------------------------------
+struct Seq {
+    DevInterner I;
+    uint64_t *queue;
+    uint64_t queue_cap;
+    bool ok;
+};
+
+__device__ uint32_t seq_alloc(Seq &S) {
+    DevCounters *c = S.I.ctr;
+    if (c->free_count > 0) {
+        c->free_count -= 1;
+        return S.I.free_list[c->free_count];
+    }
+    if (c->next_index >= S.I.capacity) {
+        set_error(S.I, ERR_OOM, 70);
+        S.ok = false;
+        return NO_NODE;
+    }
+    return (uint32_t)(c->next_index++);
+}
+
+__device__ void seq_recycle(Seq &S, uint32_t idx) {
+    const bool branch = id_is_branch(S.I.ids[idx]);
+    recycle_node(S.I, idx, S.I.ctr->free_count);
+    S.I.ctr->free_count += 1;
+    if (branch) S.I.ctr->tombstones += 1;
+}
+
+__device__ bool seq_valid(Seq &S, uint64_t id) {
+    const uint32_t i = id_index(id);
+    return i < S.I.capacity && S.I.generation[i] == id_generation(id);
+}
+
+__device__ void seq_dec(Seq &S, uint64_t id) {  // dec_ref (interner/mod.rs:260-296)
+    const uint32_t i = id_index(id);
+    if (S.I.refcount[i] == 0) {
+        set_error(S.I, ERR_REF_UB, 71);
+        S.ok = false;
+        return;
+    }
+    S.I.refcount[i] -= 1;
+    if (S.I.refcount[i] == 0) seq_recycle(S, i);
+}
+
+// get_or_create_leaf (interner/mod.rs:627-710)
+__device__ uint64_t seq_leaf(Seq &S, uint32_t v) {
+    const uint64_t s = S.I.leaf_table[v];
+    if (s > LEAF_BUSY) {
+        S.I.refcount[id_index(s)] += 1;
+        return s;
+    }
+    const uint32_t idx = seq_alloc(S);
+    if (idx == NO_NODE) return INVALID_ID;
+    const uint64_t id = make_leaf_id(idx, S.I.generation[idx]);
+    set_node_value(S.I, idx, v);
+    S.I.hash[idx] = 0;
+    S.I.ids[idx] = id;
+    S.I.refcount[idx] = 1;
+    S.I.leaf_table[v] = id;
+    return id;
+}
+
+// get_or_create_branch (interner/mod.rs:712-829)
+__device__ uint64_t seq_branch(Seq &S, const uint64_t c[8], uint32_t types, uint32_t mask) {
+    const DevInterner &I = S.I;
+    const uint64_t h = branch_fingerprint(c, (types << 8) | mask);
+    const uint32_t tag = slot_tag(h);
+    uint64_t pos = h & I.table_mask;
+    for (uint32_t p = 0; p <= I.max_probes; ++p, pos = (pos + 1) & I.table_mask) {
+        const uint64_t s = I.table[pos];
+        if (s == SLOT_EMPTY) {
+            const uint32_t idx = seq_alloc(S);
+            if (idx == NO_NODE) return INVALID_ID;
+            uint32_t cv[8];
+            for (int k = 0; k < 8; ++k) cv[k] = node_value(I, id_index(c[k]));
+            const uint64_t id = write_branch(I, idx, c, types, mask, h, calc_average8(cv));
+            I.refcount[idx] = 1;
+            I.table[pos] = make_slot(tag, idx);
+            return id;
+        }
+        if ((uint32_t)(s >> 32) == tag && s != SLOT_TOMB && key_equal(I, (uint32_t)s, c, types, mask)) {
+            const uint64_t existing = I.ids[(uint32_t)s];
+            for (int k = 0; k < 8; ++k)
+                if (c[k] != EMPTY_ID) seq_dec(S, c[k]);
+            I.refcount[(uint32_t)s] += 1;
+            return existing;
+        }
+    }
+    set_error(I, ERR_TABLE_FULL, 72);
+    S.ok = false;
+    return INVALID_ID;
+}
+
+// dec_ref_recursive (interner/mod.rs:419-534) with its fixed queue (grown under P3).
+__device__ void seq_release(Seq &S, uint64_t root) {
+    const DevInterner &I = S.I;
+    uint64_t r = 0, w = 1;
+    S.queue[0] = root;
+    while (r < w && S.ok) {
+        const uint64_t cur = S.queue[r++];
+        const uint32_t ci = id_index(cur);
+        if (I.refcount[ci] == 0) {
+            set_error(I, ERR_REF_UB, 73);
+            S.ok = false;
+            return;
+        }
+        I.refcount[ci] -= 1;
+        if (I.refcount[ci] != 0) continue;
+        for (int k = 0; k < 8; ++k) {
+            const uint64_t child = I.children[8ull * ci + k];
+            if (child == EMPTY_ID) continue;
+            const uint32_t k2 = id_index(child);
+            if (I.refcount[k2] > 1) {
+                I.refcount[k2] -= 1;
+            } else {
+                if (w >= S.queue_cap) {
+                    set_error(I, ERR_REF_UB, 74);  // release queue overflow (interner/mod.rs:509-513)
+                    S.ok = false;
+                    return;
+                }
+                S.queue[w++] = child;
+            }
+        }
+        seq_recycle(S, ci);
+    }
+}
+
+__device__ __forceinline__ uint32_t cidx(int32_t x, int32_t y, int32_t z, int cur, int max) {
+    const int sh = max - cur - 1;
+    return ((x >> sh) & 1) | (((y >> sh) & 1) << 1) | (((z >> sh) & 1) << 2);
+}
+
+// set_at_depth_iterative (voxtree.rs:393-540)
+__device__ uint64_t seq_set(Seq &S, uint64_t root, int32_t x, int32_t y, int32_t z, int d, uint32_t voxel) {
+    const DevInterner &I = S.I;
+    uint64_t st_node[11], st_leaf[11];
+    uint32_t st_idx[11];
+    uint64_t cur = root, leaf = EMPTY_ID;
+    int depth = 0;
+    while (depth < d) {
+        const uint32_t index = cidx(x, y, z, depth, d);
+        if (id_is_branch(cur)) {
+            st_node[depth] = cur;
+            st_leaf[depth] = leaf;
+            st_idx[depth] = index;
+            cur = I.children[8ull * id_index(cur) + index];
+        } else {
+            if (node_value(I, id_index(cur)) == voxel) return INVALID_ID;
+            leaf = cur;
+            cur = EMPTY_ID;
+            st_node[depth] = cur;
+            st_leaf[depth] = leaf;
+            st_idx[depth] = index;
+        }
+        ++depth;
+    }
+    if (id_is_leaf(cur) && node_value(I, id_index(cur)) == voxel) return INVALID_ID;
+    cur = seq_leaf(S, voxel);
+    while (depth > 0 && S.ok) {
+        --depth;
+        const uint64_t pn = st_node[depth], pl = st_leaf[depth];
+        const uint32_t pi = st_idx[depth];
+        if (pn != EMPTY_ID) {
+            const uint32_t types = id_types(pn) | ((id_is_leaf(cur) ? 1u : 0u) << pi);
+            uint64_t br[8];
+            for (int k = 0; k < 8; ++k) br[k] = I.children[8ull * id_index(pn) + k];
+            br[pi] = cur;
+            bool same = types == 0xFF;
+            for (int k = 0; k < 8; ++k) same = same && br[k] == cur;
+            if (!same) {
+                const uint32_t mask = id_mask(pn) | (1u << pi);
+                for (int k = 0; k < 8; ++k)
+                    if (k != (int)pi && br[k] != EMPTY_ID) I.refcount[id_index(br[k])] += 1;
+                cur = seq_branch(S, br, types, mask);
+            }
+        } else if (pl == EMPTY_ID) {
+            uint64_t ch[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            ch[pi] = cur;
+            cur = seq_branch(S, ch, (id_is_leaf(cur) ? 1u : 0u) << pi, 1u << pi);
+        } else {
+            uint64_t ch[8];
+            for (int k = 0; k < 8; ++k) ch[k] = pl;
+            I.refcount[id_index(pl)] += 7;
+            ch[pi] = cur;
+            const uint32_t types = ((~(1u << pi)) | ((id_is_leaf(cur) ? 1u : 0u) << pi)) & 0xFFu;
+            cur = seq_branch(S, ch, types, 0xFF);
+        }
+    }
+    return cur;
+}
+
+// remove_at_depth / _branch / _leaf (voxtree.rs:542-706), unrolled into a descent and an ascent.
+__device__ uint64_t seq_remove(Seq &S, uint64_t root, int32_t x, int32_t y, int32_t z, int d) {
+    const DevInterner &I = S.I;
+    uint64_t frames[11];
+    int depth = 0;
+    uint64_t node = root;
+    uint64_t result;
+    while (true) {
+        if (!seq_valid(S, node)) {
+            set_error(I, ERR_REF_PANIC, 75);
+            S.ok = false;
+            return INVALID_ID;
+        }
+        if (id_is_branch(node)) {
+            if (!(depth < d)) {
+                set_error(I, ERR_REF_PANIC, 76);  // "Branch node at max depth"
+                S.ok = false;
+                return INVALID_ID;
+            }
+            const uint32_t index = cidx(x, y, z, depth, d);
+            if (!((id_mask(node) >> index) & 1)) return INVALID_ID;
+            frames[depth] = node;
+            node = I.children[8ull * id_index(node) + index];
+            ++depth;
+            continue;
+        }
+        // remove_at_depth_leaf from `depth` down to d, built bottom-up
+        result = EMPTY_ID;
+        for (int k = d - 1; k >= depth && S.ok; --k) {
+            const uint32_t index = cidx(x, y, z, k, d);
+            uint64_t ch[8];
+            for (int j = 0; j < 8; ++j) ch[j] = node;
+            ch[index] = result;
+            const bool lf = id_is_leaf(result), em = result == EMPTY_ID;
+            const uint32_t types = ((~(1u << index)) | ((lf ? 1u : 0u) << index)) & 0xFFu;
+            const uint32_t mask = ((~(1u << index)) | ((!em ? 1u : 0u) << index)) & 0xFFu;
+            I.refcount[id_index(node)] += 7;
+            result = seq_branch(S, ch, types, mask);
+        }
+        break;
+    }
+    // ascend through the branch frames (remove_at_depth_branch)
+    while (depth > 0 && S.ok) {
+        --depth;
+        const uint64_t pn = frames[depth];
+        const uint32_t index = cidx(x, y, z, depth, d);
+        const bool empty = result == EMPTY_ID;
+        const uint32_t mask = empty ? (id_mask(pn) & ~(1u << index)) : id_mask(pn);
+        if (mask == 0) {
+            result = EMPTY_ID;
+            continue;
+        }
+        if (!id_is_branch(result)) {
+            set_error(I, ERR_REF_PANIC, 77);  // "Removing voxel should never produce a leaf node"
+            S.ok = false;
+            return INVALID_ID;
+        }
+        const uint32_t types = id_types(pn) & ~(1u << index);
+        uint64_t br[8];
+        for (int k = 0; k < 8; ++k) br[k] = I.children[8ull * id_index(pn) + k];
+        br[index] = result;
+        for (int k = 0; k < 8; ++k)
+            if (k != (int)index && br[k] != EMPTY_ID) I.refcount[id_index(br[k])] += 1;
+        result = seq_branch(S, br, types, mask);
+    }
+    return result;
+}
+
+// VoxTree::set (voxtree.rs:163-260). status: 0 unchanged, 1 changed, -1 error.
+__global__ void tree_set_kernel(DevInterner I, uint32_t tree, int32_t x, int32_t y, int32_t z, uint32_t v,
+                                uint64_t *queue, uint64_t queue_cap, int *status) {
+    Seq S{I, queue, queue_cap, true};
+    const uint64_t root = I.roots[tree];
+    const int d = I.depths[tree];
+    *status = 0;
+    if (root == EMPTY_ID && v == 0) return;
+    const uint64_t nw = v != 0 ? seq_set(S, root, x, y, z, d, v) : seq_remove(S, root, x, y, z, d);
+    if (!S.ok) {
+        *status = -1;
+        return;
+    }
+    if (nw == INVALID_ID) return;
+    if (root != EMPTY_ID) {
+        if (nw == root) {
+            set_error(I, ERR_REF_PANIC, 78);
+            *status = -1;
+            return;
+        }
+        seq_release(S, root);
+        if (!S.ok) {
+            *status = -1;
+            return;
+        }
+    }
+    I.roots[tree] = nw;
+    *status = 1;
+}
+
+// VoxTree::fill / clear (voxtree.rs:264-292). status: 1 if the tree was dirtied.
+__global__ void tree_fill_kernel(DevInterner I, uint32_t tree, uint32_t v, uint64_t *queue, uint64_t queue_cap,
+                                 int *status) {
+    Seq S{I, queue, queue_cap, true};
+    const uint64_t root = I.roots[tree];
+    *status = 0;
+    if (root != EMPTY_ID) {
+        seq_release(S, root);
+        if (!S.ok) {
+            *status = -1;
+            return;
+        }
+        I.roots[tree] = EMPTY_ID;
+        *status = 1;
+    }
+    if (v != 0) {
+        const uint64_t leaf = seq_leaf(S, v);
+        if (!S.ok) {
+            *status = -1;
+            return;
+        }
+        I.roots[tree] = leaf;
+        *status = 1;
+    }
+}
+
+// ---- maintenance -------------------------------------------------------------------------------
+__global__ void rehash_kernel(DevInterner I) {
+    const unsigned long long n = I.ctr->next_index;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x + 1; idx < n;
+         idx += stride) {
+        const uint64_t id = I.ids[idx];
+        if (id == 0 || id_is_leaf(id)) continue;
+        const uint64_t h = I.hash[idx];
+        uint64_t pos = h & I.table_mask;
+        const uint64_t slot = make_slot(slot_tag(h), (uint32_t)idx);
+        bool placed = false;
+        for (uint32_t p = 0; p <= I.max_probes; ++p, pos = (pos + 1) & I.table_mask)
+            if (atomicCAS((unsigned long long *)(I.table + pos), SLOT_EMPTY, slot) == SLOT_EMPTY) {
+                placed = true;
+                break;
+            }
+        if (!placed) set_error(I, ERR_TABLE_FULL, 80);
+    }
+}
+
+__global__ void rehash_done_kernel(DevInterner I) { I.ctr->tombstones = 0; }
+
+__global__ void count_live_kernel(DevInterner I, unsigned long long *out2) {
+    const unsigned long long n = I.ctr->next_index;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long br = 0, lf = 0;
+    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x + 1; idx < n;
+         idx += stride) {
+        const uint64_t id = I.ids[idx];
+        if (id == 0) continue;
+        if (id_is_leaf(id))
+            ++lf;
+        else
+            ++br;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        br += __shfl_down_sync(0xFFFFFFFFu, br, o);
+        lf += __shfl_down_sync(0xFFFFFFFFu, lf, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (br) atomicAdd(out2, br);
+        if (lf) atomicAdd(out2 + 1, lf);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_get_many(const DevInterner &I, uint64_t n, const uint32_t *trees, const int32_t *xyz,
+                            uint8_t *found, void *values, int num_sms, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint64_t blocks = (n + kThreads - 1) / kThreads;
+    const uint64_t cap = (uint64_t)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    count_launches(1);
+    if (I.vbits == 8)
+        get_kernel<uint8_t><<<(unsigned)blocks, kThreads, 0, s>>>(I, n, trees, xyz, found, (uint8_t *)values);
+    else
+        get_kernel<uint16_t><<<(unsigned)blocks, kThreads, 0, s>>>(I, n, trees, xyz, found, (uint16_t *)values);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,
+                           uint64_t frontier_cap, int rounds, int num_sms, cudaStream_t s) {
+    (void)frontier_cap;
+    const unsigned g = (unsigned)num_sms * 4;
+    count_launches(1);
+    release_advance_kernel<<<1, 1, 0, s>>>(I);  // clears the output count
+    count_launches(1);
+    release_roots_kernel<<<g, kThreads, 0, s>>>(I, list, frontier_a);
+    uint32_t *in = frontier_a, *out = frontier_b;
+    for (int r = 0; r < rounds; ++r) {
+        count_launches(1);
+        release_advance_kernel<<<1, 1, 0, s>>>(I);
+        count_launches(1);
+        release_round_kernel<<<g, kThreads, 0, s>>>(I, in, out);
+        uint32_t *t = in;
+        in = out;
+        out = t;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tree_set(const DevInterner &I, uint32_t tree, int32_t x, int32_t y, int32_t z, uint32_t v,
+                            uint64_t *queue, uint64_t queue_cap, int *status_out, cudaStream_t s) {
+    count_launches(1);
+    tree_set_kernel<<<1, 1, 0, s>>>(I, tree, x, y, z, v, queue, queue_cap, status_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tree_fill(const DevInterner &I, uint32_t tree, uint32_t v, uint64_t *queue,
+                             uint64_t queue_cap, int *status_out, cudaStream_t s) {
+    count_launches(1);
+    tree_fill_kernel<<<1, 1, 0, s>>>(I, tree, v, queue, queue_cap, status_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rehash(const DevInterner &I, uint64_t table_slots, int num_sms, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(I.table, 0xFF, table_slots * sizeof(uint64_t), s);
+    if (e != cudaSuccess) return e;
+    count_launches(1);
+    rehash_kernel<<<num_sms * 4, kThreads, 0, s>>>(I);
+    count_launches(1);
+    rehash_done_kernel<<<1, 1, 0, s>>>(I);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_live(const DevInterner &I, unsigned long long *out2, int num_sms, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    count_launches(1);
+    count_live_kernel<<<num_sms * 4, kThreads, 0, s>>>(I, out2);
+    return cudaGetLastError();
+}
+
+}  // namespace vxg
