@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--quick", action="store_true",
+                   help="timed build steps and gets only (no per-chunk, e2e or CPU legs); for profiling")
     return p.parse_args()
 
 
@@ -337,6 +339,13 @@ def run_ours(args):
     ti = {int(t): i for i, t in enumerate(trees)}
     ref_v = np.array([grids_np[ti[int(qt[k])], qxyz[k, 1], qxyz[k, 2], qxyz[k, 0]] for k in range(65536)])
     gets_ok = bool(np.array_equal(v_h, ref_v) and np.array_equal(f_h.astype(bool), ref_v != 0))
+
+    if args.quick:
+        print(json.dumps({"quick": True, "ms_per_step": ms, "chunks_per_s": n / (ms * 1e-3), "gets_ms": gms,
+                          "dense_kernel_ms": dense_ms, "algorithmic_bytes": int(algo_bytes), "gets_ok": gets_ok,
+                          "gpu_launches": int(launches)}))
+        call("interner_destroy")
+        return
 
     # canonical DAG of the batched build, then the per-chunk path on the same grids
     canon = export(lib, h, trees)
