@@ -212,6 +212,19 @@ int vx_profile_enable(vx_interner *it, int on);
 int vx_profile_collect(vx_interner *it, double *ms, uint64_t *count);
 /* Number of kernels this library has launched in this process. */
 uint64_t vx_kernel_launches(void);
+/* Dense-chunk construction that allocates no memory (no counterpart in the reference).
+ * Same arguments and result as vx_build_dense_async, for callers that cannot allocate device memory
+ * during the call: code recorded into a CUDA graph (allocation is not allowed during stream
+ * capture), frame loops and servers that fix their memory up front, hosts whose allocator belongs
+ * to another runtime. The levels above 32^3 blocks are staged in a fixed device array of
+ * VX_NOALLOC_SCRATCH_ENTRIES entries compiled into the library (3 MiB per GPU, held until exit):
+ * chunks of depth d > 5 need n * (8^(d-5) + ... + 8) entries, and larger requests return
+ * VX_E_BUFFER without queuing work. All calls share the array: calls whose device work overlaps
+ * race, so serialise them. The first call on a device resolves the array's address and must come
+ * before any stream capture. */
+#define VX_NOALLOC_SCRATCH_ENTRIES (1u << 18)
+int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
+                           const void *grids_dev, uint8_t *changed_dev, int max_depth);
 /* Returns the interner to its freshly created state (no nodes, empty tables); tree handles stay
  * valid and their roots become EMPTY. Same result as destroying it and creating a new interner with
  * the same budget, without reallocating device memory. */

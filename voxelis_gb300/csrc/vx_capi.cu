@@ -529,6 +529,25 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
 
 }  // namespace
 
+namespace vxg {
+// The device view, stream and SM count of an interner, for entry points compiled in other
+// translation units. When `marks_trees` is set, every tree of the interner counts as possibly
+// non-empty afterwards (the caller names trees by device handles the host does not inspect).
+bool interner_parts(vx_interner *it, DevInterner *dev, cudaStream_t *stream, int *num_sms, uint32_t *flags,
+                    bool marks_trees) {
+    if (!it) return false;
+    *dev = it->dev;
+    *stream = it->stream;
+    *num_sms = it->num_sms;
+    *flags = it->flags;
+    if (marks_trees) it->all_trees_unknown = true;
+    return true;
+}
+void interner_set_error(vx_interner *it, const char *msg) {
+    if (it) it->last_error = msg;
+}
+}  // namespace vxg
+
 extern "C" {
 
 // ---- interner ---------------------------------------------------------------------------------
