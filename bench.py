@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--workload", default="dunes", choices=["dunes", "edits", "serve"],
+                   help="dunes: batched dense build of 4096 32^3 chunks (default); edits: uneven batched edits")
     p.add_argument("--quick", action="store_true",
                    help="timed build steps and gets only (no per-chunk, e2e or CPU legs); for profiling")
     return p.parse_args()
@@ -450,7 +452,15 @@ def export(lib, h, trees):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "edits":
+        from voxelis_gb300 import bench_edits
+
+        bench_edits.run(args)
+    elif args.workload == "serve":
+        from voxelis_gb300 import bench_serve
+
+        bench_serve.run(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -151,6 +151,9 @@ int vx_batch_set(vx_batch *b, int32_t x, int32_t y, int32_t z, uint32_t value);
 int vx_batch_fill(vx_batch *b, uint32_t value);
 /* Batch::just_clear (batch.rs:187-195). */
 int vx_batch_clear(vx_batch *b);
+/* Batch::just_set for n voxels in order (xyz[3i..3i+2], values[i]); stops at the first invalid
+ * position or value and reports it. */
+int vx_batch_set_many(vx_batch *b, uint64_t n, const int32_t *xyz, const uint32_t *values);
 /* just_set over every voxel of a dense grid laid out [y][z][x] (utils/common.rs:229-230),
  * elements of the batch's voxel width. */
 int vx_batch_set_dense(vx_batch *b, const void *grid);
@@ -185,6 +188,42 @@ int vx_get_many(vx_interner *it, uint64_t n, const vx_tree *trees, const int32_t
 int vx_get_many_async(vx_interner *it, uint64_t n, const vx_tree *trees_dev,
                       const int32_t *xyz_dev, uint8_t *found_dev, void *values_dev);
 
+/* Batched apply_batch over compacted touched groups already in device memory (the Batch's non-empty
+ * (set, clear) groups, core/batch.rs:39-45). Items: trees_dev[i] with item_flags_dev[i] (bit0: the
+ * batch has a fill, bit1: it has patches) and fill_dev[i]; items must be ordered deepest tree first
+ * and name distinct trees. Records r: rec_item_dev[r] (item index), rec_group_dev[r] (bottom-group
+ * Morton index, path >> 3), set/clear masks and 8 values (16-bit elements), ordered by (item, group).
+ * changed_dev (n_items bytes) may be NULL. Equivalent to vx_apply_batches; no host synchronisation. */
+int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *trees_dev,
+                          const uint8_t *item_flags_dev, const uint32_t *fill_dev, uint32_t n_records,
+                          const uint32_t *rec_item_dev, const uint32_t *rec_group_dev,
+                          const uint8_t *rec_set_dev, const uint8_t *rec_clear_dev,
+                          const uint16_t *rec_values_dev, uint8_t *changed_dev, int max_depth);
+/* Launch shape of the batched-apply kernels (threads per block, blocks per SM); chosen by the
+ * autotuner in voxelis_gb300/tune.py. */
+int vx_tune_set(vx_interner *it, int apply_threads, int apply_blocks_per_sm);
+int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm);
+
+/* ---- world helpers for serving (no counterpart in the reference) ---------------------------- */
+/* A grid of nx x ny x nz chunks of depth chunk_depth; the chunk holding world voxel (x, y, z) is
+ * ((y >> d) * nz + (z >> d)) * nx + (x >> d), whose tree handle is trees_dev[chunk] (device memory). */
+typedef struct {
+    int32_t nx, ny, nz;
+    int32_t chunk_depth;
+    const vx_tree *trees_dev;
+} vx_world;
+/* Sphere brushes (integer voxels with |p - center|^2 <= radius^2, clipped to the world) applied in
+ * order as Batch::just_set calls (core/batch.rs:145-172) into one Batch per touched chunk, emitted as
+ * compacted touched groups sorted by (chunk, group): item_chunks[i] is the chunk of item i, and the
+ * record arrays are those of vx_apply_groups_async. Host memory. VX_E_BUFFER reports the sizes. */
+int vx_stage_spheres(int chunk_depth, int32_t nx, int32_t ny, int32_t nz, uint32_t n, const int32_t *centers,
+                     const int32_t *radii, const uint32_t *values, uint64_t cap_items, uint32_t *item_chunks,
+                     uint64_t cap_records, uint32_t *rec_item, uint32_t *rec_group, uint8_t *rec_set,
+                     uint8_t *rec_clear, uint16_t *rec_vals, uint64_t *n_items, uint64_t *n_records);
+/* Batched VoxOpsRead::get at world coordinates (world_xyz_dev[3i..3i+2]) over a vx_world. */
+int vx_world_get_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
+                       uint8_t *found_dev, void *values_dev);
+
 /* ---- verification helpers (not on the timed path) ---------------------------------------- */
 /* Canonical DFS export of the DAG reachable from `trees` (see vx_canonical). On VX_E_BUFFER
  * *n_nodes holds the required capacity. */
@@ -201,10 +240,11 @@ int vx_validate(vx_interner *it, uint32_t n_trees, const vx_tree *trees);
 #define VX_PROF_DENSE 0    /* fused dense-chunk kernel (blocks of up to 32^3 voxels)          */
 #define VX_PROF_LEVELS 1   /* fresh levels above 32^3 blocks (depth > 5)                       */
 #define VX_PROF_REFCOUNT 2 /* end-of-epoch refcount pass and allocator update                  */
-#define VX_PROF_APPLY 3    /* batched apply: bottom groups and level passes                    */
+#define VX_PROF_APPLY 3    /* batched apply: level passes and root commit                      */
 #define VX_PROF_RELEASE 4  /* breadth-first release of replaced roots                          */
 #define VX_PROF_GET 5      /* batched gets                                                     */
 #define VX_PROF_COPY 6     /* host<->device copies made inside an entry point                  */
+#define VX_PROF_BOTTOM 7   /* batched apply: the bottom-group kernel alone (part of APPLY's work) */
 #define VX_PROF_N 8
 int vx_profile_enable(vx_interner *it, int on);
 /* Waits for the stream and returns, per phase, the summed milliseconds and the number of timed
@@ -216,15 +256,18 @@ uint64_t vx_kernel_launches(void);
  * Same arguments and result as vx_build_dense_async, for callers that cannot allocate device memory
  * during the call: code recorded into a CUDA graph (allocation is not allowed during stream
  * capture), frame loops and servers that fix their memory up front, hosts whose allocator belongs
- * to another runtime. The levels above 32^3 blocks are staged in a fixed device array of
- * VX_NOALLOC_SCRATCH_ENTRIES entries compiled into the library (3 MiB per GPU, held until exit):
- * chunks of depth d > 5 need n * (8^(d-5) + ... + 8) entries, and larger requests return
+ * to another runtime. The levels above 16^3 octants are staged in a fixed device array of
+ * VX_NOALLOC_SCRATCH_BYTES compiled into the library (held by every GPU until exit): chunks of depth
+ * d >= 5 need 12 n (8 + ... + 8^(d-4)) + 4 n (1 + ... + 8^(d-5)) bytes, and larger requests return
  * VX_E_BUFFER without queuing work. All calls share the array: calls whose device work overlaps
  * race, so serialise them. The first call on a device resolves the array's address and must come
  * before any stream capture. */
-#define VX_NOALLOC_SCRATCH_ENTRIES (1u << 18)
+#define VX_NOALLOC_SCRATCH_BYTES (3u << 20)
 int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
                            const void *grids_dev, uint8_t *changed_dev, int max_depth);
+/* Waits for the stream, reports the sticky status, and rebuilds the branch table when deleted slots
+ * exceed a quarter of it (the synchronous entry points do this themselves). */
+int vx_interner_maintain(vx_interner *it);
 /* Returns the interner to its freshly created state (no nodes, empty tables); tree handles stay
  * valid and their roots become EMPTY. Same result as destroying it and creating a new interner with
  * the same budget, without reallocating device memory. */

@@ -337,6 +337,17 @@ int vxo_batch_set(void *b, int32_t x, int32_t y, int32_t z, uint32_t value) {
     });
 }
 
+int vxo_batch_set_many(void *b, uint64_t n, const int32_t *xyz, const uint32_t *values) {
+    return with_batch(b, [&](auto &bb) {
+        using T = std::decay_t<decltype(bb.fill_value())>;
+        for (uint64_t i = 0; i < n; ++i) {
+            if (!fits<T>(values[i])) return VX_E_INVALID_ARG;
+            bb.just_set(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], (T)values[i]);
+        }
+        return VX_OK;
+    });
+}
+
 int vxo_batch_fill(void *b, uint32_t value) {
     return with_batch(b, [&](auto &bb) {
         using T = std::decay_t<decltype(bb.fill_value())>;

@@ -254,3 +254,45 @@ def test_rebuild_after_release_reuses_slots(gpu_lib):
     s2 = ig.stats()
     assert s2["alive_nodes"] == s1["alive_nodes"]
     assert s2["next_index"] == s1["next_index"]
+
+
+@pytest.mark.parametrize("patches", [VX_PATCH_P1 | VX_PATCH_P2, VX_PATCH_P1 | VX_PATCH_P2 | VX_PATCH_P3 | VX_PATCH_P4])
+def test_device_group_records_match_oracle(oracle_lib, gpu_lib, patches):
+    """vx_apply_groups_async (compacted groups already in HBM) equals sequential apply_batch."""
+    import ctypes as C
+
+    import torch
+
+    depths = [7, 6, 6, 5, 5, 5]  # deepest first, as the entry point requires
+    io, ig = pair(oracle_lib, gpu_lib, 256 << 20, 16, patches)
+    to = [VoxTree(d) for d in depths]
+    tg = [VoxTree(d) for d in depths]
+    for k, d in enumerate(depths):
+        g = W.dune_chunks(1, 1, depth=d, seed=40 + k, dtype=np.uint16, **W.terrain_params(d))[0]
+        io.build_dense([to[k]], g[None])
+        ig.build_dense([tg[k]], g[None])
+    recs = []
+    for k, d in enumerate(depths):
+        xyz, vals = W.random_edits(d, (0.001, 0.01, 0.1)[k % 3], 900 + k, max_material=4095)
+        b = to[k].create_batch(io)
+        b.set_many(xyz, vals)
+        to[k].apply_batch(io, b)
+        groups, sm, cm, vv = W.edits_to_groups(d, xyz, vals)
+        recs.append((np.full(len(groups), k, np.uint32), groups, sm, cm, vv))
+    item, group, sm, cm, vv = (np.concatenate([r[j] for r in recs]) for j in range(5))
+    dev = torch.device("cuda", 0)
+
+    def t(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32 if a.dtype.itemsize == 4 else
+                                                             (np.int16 if a.dtype.itemsize == 2 else np.uint8))).to(dev)
+
+    handles = np.array([x._bind(ig) for x in tg], dtype=np.uint32)
+    args = [t(handles), t(np.full(len(tg), 2, np.uint8)), t(np.zeros(len(tg), np.uint32)), len(item),
+            t(item), t(group), t(sm), t(cm), t(vv.reshape(-1)), torch.zeros(len(tg), dtype=torch.uint8, device=dev)]
+    ptrs = [C.c_void_p(a.data_ptr()) if isinstance(a, torch.Tensor) else a for a in args]
+    torch.cuda.synchronize()
+    gpu_lib.call("apply_groups_async", ig.handle, len(tg), *ptrs, max(depths), handle=ig.handle)
+    ig.sync()
+    for x in tg:
+        x._dirty = True
+    assert_same(io, ig, to, tg)

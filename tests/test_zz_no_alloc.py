@@ -22,7 +22,13 @@ from voxelis_gb300.api import VoxInterner, VoxTree
 
 pytestmark = pytest.mark.gpu
 
-SCRATCH_ENTRIES = 1 << 18  # VX_NOALLOC_SCRATCH_ENTRIES in include/voxelis_gb300.h
+SCRATCH_BYTES = 3 << 20  # VX_NOALLOC_SCRATCH_BYTES in include/voxelis_gb300.h
+
+
+def scratch_bytes(n, depth):
+    rows = sum(n << (3 * k) for k in range(1, depth - 3))
+    counts = sum(n << (3 * k) for k in range(0, depth - 4))
+    return 12 * rows + 4 * counts + 512
 
 
 def _noalloc(lib):
@@ -86,7 +92,9 @@ def test_noalloc_refuses_requests_beyond_its_array(gpu_lib):
     tree = VoxTree(6)
     tree._bind(it)
     small = torch.zeros(64, dtype=torch.uint8, device="cuda")
-    too_many = SCRATCH_ENTRIES // 8 + 1  # depth 6 needs 8 entries per chunk
+    per_chunk = scratch_bytes(2, 6) - scratch_bytes(1, 6)
+    too_many = SCRATCH_BYTES // per_chunk + 1
+    assert scratch_bytes(too_many, 6) > SCRATCH_BYTES
     st = f(it.handle, too_many, C.c_void_p(small.data_ptr()), C.c_void_p(small.data_ptr()), None, 6)
     assert st == VX_E_BUFFER
     assert it.stats()["alive_nodes"] == 1

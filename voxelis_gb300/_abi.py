@@ -36,7 +36,7 @@ VX_PATCH_P4 = 1 << 3
 VX_MEM_HOST = 0
 VX_MEM_DEVICE = 1
 
-VX_PROF_NAMES = ["dense", "levels", "refcount", "apply", "release", "get", "copy", "unused"]
+VX_PROF_NAMES = ["dense", "levels", "refcount", "apply_levels", "release", "get", "copy", "apply_bottom"]
 VX_PROF_N = 8
 
 VX_BLOCK_EMPTY = 0
@@ -71,6 +71,11 @@ class vx_interner_stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "capacity", "node_size", "next_index", "free_count", "alive_nodes", "branch_patterns",
         "leaf_patterns", "table_slots", "table_tombstones", "error_flags")]
+
+
+class vx_world(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("chunk_depth", C.c_int32),
+                ("trees_dev", C.c_void_p)]
 
 
 class vx_canonical(C.Structure):
@@ -116,6 +121,7 @@ SIGNATURES = {
     "batch_fill": [_P, _U32],
     "batch_clear": [_P],
     "batch_set_dense": [_P, _P],
+    "batch_set_many": [_P, _U64, _P, _P],
     "batch_size": [_P, _PU64],
     "batch_has_patches": [_P, _PI],
     "apply_batch": [_P, _U32, _P, _PI],
@@ -132,11 +138,16 @@ GPU_SIGNATURES = {
     "profile_enable": [_P, _I],
     "profile_collect": [_P, C.POINTER(C.c_double), _PU64],
     "interner_reset": [_P],
+    "interner_maintain": [_P],
     "interner_set_stream": [_P, _P],
     "interner_sync": [_P],
     "trees_create": [_P, _U32, _P, _P],
     "build_dense_async": [_P, _U32, _P, _P, _P, _I],
     "get_many_async": [_P, _U64, _P, _P, _P, _P],
+    "apply_groups_async": [_P, _U32, _P, _P, _P, _U32, _P, _P, _P, _P, _P, _P, _I],
+    "tune_set": [_P, _I, _I],
+    "world_get_async": [_P, _P, _U64, _P, _P, _P],
+    "tune_get": [_P, _PI, _PI],
 }
 
 

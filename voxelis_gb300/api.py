@@ -192,6 +192,13 @@ class Batch:
         self._call("batch_set", *_pos(position), int(voxel))
         return True
 
+    def set_many(self, xyz, values):
+        """just_set for every (position, value) pair in order (last write wins per voxel)."""
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        v = np.ascontiguousarray(values, dtype=np.uint32).reshape(-1)
+        assert p.shape[0] == v.shape[0]
+        self._call("batch_set_many", C.c_uint64(p.shape[0]), _np_ptr(p), _np_ptr(v))
+
     def set(self, interner, position, voxel):
         """VoxOpsWrite for Batch (batch.rs:206-208)."""
         return self.just_set(position, voxel)

@@ -71,7 +71,7 @@ __global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
     a.it_new[i] = (f & 2) ? INVALID_ID : init;
 }
 
-__global__ void __launch_bounds__(kThreads) bottom_kernel(DevInterner I, ApplyArgs a) {
+__global__ void __launch_bounds__(512) bottom_kernel(DevInterner I, ApplyArgs a) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.n_records; base += stride) {
         const uint64_t r = base + threadIdx.x;
@@ -314,7 +314,7 @@ __global__ void starts_kernel(DevInterner I, ApplyArgs a) {
     if (j < count && a.flags[j]) a.p_start[a.pos[j]] = j;
 }
 
-__global__ void __launch_bounds__(kThreads) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+__global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
     const uint32_t n_par = (uint32_t)I.ctr->scratch[SC_PARENTS];
     const int nb = buf ^ 1;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -507,6 +507,24 @@ __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
 
 __global__ void zero_counter_kernel(DevInterner I, int slot) { I.ctr->scratch[slot] = 0; }
 
+__global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_items) return;
+    const uint32_t t = a.it_tree[i];
+    const int d = t < I.tree_cap ? I.depths[t] : TREE_UNUSED;
+    int prev = 0xFF;
+    if (i > 0) {
+        const uint32_t tp = a.it_tree[i - 1];
+        prev = tp < I.tree_cap ? I.depths[tp] : TREE_UNUSED;
+    }
+    if (d == TREE_UNUSED || d > a.max_depth || d < 2 || (i > 0 && d > prev)) {
+        set_error(I, ERR_INVALID, 46);
+        const_cast<uint8_t *>(a.it_depth)[i] = 2;
+        return;
+    }
+    const_cast<uint8_t *>(a.it_depth)[i] = (uint8_t)d;
+}
+
 }  // namespace
 
 size_t scan_tmp_words(uint32_t n) { return (size_t)(n + kScanBlock - 1) / kScanBlock + 32; }
@@ -532,16 +550,38 @@ cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uin
     return cudaGetLastError();
 }
 
-cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
+cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s) {
+    if (a.n_items == 0) return cudaSuccess;
+    count_launches(1);
+    item_depths_kernel<<<(a.n_items + kThreads - 1) / kThreads, kThreads, 0, s>>>(I, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
     const unsigned ib = (a.n_items + kThreads - 1) / kThreads;
     count_launches(1);
     prep_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
     const uint32_t R = a.n_records;
+    if (R) {
+        const int bt = a.threads > 0 ? a.threads : kThreads;
+        const unsigned cap = (unsigned)num_sms * (unsigned)(a.blocks_per_sm > 0 ? a.blocks_per_sm : 8);
+        const unsigned need = (R + bt - 1) / bt;
+        const unsigned g = need < cap ? need : cap;
+        count_launches(1);
+        bottom_kernel<<<g, bt, 0, s>>>(I, a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
+    const unsigned ib = (a.n_items + kThreads - 1) / kThreads;
+    const uint32_t R = a.n_records;
     const unsigned rb = (R + kThreads - 1) / kThreads;
     if (R) {
-        unsigned g = rb < (unsigned)num_sms * 8 ? rb : (unsigned)num_sms * 8;
-        count_launches(1);
-        bottom_kernel<<<g, kThreads, 0, s>>>(I, a);
+        const int bt = a.threads > 0 ? a.threads : kThreads;
+        const unsigned cap = (unsigned)num_sms * (unsigned)(a.blocks_per_sm > 0 ? a.blocks_per_sm : 8);
+        const unsigned need = (R + bt - 1) / bt;
+        const unsigned g = need < cap ? need : cap;
         cudaError_t e = launch_scan(a.flags, a.pos, a.scan_tmp, R, s);
         if (e != cudaSuccess) return e;
         count_launches(1);
@@ -555,7 +595,7 @@ cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, 
             count_launches(1);
             starts_kernel<<<rb, kThreads, 0, s>>>(I, a);
             count_launches(1);
-            parents_kernel<<<g, kThreads, 0, s>>>(I, a, step, buf);
+            parents_kernel<<<g, bt, 0, s>>>(I, a, step, buf);
             count_launches(1);
             next_count_kernel<<<1, 1, 0, s>>>(I);
             buf ^= 1;
@@ -566,6 +606,12 @@ cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, 
     count_launches(1);
     finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
+    cudaError_t e = launch_apply_bottom(I, a, num_sms, s);
+    if (e != cudaSuccess) return e;
+    return launch_apply_levels(I, a, num_sms, s);
 }
 
 }  // namespace vxg

@@ -22,6 +22,9 @@
 // back the references its children were pre-charged with, so after a build every node's count equals
 // the number of child slots of newly created nodes that name it, plus one per tree root. That sum is
 // computed once per epoch over the allocation log (launch_epoch_refcounts) instead of per lookup.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "vx_launch.h"
 
 namespace vxg {
@@ -300,6 +303,558 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
     }
 }
 
+// ---- 32^3 blocks: one warp per 16^3 octant, reduced in registers ------------------------------
+//
+// Lane l of warp w owns level-3 parents l and l+32 of octant w (a level-3 parent is 4^3 voxels,
+// 8 bottom groups). It reduces its 8 groups one by one in registers, then the parent; levels 2 and 1
+// of the octant are gathered with warp shuffles. Only the 8 octant roots meet in shared memory, so
+// a block costs one CTA barrier (plus the tile's own) instead of one per level. Bottom-group keys
+// (the 8 packed voxel values) are looked up first in a CTA-wide shared cache of the branches this
+// CTA already interned; only misses go to the global branch table, deduplicated within the warp.
+
+#ifndef VX_KEY_CACHE
+#define VX_KEY_CACHE 512
+#endif
+#ifndef VX_OCT_TILES
+#define VX_OCT_TILES 1
+#endif
+constexpr int kKeyCache = VX_KEY_CACHE;  // entries of the shared bottom-key cache (power of two)
+constexpr int kOctTiles = VX_OCT_TILES;  // tile buffers per warp in the octant kernel (1 or 2)
+
+struct KeyCache {
+    uint64_t *k0, *k1, *id;
+};
+
+__device__ __forceinline__ uint32_t kc_slot(uint64_t lo, uint64_t hi) {
+    return (uint32_t)(fmix64(lo ^ (hi * 0x9E3779B97F4A7C15ull)) >> 40) & (kKeyCache - 1);
+}
+
+// Branch id cached for (lo, hi), or 0. An entry is published by writing its id (>= 2) last.
+__device__ __forceinline__ uint64_t kc_lookup(const KeyCache &C, uint64_t lo, uint64_t hi) {
+    uint32_t h = kc_slot(lo, hi);
+#pragma unroll 1
+    for (int p = 0; p < 8; ++p) {
+        const uint64_t id = *(volatile uint64_t *)(C.id + h);
+        if (id == 0) return 0;
+        if (id > 1 && *(volatile uint64_t *)(C.k0 + h) == lo && *(volatile uint64_t *)(C.k1 + h) == hi) return id;
+        h = (h + 1) & (kKeyCache - 1);
+    }
+    return 0;
+}
+
+__device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64_t hi, uint64_t id) {
+    uint32_t h = kc_slot(lo, hi);
+#pragma unroll 1
+    for (int p = 0; p < 8; ++p) {
+        if (atomicCAS((unsigned long long *)(C.id + h), 0ull, 1ull) == 0ull) {
+            C.k0[h] = lo;
+            C.k1[h] = hi;
+            __threadfence_block();
+            *(volatile uint64_t *)(C.id + h) = id;
+            return;
+        }
+        h = (h + 1) & (kKeyCache - 1);
+    }
+}
+
+// 8 voxels of the bottom group whose lowest corner is (x, y, z) in a 32^3 [y][z][x] tile.
+template <class T>
+__device__ __forceinline__ void load_group32(const T *vox, uint32_t x, uint32_t y, uint32_t z, uint32_t v[8],
+                                             uint64_t &lo, uint64_t &hi) {
+    const uint32_t base = (y * 32 + z) * 32 + x;
+    const uint32_t off[4] = {base, base + 1024, base + 32, base + 1056};
+    lo = 0;
+    hi = 0;
+    if (sizeof(T) == 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = *reinterpret_cast<const uint16_t *>(vox + off[q]);
+            v[2 * q] = w & 0xFF;
+            v[2 * q + 1] = w >> 8;
+            lo |= (uint64_t)w << (16 * q);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = *reinterpret_cast<const uint32_t *>(vox + off[q]);
+            v[2 * q] = w & 0xFFFF;
+            v[2 * q + 1] = w >> 16;
+            if (q < 2)
+                lo |= (uint64_t)w << (32 * q);
+            else
+                hi |= (uint64_t)w << (32 * (q - 2));
+        }
+    }
+}
+
+// One parent from 8 children held by the calling lane: EMPTY, a collapsed leaf, or an interned
+// branch (warp-cooperative; every lane of the warp calls it).
+__device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active, const uint64_t c[8],
+                                              const uint32_t cv[8], uint64_t &out, uint32_t &out_val) {
+    uint32_t types = 0, mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        mask |= (c[k] != 0 ? 1u : 0u) << k;
+        types |= (id_is_leaf(c[k]) ? 1u : 0u) << k;
+    }
+    bool same = types == 0xFF;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
+    const bool is_branch = active && mask != 0 && !same;
+    const uint32_t lod = is_branch ? calc_average8(cv) : 0;
+    bool created;
+    const uint64_t id = warp_intern_branch(I, is_branch, c, types, mask, lod, &created);
+    if (mask == 0) {
+        out = EMPTY_ID;
+        out_val = 0;
+    } else if (same) {
+        out = c[0];
+        out_val = cv[0];
+    } else {
+        out = id;
+        out_val = lod;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void reduce_octant(const DevInterner &I, const T *vox, int w, const KeyCache &C,
+                                              uint64_t *leaf_cache, uint64_t &oct_id, uint32_t &oct_val) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t ox = (w & 1) << 4, oy = ((w >> 1) & 1) << 4, oz = (w >> 2) << 4;
+    const bool wide = sizeof(T) == 2;
+    uint64_t l3[2];
+    uint32_t l3v[2];
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        const uint32_t p = lane + 32 * pass;
+        const uint32_t px = compact3(p), py = compact3(p >> 1), pz = compact3(p >> 2);
+        uint64_t c3[8];
+        uint32_t cv3[8];
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t gx = 2 * px + (k & 1), gy = 2 * py + ((k >> 1) & 1), gz = 2 * pz + (k >> 2);
+            uint32_t v[8];
+            uint64_t lo, hi;
+            load_group32<T>(vox, ox + 2 * gx, oy + 2 * gy, oz + 2 * gz, v, lo, hi);
+            uint32_t set = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) set |= (v[j] != 0 ? 1u : 0u) << j;
+            bool uniform = set == 0xFF;
+#pragma unroll
+            for (int j = 1; j < 8; ++j) uniform = uniform && v[j] == v[0];
+            const bool is_branch = set != 0 && !uniform;
+            uint64_t id = is_branch ? kc_lookup(C, lo, hi) : 0ull;
+            const bool need = is_branch && id == 0;
+            const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+            uint32_t lod = is_branch ? calc_average8(v) : 0;
+            if (bm) {  // warp-uniform
+                unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+                if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+                grp &= bm;
+                const int leader = need ? __ffs(grp) - 1 : (int)lane;
+                const bool lead = need && leader == (int)lane;
+                uint64_t c[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+                bool created;
+                uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+                nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+                if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid);
+                if (need) id = nid;
+            }
+            if (set == 0) {
+                c3[k] = EMPTY_ID;
+                cv3[k] = 0;
+            } else if (uniform) {
+                c3[k] = leaf_of<T>(I, leaf_cache, v[0]);
+                cv3[k] = v[0];
+            } else {
+                c3[k] = id;
+                cv3[k] = lod;
+            }
+        }
+        reduce_parent(I, true, c3, cv3, l3[pass], l3v[pass]);
+    }
+    // level 2: lane q < 8 takes level-3 parents 8q .. 8q+7 (pass q >> 2)
+    uint64_t c2[8];
+    uint32_t cv2[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int src = (8 * lane + j) & 31;
+        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
+        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
+        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
+        cv2[j] = lane < 4 ? b0 : b1;
+    }
+    uint64_t l2;
+    uint32_t l2v;
+    reduce_parent(I, lane < 8, c2, cv2, l2, l2v);
+    // level 1: the octant root, from lanes 0..7
+    uint64_t c1[8];
+    uint32_t cv1[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
+        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
+    }
+    uint64_t l1;
+    uint32_t l1v;
+    reduce_parent(I, lane == 0, c1, cv1, l1, l1v);
+    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
+    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) dense32_kernel(DevInterner I, DenseArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr uint32_t V = 32768;
+    T *vox = reinterpret_cast<T *>(smem);
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + V * sizeof(T));
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache};
+    uint64_t *leaf_cache = kc + 3 * kKeyCache;
+    uint64_t *oct_id = leaf_cache + 256;
+    uint32_t *oct_val = reinterpret_cast<uint32_t *>(oct_id + 8);
+    uint64_t *bar = oct_id + 12;
+
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const uint64_t total_blocks = (uint64_t)a.n_chunks * a.blocks_per_chunk;
+    const int side = 1 << a.depth;
+    uint32_t phase = 0;
+    for (uint64_t blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
+        const uint32_t chunk = (uint32_t)(blk / a.blocks_per_chunk);
+        const uint32_t m = (uint32_t)(blk % a.blocks_per_chunk);
+        {
+            const uint32_t tree = a.trees[chunk];
+            const bool bad = tree >= I.tree_cap || I.depths[tree] != a.depth;
+            if (__syncthreads_or(bad)) {
+                if (tid == 0) set_error(I, ERR_INVALID, 23);
+                continue;
+            }
+        }
+        const T *grid = reinterpret_cast<const T *>(a.grids) + (size_t)chunk * side * side * side;
+        if (a.depth == 5) {
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(bar, V * (uint32_t)sizeof(T));
+                bulk_copy_g2s(vox, grid, V * (uint32_t)sizeof(T), bar);
+            }
+            bool ok = false;
+            for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+                if ((ok = mbar_try_wait(bar, phase))) break;
+            if (__syncthreads_or(!ok)) {  // every thread leaves together; the copy is drained first
+                if (tid == 0) set_error(I, ERR_TIMEOUT, 24);
+                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bar, phase); ++spin) {
+                }
+                return;
+            }
+            phase ^= 1u;
+        } else {
+            const uint32_t bx = compact3(m), by = compact3(m >> 1), bz = compact3(m >> 2);
+            const int vec_per_row = 32 * (int)sizeof(T) / 16;
+            for (int r = tid; r < 1024 * vec_per_row; r += blockDim.x) {
+                const int row = r / vec_per_row, v = r % vec_per_row;
+                const int y = row >> 5, z = row & 31;
+                const T *src = grid + ((size_t)(by * 32 + y) * side + (bz * 32 + z)) * side + bx * 32;
+                reinterpret_cast<uint4 *>(vox + (size_t)row * 32)[v] = __ldcs(reinterpret_cast<const uint4 *>(src) + v);
+            }
+            __syncthreads();
+        }
+
+        uint64_t oid;
+        uint32_t oval;
+        reduce_octant<T>(I, vox, (int)warp, C, leaf_cache, oid, oval);
+        if (lane == 0) {
+            oct_id[warp] = oid;
+            oct_val[warp] = oval;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint64_t c[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                c[j] = oct_id[j];
+                cv[j] = oct_val[j];
+            }
+            uint64_t root;
+            uint32_t rval;
+            reduce_parent(I, lane == 0, c, cv, root, rval);
+            if (lane == 0) {
+                if (a.depth == 5) {
+                    const uint32_t tree = a.trees[chunk];
+                    if (root != EMPTY_ID) {
+                        I.roots[tree] = root;
+                        atomicAdd(I.refcount + id_index(root), 1u);
+                    }
+                    if (a.changed) a.changed[chunk] = root != EMPTY_ID;
+                } else {
+                    a.block_roots[blk] = root;
+                    a.block_vals[blk] = rval;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- 16^3 octants, one warp each, TMA tensor copies, last-arriver reduction above ------------
+//
+// Each warp streams its own octants: lane 0 issues a 4-D tiled TMA copy (box 16 x 16 x 16 of the
+// [chunk][y][z][x] grid tensor) of the next octant into the warp's second tile while the warp reduces
+// the current one, so loads overlap work and no warp ever waits for another at a CTA barrier. An
+// octant root is stored in its level's scratch row; the warp that brings the 8th sibling of a parent
+// (an atomic arrival count per parent) reads the siblings and reduces the parent, up to the chunk
+// root. The only CTA-wide structures are the shared bottom-key cache and the 8-bit leaf cache.
+
+struct OctArgs {
+    const uint32_t *trees;
+    uint32_t n_chunks;
+    int depth;
+    uint8_t *changed;
+    uint64_t *ids;   // octant and higher level nodes: level k (1 .. depth-4) at lvl_off[k]
+    uint32_t *vals;
+    uint32_t *cnt;   // arrival counts of levels 0 .. depth-5 at cnt_off[k]
+    uint64_t lvl_off[12];
+    uint64_t cnt_off[12];
+};
+
+constexpr int kOctWarps = 8;
+
+template <class T>
+__device__ __forceinline__ void reduce_tile16(const DevInterner &I, const T *tile, const KeyCache &C,
+                                              uint64_t *leaf_cache, uint64_t &oct_id, uint32_t &oct_val) {
+    const unsigned lane = threadIdx.x & 31u;
+    const bool wide = sizeof(T) == 2;
+    uint64_t l3[2];
+    uint32_t l3v[2];
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        const uint32_t p = lane + 32 * pass;
+        const uint32_t px = compact3(p), py = compact3(p >> 1), pz = compact3(p >> 2);
+        uint64_t c3[8];
+        uint32_t cv3[8];
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t x = 4 * px + 2 * (k & 1), y = 4 * py + 2 * ((k >> 1) & 1), z = 4 * pz + 2 * (k >> 2);
+            const uint32_t base = (y * 16 + z) * 16 + x;
+            const uint32_t off[4] = {base, base + 256, base + 16, base + 272};
+            uint32_t v[8];
+            uint64_t lo = 0, hi = 0;
+            if (sizeof(T) == 1) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t w = *reinterpret_cast<const uint16_t *>(tile + off[q]);
+                    v[2 * q] = w & 0xFF;
+                    v[2 * q + 1] = w >> 8;
+                    lo |= (uint64_t)w << (16 * q);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t w = *reinterpret_cast<const uint32_t *>(tile + off[q]);
+                    v[2 * q] = w & 0xFFFF;
+                    v[2 * q + 1] = w >> 16;
+                    if (q < 2)
+                        lo |= (uint64_t)w << (32 * q);
+                    else
+                        hi |= (uint64_t)w << (32 * (q - 2));
+                }
+            }
+            uint32_t set = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) set |= (v[j] != 0 ? 1u : 0u) << j;
+            bool uniform = set == 0xFF;
+#pragma unroll
+            for (int j = 1; j < 8; ++j) uniform = uniform && v[j] == v[0];
+            const bool is_branch = set != 0 && !uniform;
+            uint64_t id = is_branch ? kc_lookup(C, lo, hi) : 0ull;
+            const bool need = is_branch && id == 0;
+            const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+            const uint32_t lod = is_branch ? calc_average8(v) : 0;
+            if (bm) {
+                unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+                if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+                grp &= bm;
+                const int leader = need ? __ffs(grp) - 1 : (int)lane;
+                const bool lead = need && leader == (int)lane;
+                uint64_t c[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+                bool created;
+                uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+                nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+                if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid);
+                if (need) id = nid;
+            }
+            if (set == 0) {
+                c3[k] = EMPTY_ID;
+                cv3[k] = 0;
+            } else if (uniform) {
+                c3[k] = leaf_of<T>(I, leaf_cache, v[0]);
+                cv3[k] = v[0];
+            } else {
+                c3[k] = id;
+                cv3[k] = lod;
+            }
+        }
+        reduce_parent(I, true, c3, cv3, l3[pass], l3v[pass]);
+    }
+    uint64_t c2[8];
+    uint32_t cv2[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int src = (8 * lane + j) & 31;
+        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
+        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
+        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
+        cv2[j] = lane < 4 ? b0 : b1;
+    }
+    uint64_t l2;
+    uint32_t l2v;
+    reduce_parent(I, lane < 8, c2, cv2, l2, l2v);
+    uint64_t c1[8];
+    uint32_t cv1[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
+        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
+    }
+    uint64_t l1;
+    uint32_t l1v;
+    reduce_parent(I, lane == 0, c1, cv1, l1, l1v);
+    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
+    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
+}
+
+__device__ __forceinline__ void tma_load_octant(void *dst, const CUtensorMap *tmap, int x, int z, int y, int c,
+                                                uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(z), "r"(y), "r"(c), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) dense_octants_kernel(DevInterner I, OctArgs a,
+                                                                 const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr uint32_t TILE = 4096 * sizeof(T);
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    T *tiles = reinterpret_cast<T *>(smem + warp * kOctTiles * TILE);
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + kOctWarps * kOctTiles * TILE);
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache};
+    uint64_t *leaf_cache = kc + 3 * kKeyCache;
+    uint64_t *bars = leaf_cache + 256 + warp * 2;
+
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    if (lane == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int d = a.depth;
+    const int ob = 3 * (d - 4);  // octant-index bits inside a chunk
+    const uint64_t n_oct = (uint64_t)a.n_chunks << ob;
+    const uint64_t total = (uint64_t)gridDim.x * kOctWarps;
+    uint64_t o = (uint64_t)blockIdx.x * kOctWarps + warp;
+    auto issue = [&](uint64_t oo, int buf) {
+        const uint32_t c = (uint32_t)(oo >> ob);
+        const uint32_t q = (uint32_t)(oo & ((1ull << ob) - 1));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bars + buf, TILE);
+        tma_load_octant(tiles + buf * 4096, &tmap, (int)(compact3(q) * 16), (int)(compact3(q >> 2) * 16),
+                        (int)(compact3(q >> 1) * 16), (int)c, bars + buf);
+    };
+    uint32_t ph0 = 0, ph1 = 0;
+    int buf = 0;
+    if (o < n_oct && lane == 0) issue(o, 0);
+    for (; o < n_oct; o += total) {
+        const uint64_t nx = o + total;
+        if (kOctTiles == 2 && nx < n_oct && lane == 0) issue(nx, buf ^ 1);
+        uint32_t &ph = buf ? ph1 : ph0;
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bars + buf, ph))) break;
+        if (__any_sync(0xFFFFFFFFu, !ok)) {  // give up: drain this warp's copies, report, leave
+            if (lane == 0) set_error(I, ERR_TIMEOUT, 25);
+            for (int b = 0; b < kOctTiles; ++b)
+                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bars + b, b ? ph1 : ph0); ++spin) {
+                }
+            return;
+        }
+        ph ^= 1u;
+        const uint32_t c = (uint32_t)(o >> ob);
+        uint64_t q = o & ((1ull << ob) - 1);
+        const uint32_t tree = a.trees[c];
+        const bool bad = tree >= I.tree_cap || I.depths[tree] != d;
+        if (bad) {
+            if (lane == 0) set_error(I, ERR_INVALID, 26);
+            if (kOctTiles == 1 && nx < n_oct && lane == 0) issue(nx, 0);
+            if (kOctTiles == 2) buf ^= 1;
+            continue;
+        }
+        uint64_t node;
+        uint32_t val;
+        reduce_tile16<T>(I, tiles + buf * 4096, C, leaf_cache, node, val);
+        __syncwarp();
+        if (kOctTiles == 1 && nx < n_oct && lane == 0) issue(nx, 0);  // single buffer: load after use
+        // climb while this warp brings the last child of a parent
+        for (int k = d - 4;; --k) {
+            if (k == 0) {
+                if (lane == 0) {
+                    if (node != EMPTY_ID) {
+                        I.roots[tree] = node;
+                        atomicAdd(I.refcount + id_index(node), 1u);
+                    }
+                    if (a.changed) a.changed[c] = node != EMPTY_ID;
+                }
+                break;
+            }
+            const uint64_t gi = a.lvl_off[k] + ((uint64_t)c << (3 * k)) + q;
+            if (lane == 0) {
+                a.ids[gi] = node;
+                a.vals[gi] = val;
+            }
+            __threadfence();
+            uint32_t arrived = 0;
+            if (lane == 0)
+                arrived = atomicAdd(a.cnt + a.cnt_off[k - 1] + ((uint64_t)c << (3 * (k - 1))) + (q >> 3), 1u);
+            arrived = __shfl_sync(0xFFFFFFFFu, arrived, 0);
+            if (arrived != 7) break;
+            __threadfence();
+            const uint64_t sb = a.lvl_off[k] + ((uint64_t)c << (3 * k)) + (q & ~7ull);
+            const uint64_t sid = lane < 8 ? ld_cg(a.ids + sb + lane) : 0ull;
+            const uint32_t sval = lane < 8 ? __ldcg(a.vals + sb + lane) : 0u;
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                ch[j] = __shfl_sync(0xFFFFFFFFu, sid, j);
+                cv[j] = __shfl_sync(0xFFFFFFFFu, sval, j);
+            }
+            reduce_parent(I, lane == 0, ch, cv, node, val);
+            node = __shfl_sync(0xFFFFFFFFu, node, 0);
+            val = __shfl_sync(0xFFFFFFFFu, val, 0);
+            q >>= 3;
+        }
+        if (kOctTiles == 2) buf ^= 1;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
@@ -412,6 +967,8 @@ __global__ void epoch_finalize_kernel(DevInterner I) {
 
 }  // namespace
 
+size_t dense32_smem_bytes(int vbytes) { return (size_t)32768 * vbytes + (3 * kKeyCache + 256 + 8) * 8 + 8 * 4 + 64; }
+
 size_t dense_smem_bytes(int bdepth, int vbytes) {
     const size_t V = (size_t)1 << (3 * bdepth);
     const size_t n_nodes = (V - 1) / 7;
@@ -419,30 +976,111 @@ size_t dense_smem_bytes(int bdepth, int vbytes) {
     return vox + n_nodes * 8 + ((n_nodes + 1) & ~(size_t)1) * 4 + 256 * 8 + 16;
 }
 
-cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s) {
-    const size_t smem = dense_smem_bytes(a.bdepth, I.vbits / 8);
+template <class K>
+static cudaError_t launch_persistent(K kernel, const DevInterner &I, const DenseArgs &a, size_t smem, int num_sms,
+                                    cudaStream_t s) {
     const uint64_t total = (uint64_t)a.n_chunks * a.blocks_per_chunk;
-    if (total == 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     int per_sm = 1;
-    cudaError_t e;
-    if (I.vbits == 8) {
-        e = cudaFuncSetAttribute(dense_blocks_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dense_blocks_kernel<uint8_t>, kThreads, smem);
-    } else {
-        e = cudaFuncSetAttribute(dense_blocks_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dense_blocks_kernel<uint16_t>, kThreads, smem);
-    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
     if (per_sm < 1) per_sm = 1;
     uint64_t grid = (uint64_t)num_sms * per_sm;
     if (grid > total) grid = total;
     count_launches(1);
-    if (I.vbits == 8)
-        dense_blocks_kernel<uint8_t><<<(unsigned)grid, kThreads, smem, s>>>(I, a);
-    else
-        dense_blocks_kernel<uint16_t><<<(unsigned)grid, kThreads, smem, s>>>(I, a);
+    kernel<<<(unsigned)grid, kThreads, smem, s>>>(I, a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s) {
+    if ((uint64_t)a.n_chunks * a.blocks_per_chunk == 0) return cudaSuccess;
+    if (a.bdepth == 5) {
+        const size_t smem = dense32_smem_bytes(I.vbits / 8);
+        if (I.vbits == 8) return launch_persistent(dense32_kernel<uint8_t>, I, a, smem, num_sms, s);
+        return launch_persistent(dense32_kernel<uint16_t>, I, a, smem, num_sms, s);
+    }
+    const size_t smem = dense_smem_bytes(a.bdepth, I.vbits / 8);
+    if (I.vbits == 8) return launch_persistent(dense_blocks_kernel<uint8_t>, I, a, smem, num_sms, s);
+    return launch_persistent(dense_blocks_kernel<uint16_t>, I, a, smem, num_sms, s);
+}
+
+size_t dense_octant_scratch_bytes(uint64_t n_chunks, int depth) {
+    size_t ids = 0, cnts = 0;
+    for (int k = 1; k <= depth - 4; ++k) ids += (size_t)n_chunks << (3 * k);
+    for (int k = 0; k <= depth - 5; ++k) cnts += (size_t)n_chunks << (3 * k);
+    return ids * 12 + cnts * 4 + 512;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
+                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s) {
+    if (n_chunks == 0) return cudaSuccess;
+    if (depth < 4 || depth > 10) return cudaErrorInvalidValue;
+    OctArgs a{};
+    a.trees = trees;
+    a.n_chunks = n_chunks;
+    a.depth = depth;
+    a.changed = changed;
+    size_t ids = 0, cnts = 0;
+    for (int k = 1; k <= depth - 4; ++k) {
+        a.lvl_off[k] = ids;
+        ids += (size_t)n_chunks << (3 * k);
+    }
+    for (int k = 0; k <= depth - 5; ++k) {
+        a.cnt_off[k] = cnts;
+        cnts += (size_t)n_chunks << (3 * k);
+    }
+    char *base = static_cast<char *>(scratch);
+    a.ids = reinterpret_cast<uint64_t *>(base);
+    a.vals = reinterpret_cast<uint32_t *>(base + ids * 8);
+    a.cnt = reinterpret_cast<uint32_t *>(base + ((ids * 12 + 255) & ~(size_t)255));
+    if (cnts) {
+        cudaError_t e = cudaMemsetAsync(a.cnt, 0, cnts * 4, s);
+        if (e != cudaSuccess) return e;
+    }
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const uint64_t side = 1ull << depth;
+    const uint32_t es = (uint32_t)(I.vbits / 8);
+    CUtensorMap tmap;
+    cuuint64_t dims[4] = {side, side, side, n_chunks};
+    cuuint64_t strides[3] = {side * es, side * side * es, side * side * side * es};
+    cuuint32_t box[4] = {16, 16, 16, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                        const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)kOctWarps * kOctTiles * 4096 * es + (3 * kKeyCache + 256 + 2 * kOctWarps) * 8 + 64;
+    const uint64_t n_oct = (uint64_t)n_chunks << (3 * (depth - 4));
+    auto launch = [&](auto kernel) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+        if (per_sm < 1) per_sm = 1;
+        uint64_t grid = (uint64_t)num_sms * per_sm;
+        const uint64_t need = (n_oct + kOctWarps - 1) / kOctWarps;
+        if (grid > need) grid = need;
+        count_launches(1);
+        kernel<<<(unsigned)grid, kThreads, smem, s>>>(I, a, tmap);
+        return cudaGetLastError();
+    };
+    if (es == 1) return launch(dense_octants_kernel<uint8_t>);
+    return launch(dense_octants_kernel<uint16_t>);
 }
 
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,

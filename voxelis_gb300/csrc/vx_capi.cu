@@ -106,6 +106,8 @@ struct vx_interner {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     int num_sms = 148;
+    int apply_threads = 256;       // launch shape of the batched-apply kernels (autotuned)
+    int apply_blocks_per_sm = 8;
     // tree table
     uint32_t tree_cap = 0;
     std::vector<uint8_t> tree_depth, tree_used, tree_maybe_nonempty;
@@ -303,6 +305,85 @@ struct Item {
     uint32_t caller_index;
 };
 
+// Device scratch of one batched apply over n items and R touched groups. With `own_inputs` the
+// item and record input arrays are carved from the workspace too (host-staging path).
+int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyArgs &a) {
+    const size_t Rp = R + 1;
+    const size_t in_items = own_inputs ? 1 : 0, in_recs = own_inputs ? 1 : 0;
+    const size_t need = Carve::need({n * 4 * in_items, n, n * in_items, n * 4 * in_items, n * 8, n * 8, n * 8, n,
+                                     n, R * 4 * in_recs, R * 4 * in_recs, R * in_recs, R * in_recs, R * 16 * in_recs,
+                                     Rp * 4, Rp * 4, scan_tmp_words((uint32_t)Rp) * 4 * 4, R * 4, R * 4, R * 4,
+                                     R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8});
+    VX_CUDA(it->ws.reserve(need));
+    Carve c(it->ws.p);
+    a.mode = 0;
+    a.n_items = n;
+    a.n_records = (uint32_t)R;
+    a.threads = it->apply_threads;
+    a.blocks_per_sm = it->apply_blocks_per_sm;
+    if (own_inputs) a.it_tree = c.take<uint32_t>(n);
+    a.it_depth = c.take<uint8_t>(n);
+    if (own_inputs) {
+        a.it_flags = c.take<uint8_t>(n);
+        a.it_fill = c.take<uint32_t>(n);
+    }
+    a.it_init = c.take<uint64_t>(n);
+    a.it_old = c.take<uint64_t>(n);
+    a.it_new = c.take<uint64_t>(n);
+    a.it_panic = c.take<uint8_t>(n);
+    a.it_changed = c.take<uint8_t>(n);
+    if (own_inputs) {
+        a.rec_item = c.take<uint32_t>(R);
+        a.rec_group = c.take<uint32_t>(R);
+        a.rec_set = c.take<uint8_t>(R);
+        a.rec_clear = c.take<uint8_t>(R);
+        a.rec_vals = c.take<uint16_t>(R * 8);
+    }
+    a.flags = c.take<uint32_t>(Rp);
+    a.pos = c.take<uint32_t>(Rp);
+    a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
+    a.e_item[0] = c.take<uint32_t>(R);
+    a.e_item[1] = c.take<uint32_t>(R);
+    a.e_path[0] = c.take<uint32_t>(R);
+    a.e_path[1] = c.take<uint32_t>(R);
+    a.e_id[0] = c.take<uint64_t>(R);
+    a.e_id[1] = c.take<uint64_t>(R);
+    a.e_val[0] = c.take<uint32_t>(R);
+    a.e_val[1] = c.take<uint32_t>(R);
+    a.p_start = c.take<uint32_t>(Rp);
+    a.rec_id = c.take<uint64_t>(R);
+    a.rec_val = c.take<uint32_t>(R);
+    a.release_list = c.take<uint64_t>(n);
+    return VX_OK;
+}
+
+// The set phase, its refcount epoch and release, then (P4) the clear pass with its own epoch and
+// release. No host synchronisation.
+int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
+    cudaStream_t s = it->stream;
+    for (int mode = 0; mode < (clear_pass ? 2 : 1); ++mode) {
+        a.mode = mode;
+        {
+            Phase ph(it, VX_PROF_BOTTOM);
+            VX_CUDA(launch_apply_bottom(it->dev, a, it->num_sms, s));
+        }
+        {
+            Phase ph(it, VX_PROF_APPLY);
+            VX_CUDA(launch_apply_levels(it->dev, a, it->num_sms, s));
+        }
+        {
+            Phase ph(it, VX_PROF_REFCOUNT);
+            VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
+        }
+        {
+            Phase ph(it, VX_PROF_RELEASE);
+            VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity, it->capacity,
+                                   11, it->num_sms, s));
+        }
+    }
+    return VX_OK;
+}
+
 int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
     const uint32_t n = (uint32_t)items.size();
     if (n == 0) return VX_OK;
@@ -348,96 +429,24 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
         }
     }
 
-    const size_t Rp = R + 1;
-    const size_t need = Carve::need({n * 4, n, n, n * 4, n * 8, n * 8, n * 8, n, n, R * 4, R * 4, R, R, R * 16,
-                                     Rp * 4, Rp * 4, scan_tmp_words((uint32_t)Rp) * 4 * 4, R * 4, R * 4, R * 4,
-                                     R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8});
-    VX_CUDA(it->ws.reserve(need));
-    Carve c(it->ws.p);
     ApplyArgs a{};
-    a.mode = 0;
-    a.n_items = n;
-    a.n_records = (uint32_t)R;
+    int st0 = carve_apply(it, n, R, true, a);
+    if (st0 != VX_OK) return st0;
     a.max_depth = max_depth;
-    uint32_t *d_tree = c.take<uint32_t>(n);
-    uint8_t *d_depth = c.take<uint8_t>(n);
-    uint8_t *d_flags = c.take<uint8_t>(n);
-    uint32_t *d_fill = c.take<uint32_t>(n);
-    a.it_tree = d_tree;
-    a.it_depth = d_depth;
-    a.it_flags = d_flags;
-    a.it_fill = d_fill;
-    a.it_init = c.take<uint64_t>(n);
-    a.it_old = c.take<uint64_t>(n);
-    a.it_new = c.take<uint64_t>(n);
-    a.it_panic = c.take<uint8_t>(n);
-    a.it_changed = c.take<uint8_t>(n);
-    uint32_t *d_ritem = c.take<uint32_t>(R), *d_rgroup = c.take<uint32_t>(R);
-    uint8_t *d_rset = c.take<uint8_t>(R), *d_rclear = c.take<uint8_t>(R);
-    uint16_t *d_rvals = c.take<uint16_t>(R * 8);
-    a.rec_item = d_ritem;
-    a.rec_group = d_rgroup;
-    a.rec_set = d_rset;
-    a.rec_clear = d_rclear;
-    a.rec_vals = d_rvals;
-    a.flags = c.take<uint32_t>(Rp);
-    a.pos = c.take<uint32_t>(Rp);
-    a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
-    a.e_item[0] = c.take<uint32_t>(R);
-    a.e_item[1] = c.take<uint32_t>(R);
-    a.e_path[0] = c.take<uint32_t>(R);
-    a.e_path[1] = c.take<uint32_t>(R);
-    a.e_id[0] = c.take<uint64_t>(R);
-    a.e_id[1] = c.take<uint64_t>(R);
-    a.e_val[0] = c.take<uint32_t>(R);
-    a.e_val[1] = c.take<uint32_t>(R);
-    a.p_start = c.take<uint32_t>(Rp);
-    a.rec_id = c.take<uint64_t>(R);
-    a.rec_val = c.take<uint32_t>(R);
-    a.release_list = c.take<uint64_t>(n);
-
     cudaStream_t s = it->stream;
-    VX_CUDA(cudaMemcpyAsync(d_tree, it_tree.data(), n * 4, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync(d_depth, it_depth.data(), n, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync(d_flags, it_flags.data(), n, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync(d_fill, it_fill.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_tree, it_tree.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_depth, it_depth.data(), n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_flags, it_flags.data(), n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_fill, it_fill.data(), n * 4, cudaMemcpyHostToDevice, s));
     if (R) {
-        VX_CUDA(cudaMemcpyAsync(d_ritem, rec_item.data(), R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync(d_rgroup, rec_group.data(), R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync(d_rset, rec_set.data(), R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync(d_rclear, rec_clear.data(), R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync(d_rvals, rec_vals.data(), R * 16, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_item, rec_item.data(), R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_group, rec_group.data(), R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_set, rec_set.data(), R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear.data(), R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals.data(), R * 16, cudaMemcpyHostToDevice, s));
     }
-    {
-        Phase ph(it, VX_PROF_APPLY);
-        VX_CUDA(launch_apply(it->dev, a, it->num_sms, s));
-    }
-    {
-        Phase ph(it, VX_PROF_REFCOUNT);
-        VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
-    }
-    {
-        Phase ph(it, VX_PROF_RELEASE);
-        VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity, it->capacity, 11,
-                               it->num_sms, s));
-    }
-    if (any_clear && (it->flags & VX_PATCH_P4)) {
-        // P4: every cleared voxel removed after the set phase, as VoxTree::set(pos, 0) would
-        a.mode = 1;
-        {
-            Phase ph(it, VX_PROF_APPLY);
-            VX_CUDA(launch_apply(it->dev, a, it->num_sms, s));
-        }
-        {
-            Phase ph(it, VX_PROF_REFCOUNT);
-            VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
-        }
-        {
-            Phase ph(it, VX_PROF_RELEASE);
-            VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity,
-                                   it->capacity, 11, it->num_sms, s));
-        }
-    }
+    int st1 = apply_sequence(it, a, any_clear && (it->flags & VX_PATCH_P4));
+    if (st1 != VX_OK) return st1;
     std::vector<uint8_t> ch(n);
     VX_CUDA(cudaMemcpyAsync(ch.data(), a.it_changed, n, cudaMemcpyDeviceToHost, s));
     int st = sync_and_check(it);
@@ -480,19 +489,27 @@ void batch_from_dense(vx_batch *b, const void *grid) {
 }
 
 // Fused dense construction on EMPTY trees (vx_build.cu). All arguments in device memory.
+#ifndef VX_DENSE_OCTANTS
+#define VX_DENSE_OCTANTS 1
+#endif
+
 int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void *d_grids, uint8_t *d_changed,
                int depth) {
-    DenseArgs a{};
-    a.grids = d_grids;
-    a.trees = d_trees;
-    a.n_chunks = n;
-    a.depth = depth;
-    a.bdepth = std::min(depth, 5);
-    a.blocks_per_chunk = 1u << (3 * (depth - a.bdepth));
-    a.changed = d_changed;
     cudaStream_t s = it->stream;
-    if (depth > 5) {
-        // level buffers: blocks, then each level above
+    if (VX_DENSE_OCTANTS && depth >= 4) {
+        VX_CUDA(it->ws.reserve(dense_octant_scratch_bytes(n, depth)));
+        Phase ph(it, VX_PROF_DENSE);
+        VX_CUDA(launch_dense_octants(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s));
+    } else if (depth > 5) {
+        // 32^3 blocks, then one launch per level above them
+        DenseArgs a{};
+        a.grids = d_grids;
+        a.trees = d_trees;
+        a.n_chunks = n;
+        a.depth = depth;
+        a.bdepth = 5;
+        a.blocks_per_chunk = 1u << (3 * (depth - 5));
+        a.changed = d_changed;
         size_t total = 0;
         for (int k = depth - 5; k >= 1; --k) total += (size_t)n << (3 * k);
         VX_CUDA(it->ws.reserve(Carve::need({total * 8, total * 4}) + 1024));
@@ -519,6 +536,14 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
             off += np;
         }
     } else {
+        DenseArgs a{};
+        a.grids = d_grids;
+        a.trees = d_trees;
+        a.n_chunks = n;
+        a.depth = depth;
+        a.bdepth = depth;
+        a.blocks_per_chunk = 1;
+        a.changed = d_changed;
         Phase ph(it, VX_PROF_DENSE);
         VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
     }
@@ -726,6 +751,13 @@ int vx_interner_set_stream(vx_interner *it, void *cuda_stream) {
 int vx_interner_sync(vx_interner *it) {
     if (!it) return VX_E_INVALID_ARG;
     return sync_and_check(it);
+}
+
+int vx_interner_maintain(vx_interner *it) {
+    if (!it) return VX_E_INVALID_ARG;
+    int st = sync_and_check(it);
+    if (st == VX_OK) maybe_rehash(it);
+    return st;
 }
 
 int vx_interner_stats_get(vx_interner *it, vx_interner_stats *out) {
@@ -943,6 +975,15 @@ int vx_batch_set(vx_batch *b, int32_t x, int32_t y, int32_t z, uint32_t value) {
     return VX_OK;
 }
 
+int vx_batch_set_many(vx_batch *b, uint64_t n, const int32_t *xyz, const uint32_t *values) {
+    if (!b || (n && (!xyz || !values))) return VX_E_INVALID_ARG;
+    for (uint64_t i = 0; i < n; ++i) {
+        const int st = vx_batch_set(b, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], values[i]);
+        if (st != VX_OK) return st;
+    }
+    return VX_OK;
+}
+
 int vx_batch_clear(vx_batch *b) {
     if (!b) return VX_E_INVALID_ARG;
     std::fill(b->set.begin(), b->set.end(), 0);
@@ -1004,6 +1045,51 @@ int vx_apply_batch(vx_interner *it, vx_tree tree, const vx_batch *batch, int *ch
     int st = vx_apply_batches(it, 1, &tree, &batch, &c);
     if (changed) *changed = c;
     return st;
+}
+
+int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *trees_dev, const uint8_t *item_flags_dev,
+                          const uint32_t *fill_dev, uint32_t n_records, const uint32_t *rec_item_dev,
+                          const uint32_t *rec_group_dev, const uint8_t *rec_set_dev, const uint8_t *rec_clear_dev,
+                          const uint16_t *rec_values_dev, uint8_t *changed_dev, int max_depth) {
+    if (!it || (n_items && (!trees_dev || !item_flags_dev || !fill_dev)) ||
+        (n_records && (!rec_item_dev || !rec_group_dev || !rec_set_dev || !rec_clear_dev || !rec_values_dev)))
+        return VX_E_INVALID_ARG;
+    if (max_depth < 2 || max_depth >= depth_limit(it->flags)) return set_err(it, VX_E_DEPTH, "unsupported max_depth");
+    it->all_trees_unknown = true;
+    if (n_items == 0) return VX_OK;
+    ApplyArgs a{};
+    int st = carve_apply(it, n_items, n_records, false, a);
+    if (st != VX_OK) return st;
+    a.it_tree = trees_dev;
+    a.it_flags = item_flags_dev;
+    a.it_fill = fill_dev;
+    a.rec_item = rec_item_dev;
+    a.rec_group = rec_group_dev;
+    a.rec_set = rec_set_dev;
+    a.rec_clear = rec_clear_dev;
+    a.rec_vals = rec_values_dev;
+    a.max_depth = max_depth;
+    VX_CUDA(launch_item_depths(it->dev, a, it->stream));
+    st = apply_sequence(it, a, (it->flags & VX_PATCH_P4) != 0);
+    if (st != VX_OK) return st;
+    if (changed_dev) VX_CUDA(cudaMemcpyAsync(changed_dev, a.it_changed, n_items, cudaMemcpyDeviceToDevice, it->stream));
+    return VX_OK;
+}
+
+int vx_tune_set(vx_interner *it, int apply_threads, int apply_blocks_per_sm) {
+    if (!it || apply_threads < 32 || apply_threads > 512 || apply_threads % 32 || apply_blocks_per_sm < 1 ||
+        apply_blocks_per_sm > 64)
+        return VX_E_INVALID_ARG;
+    it->apply_threads = apply_threads;
+    it->apply_blocks_per_sm = apply_blocks_per_sm;
+    return VX_OK;
+}
+
+int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm) {
+    if (!it || !apply_threads || !apply_blocks_per_sm) return VX_E_INVALID_ARG;
+    *apply_threads = it->apply_threads;
+    *apply_blocks_per_sm = it->apply_blocks_per_sm;
+    return VX_OK;
 }
 
 int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev, const void *grids_dev,
@@ -1155,7 +1241,7 @@ int vx_export_canonical(vx_interner *it, uint32_t n_trees, const vx_tree *trees,
     std::vector<uint64_t> roots;
     st = read_roots(it, n_trees, trees, roots);
     if (st != VX_OK) return st;
-    std::unordered_map<uint32_t, int32_t> ids;
+    std::vector<int32_t> ids(s.n, -1);  // node index -> canonical id
     std::vector<uint64_t> order, stack;
     std::vector<int32_t> croots(n_trees, -1);
     for (uint32_t t = 0; t < n_trees; ++t) {
@@ -1167,7 +1253,7 @@ int vx_export_canonical(vx_interner *it, uint32_t n_trees, const vx_tree *trees,
             stack.pop_back();
             const uint32_t idx = id_index(nd);
             if (idx >= s.n) return set_err(it, VX_E_REF_UB, "child index outside the node store");
-            if (ids.count(idx)) continue;
+            if (ids[idx] >= 0) continue;
             ids[idx] = (int32_t)order.size();
             order.push_back(nd);
             if (id_is_branch(nd))

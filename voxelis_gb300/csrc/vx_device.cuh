@@ -106,6 +106,12 @@ __host__ __device__ __forceinline__ uint32_t path_mask(int d, int k) {
 
 // ---- memory helpers --------------------------------------------------------------------------
 __device__ __forceinline__ uint64_t ld_volatile(const uint64_t *p) { return *(const volatile uint64_t *)p; }
+// Acquire load of a table slot: the node record published before the slot is visible after it.
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
 
 __device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
@@ -220,7 +226,10 @@ __device__ __forceinline__ bool key_equal(const DevInterner &I, uint32_t idx, co
 // warp-aggregated ticket range, write their node and publish it. A lane that meets a slot still being
 // written retries it next round, so no lane ever waits inside a divergent branch.
 // Returns the BlockId, or INVALID_ID on error; *created tells whether this lane inserted the node.
-__device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, bool active, const uint64_t c[8],
+#ifndef VX_INTERN_INLINE
+#define VX_INTERN_INLINE __noinline__
+#endif
+static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner &I, bool active, const uint64_t c[8],
                                                        uint32_t types, uint32_t mask, uint32_t lod, bool *created,
                                                        uint64_t h_in = 0) {
     const unsigned lane = threadIdx.x & 31u;
@@ -239,8 +248,9 @@ __device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, boo
     }
     for (uint32_t round = 0;; ++round) {
         bool claimed = false;
+        bool waiting = false;
         if (!done) {
-            uint64_t s = ld_volatile(I.table + pos);
+            uint64_t s = ld_acquire(I.table + pos);
             if (s == SLOT_EMPTY) {
                 uint64_t prev = atomicCAS((unsigned long long *)(I.table + pos), SLOT_EMPTY, make_slot(tag, IDX_BUSY));
                 if (prev == SLOT_EMPTY)
@@ -251,8 +261,9 @@ __device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, boo
             if (!claimed) {
                 if ((uint32_t)(s >> 32) == tag && s != SLOT_TOMB) {
                     uint32_t idx = (uint32_t)s;
-                    if (idx != IDX_BUSY) {
-                        __threadfence();
+                    if (idx == IDX_BUSY) {
+                        waiting = true;  // retry the same slot next round
+                    } else {
                         if (key_equal(I, idx, c, types, mask)) {
                             result = ld_cg(I.ids + idx);
                             done = true;
@@ -260,7 +271,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, boo
                             pos = (pos + 1) & I.table_mask;
                             ++probes;
                         }
-                    }  // else: retry the same slot next round
+                    }
                 } else {
                     pos = (pos + 1) & I.table_mask;
                     ++probes;
@@ -300,7 +311,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch(const DevInterner &I, boo
             }
             break;
         }
-        if (!done && !claimed) __nanosleep(0);
+        if (waiting) __nanosleep(32);
     }
     return result;
 }

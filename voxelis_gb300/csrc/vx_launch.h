@@ -25,6 +25,13 @@ struct DenseArgs {
 };
 // Builds the level-(d - bdepth) subtrees of every chunk (or the whole tree when d <= 5).
 cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s);
+
+// Fused dense construction for chunk depths 4..10: warps take 16^3 octants (TMA tensor copies),
+// levels above octants are reduced by the last-arriving warp of each parent. `scratch` must hold
+// dense_octant_scratch_bytes(n, depth) bytes; it is cleared inside.
+size_t dense_octant_scratch_bytes(uint64_t n_chunks, int depth);
+cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
+                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s);
 // One level of fresh parents above the blocks: n_parents = n_chunks * 8^k.
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
                                uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
@@ -36,6 +43,8 @@ cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
 // ---- general batch apply (vx_apply.cu) ---------------------------------------------------------
 struct ApplyArgs {
     int mode;                    // 0: set phase (set_batch_at_depth_iterative); 1: clear pass (P4)
+    int threads;                 // launch shape of the bottom/parents kernels
+    int blocks_per_sm;
     uint32_t n_items;
     uint32_t n_records;
     int max_depth;
@@ -69,6 +78,11 @@ struct ApplyArgs {
     uint64_t *release_list;      // [n_items]
 };
 cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
+// The same sequence in two parts: items + bottom groups, then the level passes and the commit.
+cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
+cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
+// Fills it_depth from the tree table and checks the deepest-first order (device-resident inputs).
+cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s);
 // Counter slots used by launch_apply (DevCounters::scratch indices).
 enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5 };
 

@@ -7,13 +7,14 @@
 // grow a device workspace on demand; this one stages the levels above the 32^3 blocks in a fixed
 // array compiled into the library.
 //
-// Limits and sharing: the array holds VX_NOALLOC_SCRATCH_ENTRIES block-level entries (3 MiB of
-// device memory that every GPU loading the library keeps until the process exits). A call needs
-// n * (8^(d-5) + 8^(d-6) + ... + 8) entries for chunks of depth d > 5 (none for d <= 5); larger
-// requests are rejected with VX_E_BUFFER before any work is queued. All calls share the one array:
-// two calls whose device work overlaps (different streams or interners at the same time) race on
-// it, so serialise them. The part of the array a call uses is cleared (cudaMemsetAsync) before its
-// kernels run.
+// Limits and sharing: the array holds VX_NOALLOC_SCRATCH_BYTES (3 MiB of device memory that every
+// GPU loading the library keeps until the process exits). For chunks of depth d >= 5 a call needs
+// 12 * n * (8 + 8^2 + ... + 8^(d-4)) + 4 * n * (1 + 8 + ... + 8^(d-5)) bytes (node rows above the
+// 16^3 octants plus their arrival counts; nothing below depth 5); larger requests are rejected with
+// VX_E_BUFFER before any work is queued. All calls share the one array: two calls whose device work
+// overlaps (different streams or interners at the same time) race on it, so serialise them. The
+// arrival counts a call uses are cleared (cudaMemsetAsync) before its kernel runs; every node row is
+// written before it is read.
 //
 // Set-up: the array's device address is resolved with cudaGetSymbolAddress once per device, on the
 // first call made with that device current; make that first call before any stream capture.
@@ -33,9 +34,9 @@ using namespace vxg;
 
 namespace {
 
-constexpr uint64_t kEntries = VX_NOALLOC_SCRATCH_ENTRIES;
-// block-root ids (8 B) then their LOD values (4 B) for every staged level
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kEntries * 12];
+constexpr uint64_t kBytes = VX_NOALLOC_SCRATCH_BYTES;
+// node rows (ids, LOD values) of the levels above 16^3 octants, then their arrival counts
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
@@ -81,9 +82,8 @@ extern "C" int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree
         interner_set_error(it, "grids must be 16-byte aligned");
         return VX_E_INVALID_ARG;
     }
-    uint64_t need = 0;
-    for (int k = max_depth - 5; k >= 1; --k) need += (uint64_t)n << (3 * k);
-    if (need > kEntries) {
+    const uint64_t need = max_depth >= 5 ? dense_octant_scratch_bytes(n, max_depth) : 0;
+    if (need > kBytes) {
         interner_set_error(it, "request exceeds the fixed scratch of vx_build_dense_noalloc");
         return VX_E_BUFFER;
     }
@@ -95,38 +95,18 @@ extern "C" int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree
     }
     interner_parts(it, &D, &s, &num_sms, &flags, true);
     if (n == 0) return VX_OK;
-
-    DenseArgs a{};
-    a.grids = grids_dev;
-    a.trees = trees_dev;
-    a.n_chunks = n;
-    a.depth = max_depth;
-    a.bdepth = max_depth < 5 ? max_depth : 5;
-    a.blocks_per_chunk = 1u << (3 * (max_depth - a.bdepth));
-    a.changed = changed_dev;
-    uint64_t *ids = reinterpret_cast<uint64_t *>(scratch);
-    uint32_t *vals = reinterpret_cast<uint32_t *>(scratch + kEntries * 8);
-    if (need) {
-        if ((e = cudaMemsetAsync(ids, 0, need * 8, s)) != cudaSuccess ||
-            (e = cudaMemsetAsync(vals, 0, need * 4, s)) != cudaSuccess) {
-            interner_set_error(it, cudaGetErrorString(e));
-            return VX_E_CUDA;
-        }
-    }
-    a.block_roots = ids;
-    a.block_vals = vals;
-    e = launch_dense_blocks(D, a, num_sms, s);
-    uint64_t *in_ids = ids;
-    uint32_t *in_vals = vals;
-    uint64_t off = (uint64_t)n << (3 * (max_depth - a.bdepth));
-    for (int k = max_depth - 6; k >= 0 && e == cudaSuccess; --k) {
-        const uint64_t np = (uint64_t)n << (3 * k);
-        uint64_t *out_ids = k > 0 ? ids + off : nullptr;
-        uint32_t *out_vals = k > 0 ? vals + off : nullptr;
-        e = launch_fresh_level(D, in_ids, in_vals, out_ids, out_vals, np, k == 0, trees_dev, changed_dev, s);
-        in_ids = out_ids;
-        in_vals = out_vals;
-        off += np;
+    if (max_depth >= 4) {
+        e = launch_dense_octants(D, grids_dev, trees_dev, n, max_depth, changed_dev, scratch, num_sms, s);
+    } else {
+        DenseArgs a{};
+        a.grids = grids_dev;
+        a.trees = trees_dev;
+        a.n_chunks = n;
+        a.depth = max_depth;
+        a.bdepth = max_depth;
+        a.blocks_per_chunk = 1;
+        a.changed = changed_dev;
+        e = launch_dense_blocks(D, a, num_sms, s);
     }
     if (e == cudaSuccess) e = launch_epoch_refcounts(D, num_sms, s);
     if (e != cudaSuccess) {

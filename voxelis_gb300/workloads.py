@@ -174,3 +174,38 @@ def random_edits(depth, density, seed, max_material=4095, clear_fraction=0.15):
     vals = rng.integers(1, max_material + 1, size=n, dtype=np.int64)
     vals[rng.random(n) < clear_fraction] = 0
     return xyz, vals
+
+
+def edits_to_groups(depth, xyz, vals):
+    """The Batch a sequence of just_set calls leaves behind (core/batch.rs:145-172), compacted:
+    sorted touched bottom groups with their (set, clear) masks and 8 values. The last write to a
+    voxel wins; a zero value records a clear (its value stays 0)."""
+    from .morton import encode_child_index_path
+
+    xyz = np.asarray(xyz, dtype=np.int64).reshape(-1, 3)
+    vals = np.asarray(vals, dtype=np.int64).reshape(-1)
+    path = encode_child_index_path(xyz[:, 0], xyz[:, 1], xyz[:, 2]).astype(np.int64)
+    order = np.argsort(path, kind="stable")
+    sp = path[order]
+    last = np.ones(len(sp), dtype=bool)
+    last[:-1] = sp[1:] != sp[:-1]
+    sel = order[last]
+    p = path[sel]
+    v = vals[sel]
+    g = p >> 3
+    slot = p & 7
+    groups, inv = np.unique(g, return_inverse=True)
+    set_mask = np.zeros(len(groups), dtype=np.uint8)
+    clear_mask = np.zeros(len(groups), dtype=np.uint8)
+    np.bitwise_or.at(set_mask, inv, ((v != 0).astype(np.uint8) << slot.astype(np.uint8)))
+    np.bitwise_or.at(clear_mask, inv, ((v == 0).astype(np.uint8) << slot.astype(np.uint8)))
+    values = np.zeros((len(groups), 8), dtype=np.uint16)
+    values[inv, slot] = v
+    return groups.astype(np.uint32), set_mask, clear_mask, values
+
+
+def terrain_params(depth):
+    """Dune terrain scaled to chunks of side 2^depth (base 3s/8, amplitude 5s/16, scale 1.5s;
+    s = 32 gives the 32^3 workload's 12, 10 and 48)."""
+    s = 1 << depth
+    return dict(base=3 * s // 8, amp=5 * s // 16, scale=1.5 * s)
