@@ -62,6 +62,10 @@ extern "C" {
 /* P4: batch clear bits are honoured, as VoxTree::set(pos, 0) applied to every cleared voxel
  *     after the set phase (voxtree.rs:563-705); without it they are ignored (voxtree.rs:779).  */
 #define VX_PATCH_P4 (1u << 3)
+/* P5: apply_batch's assert_ne!(new_root, old_root) (voxtree.rs:311) is skipped: a batch that
+ *     rebuilds the identical root releases the old root as usual, which leaves every count as it
+ *     was (the reference panics instead, e.g. when a batch re-sets full uniform groups).         */
+#define VX_PATCH_P5 (1u << 4)
 
 /* ---- memory locations --------------------------------------------------------------------- */
 typedef enum { VX_MEM_HOST = 0, VX_MEM_DEVICE = 1 } vx_mem;
@@ -180,6 +184,14 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
  * the call can be captured in a CUDA graph. */
 int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
                          const void *grids_dev, uint8_t *changed_dev, int max_depth);
+/* Batched to_vec (utils/common.rs:158-246): out receives n dense [y][z][x] grids of side 2^d, one
+ * per tree, back to back; every tree must have the same depth d. With VX_MEM_DEVICE `out` is device
+ * memory (16-byte aligned); with VX_MEM_HOST the grids are produced in pieces of whole 32-row slabs
+ * and copied out. HBM-write-bound: one CTA per 32^3 cube expands the cube's subtree in shared memory. */
+int vx_trees_to_dense(vx_interner *it, uint32_t n, const vx_tree *trees, void *out, vx_mem mem);
+/* Asynchronous form, all arguments in device memory, trees checked on the device (a tree whose
+ * depth is not `depth` reports VX_E_INVALID_ARG at the next sync and leaves its grid zero). */
+int vx_trees_to_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev, int depth, void *out_dev);
 /* Batched VoxOpsRead::get: query i reads tree trees[i] at xyz[3i..3i+2]. found[i] = 0/1,
  * values[i] has the interner's voxel width (uint8_t or uint16_t elements). Out-of-bounds
  * positions report VX_E_OOB (and found = 0). */
@@ -229,7 +241,8 @@ int vx_world_get_async(vx_interner *it, const vx_world *world, uint64_t n, const
  * *n_nodes holds the required capacity. */
 int vx_export_canonical(vx_interner *it, uint32_t n_trees, const vx_tree *trees,
                         vx_canonical *out, uint64_t *n_nodes);
-/* to_vec (utils/common.rs:158-246): dense [y][z][x] grid of the tree, voxel-width elements. */
+/* to_vec (utils/common.rs:158-246): dense [y][z][x] grid of the tree, voxel-width elements
+ * (computed on the device, copied to out_grid in host memory). */
 int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid);
 /* Checks every child reachable from the given trees: generation matches its slot and the
  * refcount is positive. VX_E_REF_UB when a dangling child is found. */

@@ -43,7 +43,7 @@ struct RefOOB : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
-enum : uint32_t { P1 = 1u << 0, P2 = 1u << 1, P3 = 1u << 2, P4 = 1u << 3 };
+enum : uint32_t { P1 = 1u << 0, P2 = 1u << 1, P3 = 1u << 2, P4 = 1u << 3, P5 = 1u << 4 };
 
 using Children = std::array<uint64_t, 8>;
 
@@ -687,7 +687,7 @@ class Tree {
         bool changed = false;
         if (new_root != bid::INVALID) {
             if (!bid::is_empty(root_)) {
-                if (new_root == root_) throw RefPanic("assert_ne!(new_root_id, self.root_id)");
+                if (new_root == root_ && !(it.flags() & P5)) throw RefPanic("assert_ne!(new_root_id, self.root_id)");
                 it.dec_ref_recursive(root_);
             }
             if (!it.is_valid_block_id(new_root)) throw RefPanic("Invalid new root id");

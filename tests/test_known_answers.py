@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from voxelis_gb300 import block_id as B
-from voxelis_gb300._abi import VX_PATCH_P1, VX_PATCH_P4, ReferencePanic
+from voxelis_gb300._abi import VX_PATCH_P1, VX_PATCH_P4, VX_PATCH_P5, ReferencePanic
 from voxelis_gb300.api import VoxInterner, VoxTree
 
 D = 5
@@ -93,6 +93,19 @@ def test_reapplying_a_uniform_batch_panics(lib):
     interner, tree, _ = build(lib, UNIFORM)
     with pytest.raises(ReferencePanic):
         build(lib, UNIFORM, tree=tree, interner=interner)
+
+
+def test_reapplying_a_uniform_batch_p5(lib):
+    """P5 skips the assert_ne!: the root is released and re-installed, so the DAG and every
+    refcount are what they were before the second batch."""
+    interner, tree, _ = build(lib, UNIFORM, patches=VX_PATCH_P5)
+    root, rc, alive = tree.get_root_id(), interner.get_ref(tree.get_root_id()), interner.stats()["alive_nodes"]
+    _, _, changed = build(lib, UNIFORM, tree=tree, interner=interner)
+    assert changed
+    assert tree.get_root_id() == root and interner.get_ref(root) == rc
+    assert interner.stats()["alive_nodes"] == alive
+    assert np.array_equal(tree.to_vec(interner), UNIFORM)
+    interner.validate([tree])
 
 
 def _collapsed_group_then_partial(lib, patches):

@@ -32,6 +32,7 @@ VX_PATCH_P1 = 1 << 0
 VX_PATCH_P2 = 1 << 1
 VX_PATCH_P3 = 1 << 2
 VX_PATCH_P4 = 1 << 3
+VX_PATCH_P5 = 1 << 4
 
 VX_MEM_HOST = 0
 VX_MEM_DEVICE = 1
@@ -148,6 +149,8 @@ GPU_SIGNATURES = {
     "tune_set": [_P, _I, _I],
     "world_get_async": [_P, _P, _U64, _P, _P, _P],
     "tune_get": [_P, _PI, _PI],
+    "trees_to_dense": [_P, _U32, _P, _P, _I],
+    "trees_to_dense_async": [_P, _U32, _P, _I, _P],
 }
 
 

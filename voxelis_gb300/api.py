@@ -118,6 +118,19 @@ class VoxInterner:
                    VX_MEM_HOST)
         return found.astype(bool), vals
 
+    def to_vec_many(self, trees):
+        """Batched to_vec over trees of one depth: an (n, S, S, S) [y][z][x] array. Uses the GPU
+        library's vx_trees_to_dense; on the oracle it is to_vec per tree."""
+        if not trees:
+            return np.zeros((0, 0, 0, 0), dtype=self.dtype)
+        if not self.lib.has("trees_to_dense"):
+            return np.stack([t.to_vec(self) for t in trees])
+        n = 1 << trees[0].max_depth_value
+        handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)
+        out = np.zeros((len(trees), n, n, n), dtype=self.dtype)
+        self._call("trees_to_dense", len(trees), _np_ptr(handles), _np_ptr(out), VX_MEM_HOST)
+        return out
+
     def apply_batches(self, trees, batches):
         """n apply_batch calls in one batched device pass; returns the changed flags."""
         n = len(trees)

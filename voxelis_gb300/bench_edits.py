@@ -119,15 +119,19 @@ def run(args):
     call("profile_collect", prof_ms, prof_n)
     ms = []
     launches0 = lib.kernel_launches()
+    phases = {}
     for _ in range(args.steps):
+        call("profile_enable", 0)
         rebuild()
-        call("profile_collect", prof_ms, prof_n)
+        call("profile_enable", 1)
         ms.append(timed(apply_all))
         call("interner_sync")
+        call("profile_collect", prof_ms, prof_n)
+        for k in range(VX_PROF_N):
+            if prof_n[k]:
+                phases[VX_PROF_NAMES[k]] = phases.get(VX_PROF_NAMES[k], 0.0) + prof_ms[k]
     launches = (lib.kernel_launches() - launches0) / args.steps - 3 * 2  # minus the rebuild launches
-    call("profile_collect", prof_ms, prof_n)
     call("profile_enable", 0)
-    phases = {VX_PROF_NAMES[k]: prof_ms[k] for k in range(VX_PROF_N) if prof_n[k]}
     apply_ms = statistics.median(ms)
     from ._abi import vx_interner_stats
 

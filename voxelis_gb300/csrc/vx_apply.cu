@@ -255,6 +255,67 @@ __global__ void __launch_bounds__(kThreads) scan_blocks_kernel(const uint32_t *i
     if (threadIdx.x == kThreads - 1) sums[blockIdx.x] = warp_tot[kThreads / 32 - 1];
 }
 
+// Variants reading the element count from device memory (entries of a level pass); blocks past the
+// count only record an empty block sum.
+__global__ void __launch_bounds__(kThreads) scan_blocks_dev_kernel(const uint32_t *in, uint32_t *out, uint32_t *sums,
+                                                                  const unsigned long long *n_dev) {
+    const uint32_t n = (uint32_t)*n_dev;
+    if (blockIdx.x * kScanBlock >= n) {
+        if (threadIdx.x == 0) sums[blockIdx.x] = 0;
+        return;
+    }
+    __shared__ uint32_t warp_tot[kThreads / 32];
+    const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanPer;
+    uint32_t x[kScanPer];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        x[k] = (base + k < n) ? in[base + k] : 0u;
+        local += x[k];
+    }
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (unsigned)o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kThreads / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (unsigned)o) w += y;
+        }
+        if (lane < kThreads / 32) warp_tot[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = incl - local + (warp ? warp_tot[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += x[k];
+    }
+    if (threadIdx.x == kThreads - 1) sums[blockIdx.x] = warp_tot[kThreads / 32 - 1];
+}
+
+__global__ void scan_add_dev_kernel(uint32_t *out, const uint32_t *sums, const unsigned long long *n_dev) {
+    const uint32_t n = (uint32_t)*n_dev;
+    const uint32_t b = blockIdx.x;
+    if (b == 0 || b * kScanBlock >= n) return;
+    const uint32_t add = sums[b];
+    const uint32_t base = b * kScanBlock;
+    for (uint32_t k = threadIdx.x; k < kScanBlock; k += blockDim.x)
+        if (base + k < n) out[base + k] += add;
+}
+
+__global__ void scan_total_dev_kernel(const uint32_t *in, uint32_t *out, const unsigned long long *n_dev) {
+    const uint32_t n = (uint32_t)*n_dev;
+    out[n] = n ? out[n - 1] + in[n - 1] : 0u;
+}
+
 __global__ void scan_add_kernel(uint32_t *out, const uint32_t *sums, uint32_t n) {
     const uint32_t b = blockIdx.x;
     if (b == 0) return;
@@ -284,34 +345,31 @@ __device__ __forceinline__ uint32_t parent_key_path(uint32_t path, int d, int t)
 }
 
 __global__ void heads_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.n_records) return;
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
-    uint32_t head = 0;
-    if (j < count) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
         const uint32_t i = a.e_item[buf][j];
         const int d = a.it_depth[i];
         const int t = d - step;
-        head = 1;
+        uint32_t head = 1;
         if (j > 0) {
             const uint32_t ip = a.e_item[buf][j - 1];
             if (ip == i && parent_key_path(a.e_path[buf][j - 1], d, t) == parent_key_path(a.e_path[buf][j], d, t))
                 head = 0;
         }
+        a.flags[j] = head;
     }
-    a.flags[j] = head;
 }
 
 __global__ void starts_kernel(DevInterner I, ApplyArgs a) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
-    if (j == 0) {
-        const uint32_t np = a.pos[a.n_records];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint32_t np = a.pos[count];
         a.p_start[np] = count;
         I.ctr->scratch[SC_PARENTS] = np;
         I.ctr->scratch[SC_ROOTS] = 0;
     }
-    if (j < count && a.flags[j]) a.p_start[a.pos[j]] = j;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
+        if (a.flags[j]) a.p_start[a.pos[j]] = j;
 }
 
 __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
@@ -494,7 +552,7 @@ __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
     const uint8_t f = a.it_flags[i];
     if ((f & 3) && nw != EMPTY_ID) atomicAdd(I.refcount + id_index(nw), 1u);  // the tree's root reference
     if (old != EMPTY_ID) {
-        if (nw == old) {  // assert_ne!(new_root_id, self.root_id) (voxtree.rs:311)
+        if (nw == old && !(I.flags & (1u << 4))) {  // assert_ne!(new_root_id, self.root_id) (voxtree.rs:311)
             set_error(I, ERR_REF_PANIC, 41);
             return;
         }
@@ -528,6 +586,25 @@ __global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
 }  // namespace
 
 size_t scan_tmp_words(uint32_t n) { return (size_t)(n + kScanBlock - 1) / kScanBlock + 32; }
+
+// Scan of the first *n_dev of n_max flags (count in device memory).
+static cudaError_t launch_scan_dev(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n_max,
+                                   const unsigned long long *n_dev, cudaStream_t s) {
+    const uint32_t nb = (n_max + kScanBlock - 1) / kScanBlock;
+    if (nb == 0) return cudaSuccess;
+    count_launches(1);
+    scan_blocks_dev_kernel<<<nb, kThreads, 0, s>>>(flags, pos, tmp, n_dev);
+    if (nb > 1) {
+        uint32_t *tmp2 = tmp + nb;
+        cudaError_t e = launch_scan(tmp, tmp2, tmp2 + nb + 1 + 32, nb, s);
+        if (e != cudaSuccess) return e;
+        count_launches(1);
+        scan_add_dev_kernel<<<nb, kThreads, 0, s>>>(pos, tmp2, n_dev);
+    }
+    count_launches(1);
+    scan_total_dev_kernel<<<1, 1, 0, s>>>(flags, pos, n_dev);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s) {
     const uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
@@ -587,13 +664,14 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
         count_launches(1);
         scatter_bottom_kernel<<<rb, kThreads, 0, s>>>(I, a);
         int buf = 0;
+        const unsigned sb = rb < (unsigned)num_sms * 16 ? rb : (unsigned)num_sms * 16;
         for (int step = 1; step <= a.max_depth - 1; ++step) {
             count_launches(1);
-            heads_kernel<<<rb, kThreads, 0, s>>>(I, a, step, buf);
-            e = launch_scan(a.flags, a.pos, a.scan_tmp, R, s);
+            heads_kernel<<<sb, kThreads, 0, s>>>(I, a, step, buf);
+            e = launch_scan_dev(a.flags, a.pos, a.scan_tmp, R, &I.ctr->scratch[SC_ENTRIES], s);
             if (e != cudaSuccess) return e;
             count_launches(1);
-            starts_kernel<<<rb, kThreads, 0, s>>>(I, a);
+            starts_kernel<<<sb, kThreads, 0, s>>>(I, a);
             count_launches(1);
             parents_kernel<<<g, bt, 0, s>>>(I, a, step, buf);
             count_launches(1);

@@ -1097,7 +1097,7 @@ cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, con
 
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s) {
     count_launches(1);
-    epoch_refcount_kernel<<<num_sms * 2, kThreads, 0, s>>>(I);
+    epoch_refcount_kernel<<<num_sms * 16, kThreads, 0, s>>>(I);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_epoch_finalize(I, s);

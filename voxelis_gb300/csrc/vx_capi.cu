@@ -1319,58 +1319,65 @@ int vx_validate(vx_interner *it, uint32_t n_trees, const vx_tree *trees) {
     return VX_OK;
 }
 
-int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid) {
-    if (!it || !out_grid || !tree_ok(it, tree)) return VX_E_INVALID_ARG;
-    Snapshot s;
-    int st = take_snapshot(it, s);
-    if (st != VX_OK) return st;
-    uint64_t root = 0;
-    st = read_root(it, tree, &root);
-    if (st != VX_OK) return st;
-    const int md = it->tree_depth[tree];
-    const size_t n = (size_t)1 << md, size = n * n * n;
-    const int vb = it->vbits / 8;
-    auto put = [&](size_t i, uint32_t v) {
-        if (vb == 1)
-            static_cast<uint8_t *>(out_grid)[i] = (uint8_t)v;
-        else
-            static_cast<uint16_t *>(out_grid)[i] = (uint16_t)v;
-    };
-    if (!id_is_branch(root)) {  // utils/common.rs:169-171
-        const uint32_t v = s.values[id_index(root)];
-        for (size_t i = 0; i < size; ++i) put(i, v);
-        return VX_OK;
+int vx_trees_to_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev, int depth, void *out_dev) {
+    if (!it || depth < 1 || depth > 10 || (n && (!trees_dev || !out_dev))) return VX_E_INVALID_ARG;
+    if (reinterpret_cast<uintptr_t>(out_dev) % 16) return set_err(it, VX_E_INVALID_ARG, "out_dev must be 16-byte aligned");
+    if (n == 0) return VX_OK;
+    const int lc = depth < 5 ? depth : 5;
+    const uint64_t cubes = (uint64_t)n << (3 * (depth - lc));
+    Phase ph(it, VX_PROF_GET);
+    VX_CUDA(launch_to_dense(it->dev, trees_dev, depth, 0, cubes, out_dev, it->num_sms, it->stream));
+    return VX_OK;
+}
+
+int vx_trees_to_dense(vx_interner *it, uint32_t n, const vx_tree *trees, void *out, vx_mem mem) {
+    if (!it || (n && (!trees || !out))) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    const int d = tree_ok(it, trees[0]) ? (int)it->tree_depth[trees[0]] : -1;
+    for (uint32_t k = 0; k < n; ++k)
+        if (!tree_ok(it, trees[k]) || it->tree_depth[trees[k]] != d) return VX_E_INVALID_ARG;
+    if (d < 1) return VX_E_INVALID_ARG;
+    const size_t vb = it->vbits / 8;
+    const int lc = d < 5 ? d : 5;
+    const uint64_t K = 1ull << (d - lc), S = 1ull << d;
+    const uint64_t slab_bytes = (S * S << lc) * vb;  // one cy-slab: K^2 cubes
+    const uint64_t n_slabs = (uint64_t)n * K;
+    if (mem == VX_MEM_DEVICE) {
+        if (reinterpret_cast<uintptr_t>(out) % 16) return set_err(it, VX_E_INVALID_ARG, "out must be 16-byte aligned");
+        VX_CUDA(it->staging.reserve(Carve::need({(size_t)n * 4})));
+        uint32_t *dt = static_cast<uint32_t *>(it->staging.p);
+        VX_CUDA(cudaMemcpyAsync(dt, trees, (size_t)n * 4, cudaMemcpyHostToDevice, it->stream));
+        {
+            Phase ph(it, VX_PROF_GET);
+            VX_CUDA(launch_to_dense(it->dev, dt, d, 0, n_slabs * K * K, out, it->num_sms, it->stream));
+        }
+        return sync_and_check(it);
     }
-    for (size_t i = 0; i < size; ++i) put(i, 0);
-    if (root == 0) return VX_OK;
-    struct E {
-        uint64_t id;
-        int32_t x, y, z;
-        int depth;
-    };
-    std::vector<E> stack{{root, 0, 0, 0, 0}};
-    while (!stack.empty()) {
-        E e = stack.back();
-        stack.pop_back();
-        const uint32_t idx = id_index(e.id);
-        if (id_is_branch(e.id) && e.depth < md) {
-            const int32_t half = 1 << (md - e.depth - 1);
-            for (int i = 7; i >= 0; --i) {
-                const uint64_t c = s.children[8ull * idx + i];
-                if (!c) continue;
-                stack.push_back({c, e.x + (i & 1) * half, e.y + ((i >> 1) & 1) * half, e.z + ((i >> 2) & 1) * half,
-                                 e.depth + 1});
-            }
-        } else {
-            const uint32_t v = s.values[idx];
-            if (!v) continue;
-            const size_t side = (size_t)1 << (md - e.depth);
-            for (size_t yy = e.y; yy < e.y + side; ++yy)
-                for (size_t zz = e.z; zz < e.z + side; ++zz)
-                    for (size_t xx = e.x; xx < e.x + side; ++xx) put((yy * n + zz) * n + xx, v);
+    // host output: whole cy-slabs through a device buffer of at most ~256 MiB per piece
+    const uint64_t piece_slabs = std::max<uint64_t>(1, ((uint64_t)256 << 20) / slab_bytes);
+    const uint64_t piece = std::min(piece_slabs, n_slabs);
+    VX_CUDA(it->staging.reserve(Carve::need({(size_t)n * 4, (size_t)(piece * slab_bytes)})));
+    Carve c(it->staging.p);
+    uint32_t *dt = c.take<uint32_t>(n);
+    uint8_t *dg = c.take<uint8_t>(piece * slab_bytes);
+    VX_CUDA(cudaMemcpyAsync(dt, trees, (size_t)n * 4, cudaMemcpyHostToDevice, it->stream));
+    for (uint64_t s0 = 0; s0 < n_slabs; s0 += piece) {
+        const uint64_t ns = std::min(piece, n_slabs - s0);
+        {
+            Phase ph(it, VX_PROF_GET);
+            VX_CUDA(launch_to_dense(it->dev, dt, d, s0 * K * K, ns * K * K, dg, it->num_sms, it->stream));
+        }
+        {
+            Phase ph(it, VX_PROF_COPY);
+            VX_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(out) + s0 * slab_bytes, dg, ns * slab_bytes,
+                                    cudaMemcpyDeviceToHost, it->stream));
         }
     }
-    return VX_OK;
+    return sync_and_check(it);
+}
+
+int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid) {
+    return vx_trees_to_dense(it, 1, &tree, out_grid, VX_MEM_HOST);
 }
 
 }  // extern "C"

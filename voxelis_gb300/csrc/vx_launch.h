@@ -93,6 +93,12 @@ size_t scan_tmp_words(uint32_t n);
 // ---- reads, releases, single-voxel operations, maintenance (vx_ops.cu) -------------------------
 cudaError_t launch_get_many(const DevInterner &I, uint64_t n, const uint32_t *trees, const int32_t *xyz,
                             uint8_t *found, void *values, int num_sms, cudaStream_t s);
+// to_vec over trees of depth d into [y][z][x] grids: cubes [cube_begin, cube_begin + n_cubes) of side
+// min(32, 2^d), ordered (tree, cy, cz, cx); cube_begin must start a cy-slab and `out` points at that
+// slab's first element.
+size_t to_dense_smem_bytes(int d, int vbits);
+cudaError_t launch_to_dense(const DevInterner &I, const uint32_t *trees, int d, uint64_t cube_begin,
+                            uint64_t n_cubes, void *out, int num_sms, cudaStream_t s);
 // Releases the roots listed in `list` (count at ctr->scratch[SC_RELEASE]) with `rounds`
 // breadth-first rounds, using two frontier buffers of `frontier_cap` entries.
 cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,

@@ -515,7 +515,188 @@ __global__ void count_live_kernel(DevInterner I, unsigned long long *out2) {
     }
 }
 
+
+// ---- to_vec: DAG -> dense grid (utils/common.rs:158-246) ----------------------------------------
+// One CTA per cube of side C = 2^lc (lc = min(d, 5)) of one tree; cubes are ordered (tree, cy, cz,
+// cx), so a run of whole cy-slabs is one contiguous range of the output. Thread 0 descends from the
+// root to the cube's root (d - lc levels); EMPTY or a leaf met on the way, or as the cube root, makes
+// the cube uniform (EMPTY children are never visited by to_vec, leaving the default; a leaf fills
+// its whole sub-cube). Otherwise the cube's subtree is expanded level by level in shared memory,
+// 8^k ids at level k in Morton order, a leaf or EMPTY replicating into its 8 children; the last
+// level resolves each voxel to the value of the node covering it (a leaf's value, or the value of a
+// node at depth d, as to_vec's else-branch does) and the CTA writes the cube row by row with 16-byte
+// stores.
+constexpr int kDenseOutThreads = 256;
+
+__device__ __forceinline__ uint32_t morton_compact3(uint32_t m) {
+    m &= 0x09249249u;
+    m = (m ^ (m >> 2)) & 0x030C30C3u;
+    m = (m ^ (m >> 4)) & 0x0300F00Fu;
+    m = (m ^ (m >> 8)) & 0x030000FFu;
+    m = (m ^ (m >> 16)) & 0x000003FFu;
+    return m;
+}
+
+template <class T>
+__device__ __forceinline__ uint4 replicate16(uint32_t v) {
+    uint32_t w = sizeof(T) == 1 ? (v & 0xFFu) * 0x01010101u : (v & 0xFFFFu) * 0x00010001u;
+    return make_uint4(w, w, w, w);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kDenseOutThreads) to_dense_kernel(DevInterner I, const uint32_t *trees, int d,
+                                                                     int lc, uint64_t cube_begin, uint64_t n_cubes,
+                                                                     T *out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t C = 1u << lc;
+    const uint32_t K = 1u << (d - lc);          // cubes per axis
+    const uint64_t K2 = (uint64_t)K * K, K3 = K2 * K;
+    const uint64_t S = 1ull << d;
+    const uint64_t slab_elems = (uint64_t)C * S * S;
+    const uint32_t tile_elems = C * C * C;
+    T *tile = reinterpret_cast<T *>(smem);
+    uint64_t *lv_big = reinterpret_cast<uint64_t *>(smem + ((tile_elems * sizeof(T) + 15) & ~15u));
+    uint64_t *lv_small = lv_big + (lc >= 1 ? (1u << (3 * (lc - 1))) : 1u);
+    __shared__ uint64_t cube_root;
+    __shared__ int uniform;  // 1: whole cube = cube_val
+    __shared__ uint32_t cube_val;
+    const uint64_t first_slab = cube_begin / K2;
+    bool bad = false;
+    for (uint64_t c = cube_begin + blockIdx.x; c < cube_begin + n_cubes; c += gridDim.x) {
+        const uint64_t t_idx = c / K3;
+        const uint32_t within = (uint32_t)(c % K3);
+        const uint32_t cx = within % K, cz = (within / K) % K, cy = within / (K * K);
+        if (threadIdx.x == 0) {
+            const uint32_t t = __ldg(trees + t_idx);
+            const int td = t < I.tree_cap ? I.depths[t] : TREE_UNUSED;
+            uint64_t node = EMPTY_ID;
+            int un = 1;
+            uint32_t val = 0;
+            if (td != d) {
+                bad = true;
+            } else {
+                node = I.roots[t];
+                const int L0 = d - lc;
+                for (int depth = 0; depth < L0 && node != EMPTY_ID && id_is_branch(node); ++depth) {
+                    const int sh = L0 - depth - 1;
+                    const uint32_t ci = ((cx >> sh) & 1) | (((cy >> sh) & 1) << 1) | (((cz >> sh) & 1) << 2);
+                    node = I.children[8ull * id_index(node) + ci];
+                }
+                if (node == EMPTY_ID) {
+                    val = 0;
+                } else if (!id_is_branch(node)) {
+                    val = node_value(I, id_index(node));
+                } else {
+                    un = 0;
+                }
+            }
+            cube_root = node;
+            uniform = un;
+            cube_val = val;
+        }
+        __syncthreads();
+        T *dst = out + (c / K2 - first_slab) * slab_elems;  // the cube's cy-slab
+        const uint64_t cube_off = (uint64_t)cz * C * S + (uint64_t)cx * C;
+        if (!uniform) {
+            // level-by-level expansion: level 0 is the cube root; ping-pong between the two id buffers
+            // so that level lc-1 (the parents of the voxels) lands in lv_big
+            uint64_t *cur = ((lc - 1) & 1) ? lv_small : lv_big;
+            if (threadIdx.x == 0) cur[0] = cube_root;
+            __syncthreads();
+            for (int k = 0; k + 1 < lc; ++k) {
+                uint64_t *nxt = (cur == lv_big) ? lv_small : lv_big;
+                const uint32_t m = 1u << (3 * (k + 1));
+                for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+                    const uint64_t p = cur[j >> 3];
+                    uint64_t ch = p;
+                    if (p != EMPTY_ID && id_is_branch(p)) ch = I.children[8ull * id_index(p) + (j & 7)];
+                    nxt[j] = ch;
+                }
+                __syncthreads();
+                cur = nxt;
+            }
+            const uint32_t m = 1u << (3 * (lc - 1));
+            for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+                const uint64_t p = cur[j];
+                uint32_t v8[8];
+                if (p == EMPTY_ID) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v8[k] = 0;
+                } else if (!id_is_branch(p)) {
+                    const uint32_t v = node_value(I, id_index(p));
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v8[k] = v;
+                } else {
+                    const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(I.children + 8ull * id_index(p));
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const ulonglong2 w = src[k];
+                        v8[2 * k] = w.x ? node_value(I, id_index(w.x)) : 0u;
+                        v8[2 * k + 1] = w.y ? node_value(I, id_index(w.y)) : 0u;
+                    }
+                }
+                const uint32_t bx = morton_compact3(j), by = morton_compact3(j >> 1), bz = morton_compact3(j >> 2);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const uint32_t x = 2 * bx + (k & 1), y = 2 * by + ((k >> 1) & 1), z = 2 * bz + (k >> 2);
+                    tile[(y * C + z) * C + x] = (T)v8[k];
+                }
+            }
+            __syncthreads();
+        }
+        // store the cube: rows of C elements along x
+        const uint32_t row_bytes = C * (uint32_t)sizeof(T);
+        if (row_bytes % 16 == 0) {
+            const uint32_t vec_per_row = row_bytes / 16, rows = C * C;
+            const uint4 fillv = replicate16<T>(cube_val);
+            for (uint32_t q = threadIdx.x; q < rows * vec_per_row; q += blockDim.x) {
+                const uint32_t r = q / vec_per_row, v = q % vec_per_row;
+                const uint32_t y = r / C, z = r % C;
+                uint4 w = uniform ? fillv : reinterpret_cast<const uint4 *>(tile + (size_t)r * C)[v];
+                T *row = dst + cube_off + (uint64_t)y * S * S + (uint64_t)z * S;
+                reinterpret_cast<uint4 *>(row)[v] = w;
+            }
+        } else {
+            for (uint32_t q = threadIdx.x; q < tile_elems; q += blockDim.x) {
+                const uint32_t y = q / (C * C), z = (q / C) % C, x = q % C;
+                dst[cube_off + (uint64_t)y * S * S + (uint64_t)z * S + x] = uniform ? (T)cube_val : tile[q];
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_error(I, ERR_INVALID, 52);
+}
 }  // namespace
+
+
+size_t to_dense_smem_bytes(int d, int vbits) {
+    const int lc = d < 5 ? d : 5;
+    const size_t tile = ((size_t)1 << (3 * lc)) * (vbits / 8);
+    const size_t big = lc >= 1 ? ((size_t)1 << (3 * (lc - 1))) : 1;
+    const size_t small = lc >= 2 ? ((size_t)1 << (3 * (lc - 2))) : 1;
+    return ((tile + 15) & ~(size_t)15) + 8 * (big + small);
+}
+
+cudaError_t launch_to_dense(const DevInterner &I, const uint32_t *trees, int d, uint64_t cube_begin,
+                            uint64_t n_cubes, void *out, int num_sms, cudaStream_t s) {
+    if (n_cubes == 0) return cudaSuccess;
+    const int lc = d < 5 ? d : 5;
+    const size_t smem = to_dense_smem_bytes(d, I.vbits);
+    uint64_t blocks = n_cubes;
+    const uint64_t cap = (uint64_t)num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    count_launches(1);
+    if (I.vbits == 8) {
+        cudaFuncSetAttribute(to_dense_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        to_dense_kernel<uint8_t><<<(unsigned)blocks, kDenseOutThreads, smem, s>>>(I, trees, d, lc, cube_begin,
+                                                                                  n_cubes, (uint8_t *)out);
+    } else {
+        cudaFuncSetAttribute(to_dense_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        to_dense_kernel<uint16_t><<<(unsigned)blocks, kDenseOutThreads, smem, s>>>(I, trees, d, lc, cube_begin,
+                                                                                   n_cubes, (uint16_t *)out);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_get_many(const DevInterner &I, uint64_t n, const uint32_t *trees, const int32_t *xyz,
                             uint8_t *found, void *values, int num_sms, cudaStream_t s) {

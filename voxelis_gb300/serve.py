@@ -1,6 +1,7 @@
 """A serving loop over a device-resident voxel world (continuous batching of edit and get requests).
 
-World: nx x ny x nz chunks of MaxDepth d in one interner (patches P1 + P4: carves are honoured).
+World: nx x ny x nz chunks of MaxDepth d in one interner (patches P1 + P4 + P5: carves are honoured,
+and a fill that leaves a chunk as it was is a no-op instead of the reference's assert_ne! panic).
 Requests arrive over time; each is either
   edit  a sphere brush (center, radius, value; value 0 carves) applied as Batch::just_set calls
         into one Batch per touched chunk, then apply_batch on each of those chunks, or
@@ -22,7 +23,7 @@ import time
 import numpy as np
 
 from . import workloads as W
-from ._abi import VX_PATCH_P1, VX_PATCH_P4, vx_interner_stats, vx_world, gpu_lib
+from ._abi import VX_PATCH_P1, VX_PATCH_P4, VX_PATCH_P5, vx_interner_stats, vx_world, gpu_lib
 
 EDIT, GET = 0, 1
 
@@ -30,7 +31,7 @@ EDIT, GET = 0, 1
 class World:
     """nx*ny*nz chunks of depth d; chunk id = (cy * nz + cz) * nx + cx."""
 
-    def __init__(self, nx, ny, nz, depth, budget, bits=8, patches=VX_PATCH_P1 | VX_PATCH_P4, lib=None):
+    def __init__(self, nx, ny, nz, depth, budget, bits=8, patches=VX_PATCH_P1 | VX_PATCH_P4 | VX_PATCH_P5, lib=None):
         import torch
 
         self.torch = torch

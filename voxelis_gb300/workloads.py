@@ -165,11 +165,61 @@ def caves(depth, seed=99, dtype=np.uint8):
     return out
 
 
-def random_edits(depth, density, seed, max_material=4095, clear_fraction=0.15):
-    """(x, y, z, value) edits at uniform positions: count = density * voxels; value 0 is a clear."""
+def caves_torch(depth, seed=99, device=None, y_block=64):
+    """caves() computed with torch (float64, op for op the same arithmetic as perlin3), for grids too
+    large to generate on the host in reasonable time; returns a [y][z][x] uint8 tensor on `device`."""
+    import torch
+
+    side = 1 << depth
+    perm = torch.tensor(permutation(seed), dtype=torch.int64, device=device)
+    g3 = torch.tensor(_G3, dtype=torch.float64, device=device)
+    out = torch.empty((side, side, side), dtype=torch.uint8, device=device)
+    zz, xx = torch.meshgrid(torch.arange(side, dtype=torch.float64, device=device) / 64.0,
+                            torch.arange(side, dtype=torch.float64, device=device) / 64.0, indexing="ij")
+
+    def fade(t):
+        return t * t * t * (t * (t * 6.0 - 15.0) + 10.0)
+
+    for y0 in range(0, side, y_block):
+        yy = (torch.arange(y0, min(side, y0 + y_block), dtype=torch.float64, device=device) / 64.0)[:, None, None]
+        x = xx[None].expand(yy.shape[0], side, side)
+        z = zz[None].expand(yy.shape[0], side, side)
+        y = yy.expand(yy.shape[0], side, side)
+        x0, y0_, z0 = torch.floor(x), torch.floor(y), torch.floor(z)
+        xi, yi, zi = x0.long() & 255, y0_.long() & 255, z0.long() & 255
+        xf, yf, zf = x - x0, y - y0_, z - z0
+        u, v, w = fade(xf), fade(yf), fade(zf)
+
+        def g(ix, iy, iz, dx, dy, dz):
+            h = perm[perm[perm[ix] + iy] + iz] & 15
+            return g3[h, 0] * dx + g3[h, 1] * dy + g3[h, 2] * dz
+
+        n000 = g(xi, yi, zi, xf, yf, zf)
+        n100 = g(xi + 1, yi, zi, xf - 1, yf, zf)
+        n010 = g(xi, yi + 1, zi, xf, yf - 1, zf)
+        n110 = g(xi + 1, yi + 1, zi, xf - 1, yf - 1, zf)
+        n001 = g(xi, yi, zi + 1, xf, yf, zf - 1)
+        n101 = g(xi + 1, yi, zi + 1, xf - 1, yf, zf - 1)
+        n011 = g(xi, yi + 1, zi + 1, xf, yf - 1, zf - 1)
+        n111 = g(xi + 1, yi + 1, zi + 1, xf - 1, yf - 1, zf - 1)
+        x00 = n000 + u * (n100 - n000)
+        x10 = n010 + u * (n110 - n010)
+        x01 = n001 + u * (n101 - n001)
+        x11 = n011 + u * (n111 - n011)
+        a = x00 + v * (x10 - x00)
+        b = x01 + v * (x11 - x01)
+        n = a + w * (b - a)
+        out[y0:y0 + yy.shape[0]] = torch.where(n > 0.1, 1 + torch.floor(3 * torch.abs(n)),
+                                               torch.zeros_like(n)).to(torch.uint8)
+    return out
+
+
+def random_edits(depth, density, seed, max_material=4095, clear_fraction=0.15, count=None):
+    """(x, y, z, value) edits at uniform positions: count = density * voxels (or `count`); value 0 is
+    a clear."""
     side = 1 << depth
     rng = np.random.default_rng(seed)
-    n = max(1, int(round(density * side ** 3)))
+    n = count if count is not None else max(1, int(round(density * side ** 3)))
     xyz = rng.integers(0, side, size=(n, 3), dtype=np.int64)
     vals = rng.integers(1, max_material + 1, size=n, dtype=np.int64)
     vals[rng.random(n) < clear_fraction] = 0
