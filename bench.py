@@ -124,6 +124,19 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def profiled_traffic(summary):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) recorded from one ncu
+    capture in profiles/<summary>: the line 'traffic_bytes_per_launch: N', or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            for ln in f:
+                if ln.strip().startswith("traffic_bytes_per_launch:"):
+                    return int(float(ln.split(":", 1)[1].split()[0]))
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 # ---- the CPU legs ----------------------------------------------------------------------------------
 def oracle_lib():
     from oracle import build as oracle_build
@@ -408,7 +421,8 @@ def run_ours(args):
         "batched_over_per_chunk": pc_ms / ms,
         "dag": {"nodes": int(new_nodes), "canonical_nodes": int(len(canon["kind"])), "node_size": int(node_size)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "dense_blocks_kernel",
+                     "frac": achieved / peak, "traffic": profiled_traffic("dense_octants_kernel_dunes4096.md"),
+                     "kernel": "dense_octants_kernel",
                      "kernel_ms": dense_ms, "algorithmic_bytes": int(algo_bytes), "peak_kind": peak_kind},
         "phases": phases,
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "chunks/s", "ms": e2e_ms,

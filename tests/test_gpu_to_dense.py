@@ -2,7 +2,8 @@
 oracle's to_vec, tree by tree, bit-exact (integer work). Covers every depth 1..8, u8 and u16, EMPTY
 trees, trees whose root is a leaf (fill), collapsed leaves at every level (P1 + uniform sub-cubes),
 host and device output, and a size-independent round trip (dense build -> to_vec == input) on a
-MaxDepth 9 tree. A tree of the wrong depth is refused."""
+MaxDepth 9 tree. A tree of the wrong depth is refused. (MaxDepth 1 trees are made with fill and
+single-voxel set: the reference's batch path needs MaxDepth >= 2.)"""
 import ctypes as C
 
 import numpy as np
@@ -25,6 +26,12 @@ def _trees(lib, depth, bits, seed, n=5):
     side = 1 << depth
     hi = 255 if bits == 8 else 4095
     trees[1].fill(it, 7)
+    if depth < 2:  # batches need MaxDepth >= 2 (the reference's batch path underflows below)
+        trees[2].fill(it, 3)
+        trees[3].set(it, (1, 0, 1), 9)
+        trees[4].set(it, (0, 1, 0), 5)
+        trees[4].set(it, (1, 1, 1), 6)
+        return it, trees
     # blocky: 4^3-voxel (or whole-tree) blocks of one value, so leaves sit at several depths
     blk = max(1, side // 4)
     coarse = rng.integers(0, 4, (side // blk,) * 3)

@@ -23,6 +23,7 @@
 // the number of child slots of newly created nodes that name it, plus one per tree root. That sum is
 // computed once per epoch over the allocation log (launch_epoch_refcounts) instead of per lookup.
 #include <cuda.h>
+#include <type_traits>
 #include <cudaTypedefs.h>
 
 #include "vx_launch.h"
@@ -318,37 +319,46 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
 #ifndef VX_OCT_TILES
 #define VX_OCT_TILES 1
 #endif
+#ifndef VX_TILE_V2
+#define VX_TILE_V2 3  // 0: per-lane groups; 2: + shared quad cache; 3: + device-wide quad memo
+#endif
 constexpr int kKeyCache = VX_KEY_CACHE;  // entries of the shared bottom-key cache (power of two)
 constexpr int kOctTiles = VX_OCT_TILES;  // tile buffers per warp in the octant kernel (1 or 2)
 
 struct KeyCache {
     uint64_t *k0, *k1, *id;
+    uint32_t *val;  // LOD value of each entry, or null when the caller does not cache it
 };
 
 __device__ __forceinline__ uint32_t kc_slot(uint64_t lo, uint64_t hi) {
     return (uint32_t)(fmix64(lo ^ (hi * 0x9E3779B97F4A7C15ull)) >> 40) & (kKeyCache - 1);
 }
 
-// Branch id cached for (lo, hi), or 0. An entry is published by writing its id (>= 2) last.
-__device__ __forceinline__ uint64_t kc_lookup(const KeyCache &C, uint64_t lo, uint64_t hi) {
+// Branch id cached for (lo, hi), or 0 (and its LOD value in *lod when cached). An entry is
+// published by writing its id (>= 2) last.
+__device__ __forceinline__ uint64_t kc_lookup(const KeyCache &C, uint64_t lo, uint64_t hi, uint32_t *lod = nullptr) {
     uint32_t h = kc_slot(lo, hi);
 #pragma unroll 1
     for (int p = 0; p < 8; ++p) {
         const uint64_t id = *(volatile uint64_t *)(C.id + h);
         if (id == 0) return 0;
-        if (id > 1 && *(volatile uint64_t *)(C.k0 + h) == lo && *(volatile uint64_t *)(C.k1 + h) == hi) return id;
+        if (id > 1 && *(volatile uint64_t *)(C.k0 + h) == lo && *(volatile uint64_t *)(C.k1 + h) == hi) {
+            if (lod) *lod = *(volatile uint32_t *)(C.val + h);
+            return id;
+        }
         h = (h + 1) & (kKeyCache - 1);
     }
     return 0;
 }
 
-__device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64_t hi, uint64_t id) {
+__device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64_t hi, uint64_t id, uint32_t lod = 0) {
     uint32_t h = kc_slot(lo, hi);
 #pragma unroll 1
     for (int p = 0; p < 8; ++p) {
         if (atomicCAS((unsigned long long *)(C.id + h), 0ull, 1ull) == 0ull) {
             C.k0[h] = lo;
             C.k1[h] = hi;
+            if (C.val) C.val[h] = lod;
             __threadfence_block();
             *(volatile uint64_t *)(C.id + h) = id;
             return;
@@ -625,6 +635,12 @@ struct OctArgs {
     uint32_t *cnt;   // arrival counts of levels 0 .. depth-5 at cnt_off[k]
     uint64_t lvl_off[12];
     uint64_t cnt_off[12];
+    // quad memo (optional: slots == nullptr disables it)
+    unsigned long long *memo_slots;  // tag:32 | (record + 1):32, 0 = empty
+    unsigned int *memo_count;        // records handed out
+    unsigned char *memo_recs;        // record r: 16 row words, then id (8 B) and LOD value (4 B)
+    uint32_t memo_mask;              // slots - 1
+    uint32_t memo_cap;               // records
 };
 
 constexpr int kOctWarps = 8;
@@ -735,6 +751,553 @@ __device__ __forceinline__ void reduce_tile16(const DevInterner &I, const T *til
     oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
 }
 
+// ---- octant reduction with whole-quad fast paths ------------------------------------------------
+//
+// Lane l owns the level-3 parents ("quads", 4^3 voxels) l and l+32 of the warp's 16^3 octant. It
+// loads the quad as 16 row words (4 voxels along x each) and decides with word compares whether the
+// quad is uniform: then the quad is EMPTY or one leaf and none of its 8 bottom groups needs any
+// work, exactly what Phase 1 + Phase 2 produce for it (a uniform full group becomes a leaf; 8 equal
+// leaves collapse; 8 EMPTY children leave EMPTY). For 8-bit voxels a non-uniform quad's 64 raw
+// bytes then key a CTA-wide cache of the quads this CTA already reduced (the quad's node is a pure
+// function of its voxels), so repeated surface patterns skip the group work too. Parents above the
+// quads are looked up in the same cache by their 8 child ids. Every cache entry also holds the
+// node's LOD value, so hits skip calc_average. Only misses reach the bottom-group path of
+// reduce_tile16 and the global branch table.
+
+#ifndef VX_NODE_CACHE
+#define VX_NODE_CACHE 256
+#endif
+constexpr int kNodeCache = VX_NODE_CACHE;  // entries (power of two)
+constexpr int kNodeCacheAlloc = VX_TILE_V2 ? kNodeCache : 0;  // entries with shared memory behind them
+
+struct NodeCache {
+    uint64_t *key;   // [kNodeCache][8]
+    uint64_t *id;    // 0 free, 1 being written, else a branch id
+    uint32_t *meta;  // kind << 31 | LOD value (kind 0: quad voxels, 1: child ids)
+};
+
+__device__ __forceinline__ uint32_t nc_slot(const uint64_t k[8], uint32_t kind) {
+    uint32_t h = kind ? 0x2545F491u : 0x9E3779B9u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        h = h * 0x01000193u + (uint32_t)k[i];
+        h = h * 0x01000193u + (uint32_t)(k[i] >> 32);
+    }
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    return h & (kNodeCache - 1);
+}
+
+__device__ __forceinline__ uint64_t nc_lookup(const NodeCache &N, const uint64_t k[8], uint32_t kind,
+                                              uint32_t &lod) {
+    uint32_t h = nc_slot(k, kind);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        const uint64_t id = *(volatile uint64_t *)(N.id + h);
+        if (id == 0) return 0;
+        if (id > 1) {
+            const uint32_t m = *(volatile uint32_t *)(N.meta + h);
+            bool eq = (m >> 31) == kind;
+            const volatile ulonglong2 *e = reinterpret_cast<const volatile ulonglong2 *>(N.key + 8 * h);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint64_t a = e[i].x, b = e[i].y;
+                eq = eq && a == k[2 * i] && b == k[2 * i + 1];
+            }
+            if (eq) {
+                lod = m & 0x7FFFFFFFu;
+                return id;
+            }
+        }
+        h = (h + 1) & (kNodeCache - 1);
+    }
+    return 0;
+}
+
+__device__ __forceinline__ void nc_insert(const NodeCache &N, const uint64_t k[8], uint32_t kind, uint64_t id,
+                                          uint32_t lod) {
+    uint32_t h = nc_slot(k, kind);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        if (atomicCAS((unsigned long long *)(N.id + h), 0ull, 1ull) == 0ull) {
+            ulonglong2 *e = reinterpret_cast<ulonglong2 *>(N.key + 8 * h);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) e[i] = make_ulonglong2(k[2 * i], k[2 * i + 1]);
+            N.meta[h] = (kind << 31) | lod;
+            __threadfence_block();
+            *(volatile uint64_t *)(N.id + h) = id;
+            return;
+        }
+        h = (h + 1) & (kNodeCache - 1);
+    }
+}
+
+// reduce_parent with the parent looked up first in the node cache by its 8 child ids.
+__device__ __forceinline__ void reduce_parent_cached(const DevInterner &I, const NodeCache &N, bool active,
+                                                     const uint64_t c[8], const uint32_t cv[8], uint64_t &out,
+                                                     uint32_t &out_val) {
+    uint32_t types = 0, mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        mask |= (c[k] != 0 ? 1u : 0u) << k;
+        types |= (id_is_leaf(c[k]) ? 1u : 0u) << k;
+    }
+    bool same = types == 0xFF;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
+    const bool is_branch = active && mask != 0 && !same;
+    uint32_t lod = 0;
+    uint64_t id = is_branch ? nc_lookup(N, c, 1u, lod) : 0ull;
+    const bool need = is_branch && id == 0;
+    if (__any_sync(0xFFFFFFFFu, need)) {
+        if (need) lod = calc_average8(cv);
+        bool created;
+        const uint64_t nid = warp_intern_branch(I, need, c, types, mask, lod, &created);
+        if (need) {
+            id = nid;
+            if (nid != INVALID_ID) nc_insert(N, c, 1u, nid, lod);
+        }
+    }
+    if (mask == 0) {
+        out = EMPTY_ID;
+        out_val = 0;
+    } else if (same) {
+        out = c[0];
+        out_val = cv[0];
+    } else {
+        out = id;
+        out_val = lod;
+    }
+}
+
+// Nonzero-voxel mask of 8 voxels packed as in load_group32 (voxel j in bits [j*w, (j+1)*w)).
+template <class T>
+__device__ __forceinline__ uint32_t set_mask8(uint64_t lo, uint64_t hi) {
+    if (sizeof(T) == 1) {
+        const uint32_t a = __vcmpne4((uint32_t)lo, 0u) & 0x01010101u, b = __vcmpne4((uint32_t)(lo >> 32), 0u) & 0x01010101u;
+        return ((a * 0x01020408u) >> 24) | (((b * 0x01020408u) >> 24) << 4);
+    } else {
+        auto nz2 = [](uint32_t x) {
+            const uint32_t m = __vcmpne2(x, 0u) & 0x00010001u;
+            return (m | (m >> 15)) & 3u;
+        };
+        return nz2((uint32_t)lo) | (nz2((uint32_t)(lo >> 32)) << 2) | (nz2((uint32_t)hi) << 4) |
+               (nz2((uint32_t)(hi >> 32)) << 6);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void unpack8(uint64_t lo, uint64_t hi, uint32_t v[8]) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (sizeof(T) == 1)
+            v[j] = (uint32_t)(lo >> (8 * j)) & 0xFFu;
+        else
+            v[j] = (uint32_t)((j < 4 ? lo : hi) >> (16 * (j & 3))) & 0xFFFFu;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void reduce_tile16_v2(const DevInterner &I, const T *tile, const KeyCache &C,
+                                                 const NodeCache &N, uint64_t *leaf_cache, uint64_t &oct_id,
+                                                 uint32_t &oct_val) {
+    using W = typename std::conditional<sizeof(T) == 1, uint32_t, uint64_t>::type;  // 4 voxels along x
+    const unsigned lane = threadIdx.x & 31u;
+    const bool wide = sizeof(T) == 2;
+    uint64_t l3[2];
+    uint32_t l3v[2];
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        const uint32_t p = lane + 32 * pass;
+        const uint32_t qx = compact3(p), qy = compact3(p >> 1), qz = compact3(p >> 2);
+        const T *qbase = tile + ((4 * qy) * 16 + 4 * qz) * 16 + 4 * qx;
+        // the quad's 16 row words, row r = yy * 4 + zz
+        W w[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) w[r] = *reinterpret_cast<const W *>(qbase + ((r >> 2) * 16 + (r & 3)) * 16);
+        const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
+        const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
+        bool uniform = true;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) uniform = uniform && w[r] == splat;
+        uint64_t qid = 0;
+        uint32_t qval = 0;
+        bool active = false;
+        uint64_t key[8];
+        if (uniform) {
+            qid = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
+            qval = v0;
+        } else if (sizeof(T) == 1) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) key[i] = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
+            qid = nc_lookup(N, key, 0u, qval);
+            active = qid == 0;
+        } else {
+            active = true;
+        }
+        if (__any_sync(0xFFFFFFFFu, active)) {
+            uint64_t c3[8];
+            uint32_t cv3[8];
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                // bottom group k of the quad: rows (2gy + dy, 2gz + dz), voxels 2gx, 2gx + 1
+                const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
+                const T *g = qbase + ((2 * gy) * 16 + 2 * gz) * 16 + 2 * gx;
+                uint64_t lo = 0, hi = 0;
+                if (sizeof(T) == 1) {
+                    const uint32_t p0 = *reinterpret_cast<const uint16_t *>(g);
+                    const uint32_t p1 = *reinterpret_cast<const uint16_t *>(g + 256);
+                    const uint32_t p2 = *reinterpret_cast<const uint16_t *>(g + 16);
+                    const uint32_t p3 = *reinterpret_cast<const uint16_t *>(g + 272);
+                    lo = (uint64_t)(p0 | (p1 << 16)) | ((uint64_t)(p2 | (p3 << 16)) << 32);
+                } else {
+                    lo = (uint64_t)*reinterpret_cast<const uint32_t *>(g) |
+                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 256) << 32);
+                    hi = (uint64_t)*reinterpret_cast<const uint32_t *>(g + 16) |
+                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 272) << 32);
+                }
+                const uint32_t set = set_mask8<T>(lo, hi);
+                const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+                const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
+                                                 : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
+                const bool is_branch = active && set != 0 && !(guni && set == 0xFFu);
+                uint32_t lod = 0;
+                uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
+                const bool need = is_branch && id == 0;
+                const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+                if (bm) {  // warp-uniform
+                    uint32_t v[8];
+                    unpack8<T>(lo, hi, v);
+                    if (need) lod = calc_average8(v);
+                    unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+                    if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+                    grp &= bm;
+                    const int leader = need ? __ffs(grp) - 1 : (int)lane;
+                    const bool lead = need && leader == (int)lane;
+                    uint64_t c[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+                    bool created;
+                    uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+                    nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+                    if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+                    if (need) id = nid;
+                }
+                if (set == 0) {
+                    c3[k] = EMPTY_ID;
+                    cv3[k] = 0;
+                } else if (!is_branch) {  // a uniform full group (or an inactive lane)
+                    c3[k] = active ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
+                    cv3[k] = gv0;
+                } else {
+                    c3[k] = id;
+                    cv3[k] = lod;
+                }
+            }
+            uint64_t pid;
+            uint32_t pval;
+            reduce_parent(I, active, c3, cv3, pid, pval);
+            if (active) {
+                qid = pid;
+                qval = pval;
+                if (sizeof(T) == 1 && pid != INVALID_ID) {
+                    // the key again from the tile (cheaper than keeping 16 registers live)
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        key[i] = (uint64_t)*reinterpret_cast<const W *>(qbase + (((2 * i) >> 2) * 16 + ((2 * i) & 3)) * 16) |
+                                 ((uint64_t)*reinterpret_cast<const W *>(qbase + (((2 * i + 1) >> 2) * 16 + ((2 * i + 1) & 3)) * 16)
+                                  << 32);
+                    nc_insert(N, key, 0u, pid, pval);
+                }
+            }
+        }
+        l3[pass] = qid;
+        l3v[pass] = qval;
+    }
+    // level 2: lane q < 8 takes quads 8q .. 8q+7 (pass q >> 2)
+    uint64_t c2[8];
+    uint32_t cv2[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int src = (8 * lane + j) & 31;
+        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
+        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
+        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
+        cv2[j] = lane < 4 ? b0 : b1;
+    }
+    uint64_t l2;
+    uint32_t l2v;
+    reduce_parent_cached(I, N, lane < 8, c2, cv2, l2, l2v);
+    uint64_t c1[8];
+    uint32_t cv1[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
+        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
+    }
+    uint64_t l1;
+    uint32_t l1v;
+    reduce_parent_cached(I, N, lane == 0, c1, cv1, l1, l1v);
+    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
+    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
+}
+
+// ---- octant reduction with a device-wide quad memo ---------------------------------------------
+//
+// Terrain repeats: the 4096-chunk dune workload has 508k non-uniform quads (4^3 voxels) but only
+// 4,468 distinct ones. A quad's node is a pure function of its voxels, so a call-wide memo in global
+// memory (open addressing, 64-bit slots tag:32 | record+1, records = the quad's 16 row words, its node
+// id and LOD value, published by a CAS after the record is written and fenced) replaces the 8-group
+// reduction and the level-3 intern of every repeated quad by one slot load and one record load. Each
+// lane keeps its two quads' probes in flight together. Misses take the bottom-group path of
+// reduce_tile16_v2 and insert the result; the memo only ever holds nodes created or found in this
+// call (no release runs during a build), and inserts stop when its records run out.
+
+template <class T>
+struct QuadWord {
+    using type = typename std::conditional<sizeof(T) == 1, uint32_t, uint64_t>::type;
+};
+
+template <class T>
+__device__ __forceinline__ void quad_rows(const T *qbase, typename QuadWord<T>::type w[16]) {
+    using W = typename QuadWord<T>::type;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) w[r] = *reinterpret_cast<const W *>(qbase + ((r >> 2) * 16 + (r & 3)) * 16);
+}
+
+// Record r's address; the record's content is 16 row words of 4 voxels.
+template <class T>
+__device__ __forceinline__ unsigned char *memo_rec(const OctArgs &a, uint32_t r) {
+    return a.memo_recs + (size_t)r * (16 * 4 * sizeof(T) + 16);
+}
+
+template <class T>
+__device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T *qbase, uint64_t &id, uint32_t &lod) {
+    using W = typename QuadWord<T>::type;
+    const unsigned char *rec = memo_rec<T>(a, r);
+    const uint4 *rv = reinterpret_cast<const uint4 *>(rec);
+    bool eq = true;
+#pragma unroll
+    for (int k = 0; k < 4 * (int)sizeof(T); ++k) {
+        const uint4 x = __ldcg(rv + k);
+        if (sizeof(T) == 1) {
+            eq = eq && x.x == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k) >> 2) * 16 + ((4 * k) & 3)) * 16) &&
+                 x.y == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 1) >> 2) * 16 + ((4 * k + 1) & 3)) * 16) &&
+                 x.z == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 2) >> 2) * 16 + ((4 * k + 2) & 3)) * 16) &&
+                 x.w == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 3) >> 2) * 16 + ((4 * k + 3) & 3)) * 16);
+        } else {
+            const W a0 = *reinterpret_cast<const W *>(qbase + (((2 * k) >> 2) * 16 + ((2 * k) & 3)) * 16);
+            const W a1 = *reinterpret_cast<const W *>(qbase + (((2 * k + 1) >> 2) * 16 + ((2 * k + 1) & 3)) * 16);
+            eq = eq && ((uint64_t)x.x | ((uint64_t)x.y << 32)) == (uint64_t)a0 &&
+                 ((uint64_t)x.z | ((uint64_t)x.w << 32)) == (uint64_t)a1;
+        }
+    }
+    if (!eq) return false;
+    const uint4 tail = __ldcg(reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T)));
+    id = (uint64_t)tail.x | ((uint64_t)tail.y << 32);
+    lod = tail.z;
+    return true;
+}
+
+template <class T>
+__device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint32_t h2, const T *qbase, uint64_t id,
+                                            uint32_t lod) {
+    using W = typename QuadWord<T>::type;
+    const uint32_t r = atomicAdd(a.memo_count, 1u);
+    if (r >= a.memo_cap) return;
+    unsigned char *rec = memo_rec<T>(a, r);
+    W *dst = reinterpret_cast<W *>(rec);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) dst[k] = *reinterpret_cast<const W *>(qbase + ((k >> 2) * 16 + (k & 3)) * 16);
+    *reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T)) = make_uint4((uint32_t)id, (uint32_t)(id >> 32), lod, 0u);
+    __threadfence();
+    uint32_t slot = h1 & a.memo_mask;
+    const unsigned long long v = ((unsigned long long)h2 << 32) | (r + 1u);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        if (atomicCAS(a.memo_slots + slot, 0ull, v) == 0ull) return;
+        slot = (slot + 1) & a.memo_mask;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const OctArgs &a, const T *tile,
+                                                 const KeyCache &C, const NodeCache &N, uint64_t *leaf_cache,
+                                                 uint64_t &oct_id, uint32_t &oct_val) {
+    using W = typename QuadWord<T>::type;
+    const unsigned lane = threadIdx.x & 31u;
+    const bool wide = sizeof(T) == 2;
+    const bool memo = a.memo_slots != nullptr;
+    const T *qb[2];
+    bool uni[2];
+    uint32_t h1[2], h2[2];
+    uint64_t qid[2];
+    uint32_t qval[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const uint32_t p = lane + 32 * q;
+        const uint32_t qx = compact3(p), qy = compact3(p >> 1), qz = compact3(p >> 2);
+        qb[q] = tile + ((4 * qy) * 16 + 4 * qz) * 16 + 4 * qx;
+        W w[16];
+        quad_rows<T>(qb[q], w);
+        const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
+        const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
+        bool u = true;
+        uint32_t x = 0x9E3779B9u, y = 0x7F4A7C15u;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            u = u && w[r] == splat;
+            x = x * 0x01000193u + (uint32_t)w[r];
+            y = (y ^ (uint32_t)w[r]) * 0x85EBCA6Bu;
+            if (sizeof(T) == 2) {
+                x = x * 0x01000193u + (uint32_t)((uint64_t)w[r] >> 32);
+                y = (y ^ (uint32_t)((uint64_t)w[r] >> 32)) * 0x85EBCA6Bu;
+            }
+        }
+        x ^= x >> 15;
+        x *= 0x2C1B3C6Du;
+        x ^= x >> 12;
+        y ^= y >> 16;
+        uni[q] = u;
+        h1[q] = x;
+        h2[q] = y;
+        qid[q] = 0;
+        qval[q] = v0;
+        if (u) qid[q] = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
+    }
+    // memo probes, both quads in flight
+    bool look[2];
+    uint32_t slot[2];
+    unsigned long long sv[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        look[q] = memo && !uni[q];
+        slot[q] = h1[q] & a.memo_mask;
+        sv[q] = look[q] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[q]) : 0ull;
+    }
+#pragma unroll 1
+    for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!look[q]) continue;
+            if (sv[q] == 0ull) {
+                look[q] = false;  // empty slot: not in the memo
+            } else if ((uint32_t)(sv[q] >> 32) == h2[q] &&
+                       memo_match<T>(a, (uint32_t)sv[q] - 1u, qb[q], qid[q], qval[q])) {
+                look[q] = false;
+            } else if (step == 3) {
+                look[q] = false;
+            } else {
+                slot[q] = (slot[q] + 1) & a.memo_mask;
+                sv[q] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[q]);
+            }
+        }
+    }
+    uint64_t l3[2];
+    uint32_t l3v[2];
+#pragma unroll 1
+    for (int q = 0; q < 2; ++q) {
+        const bool active = !uni[q] && qid[q] == 0;
+        if (__any_sync(0xFFFFFFFFu, active)) {
+            const T *qbase = qb[q];
+            uint64_t c3[8];
+            uint32_t cv3[8];
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
+                const T *g = qbase + ((2 * gy) * 16 + 2 * gz) * 16 + 2 * gx;
+                uint64_t lo = 0, hi = 0;
+                if (sizeof(T) == 1) {
+                    const uint32_t p0 = *reinterpret_cast<const uint16_t *>(g);
+                    const uint32_t p1 = *reinterpret_cast<const uint16_t *>(g + 256);
+                    const uint32_t p2 = *reinterpret_cast<const uint16_t *>(g + 16);
+                    const uint32_t p3 = *reinterpret_cast<const uint16_t *>(g + 272);
+                    lo = (uint64_t)(p0 | (p1 << 16)) | ((uint64_t)(p2 | (p3 << 16)) << 32);
+                } else {
+                    lo = (uint64_t)*reinterpret_cast<const uint32_t *>(g) |
+                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 256) << 32);
+                    hi = (uint64_t)*reinterpret_cast<const uint32_t *>(g + 16) |
+                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 272) << 32);
+                }
+                const uint32_t set = set_mask8<T>(lo, hi);
+                const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+                const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
+                                                 : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
+                const bool is_branch = active && set != 0 && !(guni && set == 0xFFu);
+                uint32_t lod = 0;
+                uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
+                const bool need = is_branch && id == 0;
+                const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+                if (bm) {
+                    uint32_t v[8];
+                    unpack8<T>(lo, hi, v);
+                    if (need) lod = calc_average8(v);
+                    unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+                    if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+                    grp &= bm;
+                    const int leader = need ? __ffs(grp) - 1 : (int)lane;
+                    const bool lead = need && leader == (int)lane;
+                    uint64_t c[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+                    bool created;
+                    uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+                    nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+                    if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+                    if (need) id = nid;
+                }
+                if (set == 0) {
+                    c3[k] = EMPTY_ID;
+                    cv3[k] = 0;
+                } else if (!is_branch) {
+                    c3[k] = active ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
+                    cv3[k] = gv0;
+                } else {
+                    c3[k] = id;
+                    cv3[k] = lod;
+                }
+            }
+            uint64_t pid;
+            uint32_t pval;
+            reduce_parent(I, active, c3, cv3, pid, pval);
+            if (active) {
+                qid[q] = pid;
+                qval[q] = pval;
+                if (memo && pid != INVALID_ID) memo_insert<T>(a, h1[q], h2[q], qbase, pid, pval);
+            }
+        }
+        l3[q] = qid[q];
+        l3v[q] = qval[q];
+    }
+    // level 2: lane q < 8 takes quads 8q .. 8q+7 (pass q >> 2)
+    uint64_t c2[8];
+    uint32_t cv2[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int src = (8 * lane + j) & 31;
+        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
+        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
+        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
+        cv2[j] = lane < 4 ? b0 : b1;
+    }
+    uint64_t l2;
+    uint32_t l2v;
+    reduce_parent_cached(I, N, lane < 8, c2, cv2, l2, l2v);
+    uint64_t c1[8];
+    uint32_t cv1[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
+        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
+    }
+    uint64_t l1;
+    uint32_t l1v;
+    reduce_parent_cached(I, N, lane == 0, c1, cv1, l1, l1v);
+    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
+    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
+}
+
 __device__ __forceinline__ void tma_load_octant(void *dst, const CUtensorMap *tmap, int x, int z, int y, int c,
                                                 uint64_t *bar) {
     asm volatile(
@@ -744,19 +1307,28 @@ __device__ __forceinline__ void tma_load_octant(void *dst, const CUtensorMap *tm
         : "memory");
 }
 
+#ifdef VX_OCT_MAXNREG
+#define VX_OCT_BOUNDS __maxnreg__(VX_OCT_MAXNREG)
+#else
+#define VX_OCT_BOUNDS __launch_bounds__(kThreads)
+#endif
 template <class T>
-__global__ void __launch_bounds__(kThreads) dense_octants_kernel(DevInterner I, OctArgs a,
+__global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
                                                                  const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr uint32_t TILE = 4096 * sizeof(T);
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     T *tiles = reinterpret_cast<T *>(smem + warp * kOctTiles * TILE);
     uint64_t *kc = reinterpret_cast<uint64_t *>(smem + kOctWarps * kOctTiles * TILE);
-    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache};
     uint64_t *leaf_cache = kc + 3 * kKeyCache;
     uint64_t *bars = leaf_cache + 256 + warp * 2;
+    uint64_t *nc = leaf_cache + 256 + 2 * kOctWarps;
+    uint32_t *u32s = reinterpret_cast<uint32_t *>(nc + 9 * kNodeCacheAlloc);
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, u32s};
+    NodeCache N{nc, nc + 8 * kNodeCache, u32s + kKeyCache};
 
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    for (unsigned k = tid; k < kNodeCacheAlloc; k += blockDim.x) N.id[k] = 0;
     if (sizeof(T) == 1)
         for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
     if (lane == 0) {
@@ -809,7 +1381,13 @@ __global__ void __launch_bounds__(kThreads) dense_octants_kernel(DevInterner I, 
         }
         uint64_t node;
         uint32_t val;
+#if VX_TILE_V2 == 3
+        reduce_tile16_v3<T>(I, a, tiles + buf * 4096, C, N, leaf_cache, node, val);
+#elif VX_TILE_V2
+        reduce_tile16_v2<T>(I, tiles + buf * 4096, C, N, leaf_cache, node, val);
+#else
         reduce_tile16<T>(I, tiles + buf * 4096, C, leaf_cache, node, val);
+#endif
         __syncwarp();
         if (kOctTiles == 1 && nx < n_oct && lane == 0) issue(nx, 0);  // single buffer: load after use
         // climb while this warp brings the last child of a parent
@@ -846,7 +1424,11 @@ __global__ void __launch_bounds__(kThreads) dense_octants_kernel(DevInterner I, 
                 ch[j] = __shfl_sync(0xFFFFFFFFu, sid, j);
                 cv[j] = __shfl_sync(0xFFFFFFFFu, sval, j);
             }
+#if VX_TILE_V2
+            reduce_parent_cached(I, N, lane == 0, ch, cv, node, val);
+#else
             reduce_parent(I, lane == 0, ch, cv, node, val);
+#endif
             node = __shfl_sync(0xFFFFFFFFu, node, 0);
             val = __shfl_sync(0xFFFFFFFFu, val, 0);
             q >>= 3;
@@ -904,11 +1486,38 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
 // Adds one reference per child slot of every node created in this epoch. Leaf children of 8-bit
 // interners are first summed per value in shared memory (a handful of leaves is named by most
 // bottom branches).
+// Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
+// bottom groups), so they are summed per CTA before touching global memory: 8-bit leaves in a
+// 256-entry array indexed by value, wider leaves in an open-addressed shared table keyed by node
+// index (entries that find no slot within kLeafProbe steps go straight to global atomics).
+constexpr int kLeafTab = 4096;
+constexpr int kLeafProbe = 16;
+
+__device__ __forceinline__ void leaf_tab_add(uint32_t *tab_key, uint32_t *tab_cnt, const DevInterner &I,
+                                             uint32_t idx, uint32_t cnt) {
+    const uint32_t key = idx + 1;
+    uint32_t h = (key * 0x9E3779B1u) >> 20;  // 12 bits: kLeafTab entries
+#pragma unroll 1
+    for (int p = 0; p < kLeafProbe; ++p) {
+        uint32_t k = tab_key[h];
+        if (k == 0) k = atomicCAS(tab_key + h, 0u, key), k = k ? k : key;
+        if (k == key) {
+            atomicAdd(tab_cnt + h, cnt);
+            return;
+        }
+        h = (h + 1) & (kLeafTab - 1);
+    }
+    atomicAdd(I.refcount + idx, cnt);
+}
+
 __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I) {
     __shared__ uint32_t leaf_cnt[256];
+    __shared__ uint32_t tab_key[kLeafTab], tab_cnt[kLeafTab];
     const bool small = I.vbits == 8;
     if (small)
         for (unsigned k = threadIdx.x; k < 256; k += blockDim.x) leaf_cnt[k] = 0;
+    else
+        for (unsigned k = threadIdx.x; k < kLeafTab; k += blockDim.x) tab_key[k] = 0, tab_cnt[k] = 0;
     __syncthreads();
     const unsigned long long n = I.ctr->alloc_count;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -936,14 +1545,18 @@ __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I)
                 if (j > k && c[j] == c[k]) ++cnt;
             }
             if (seen) continue;
-            if (small && id_is_leaf(c[k]))
-                atomicAdd(&leaf_cnt[node_value(I, id_index(c[k]))], cnt);
-            else
+            if (id_is_leaf(c[k])) {
+                if (small)
+                    atomicAdd(&leaf_cnt[node_value(I, id_index(c[k]))], cnt);
+                else
+                    leaf_tab_add(tab_key, tab_cnt, I, id_index(c[k]), cnt);
+            } else {
                 atomicAdd(I.refcount + id_index(c[k]), cnt);
+            }
         }
     }
     __syncthreads();
-    if (small)
+    if (small) {
         for (unsigned v = threadIdx.x; v < 256; v += blockDim.x)
             if (leaf_cnt[v]) {
                 const uint64_t lid = I.leaf_table[v];
@@ -952,6 +1565,10 @@ __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I)
                 else
                     set_error(I, ERR_INTERNAL, 30);
             }
+    } else {
+        for (unsigned k = threadIdx.x; k < kLeafTab; k += blockDim.x)
+            if (tab_key[k] && tab_cnt[k]) atomicAdd(I.refcount + tab_key[k] - 1, tab_cnt[k]);
+    }
 }
 
 __global__ void epoch_finalize_kernel(DevInterner I) {
@@ -1024,8 +1641,27 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// Quad memo geometry for a call: slots = a power of two near a quarter of the call's quads (1 Ki to
+// 2 Mi), records = half the slots.
+static void memo_geometry(uint64_t n_chunks, int depth, uint64_t *slots, uint64_t *recs) {
+    const uint64_t quads = n_chunks << (3 * (depth - 2));
+    uint64_t sl = 1024;
+    while (sl < quads / 4 && sl < (1ull << 21)) sl <<= 1;
+    *slots = sl;
+    *recs = sl / 2;
+}
+
+size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits) {
+    if (depth < 4) return 0;
+    uint64_t sl, rc;
+    memo_geometry(n_chunks, depth, &sl, &rc);
+    const size_t stride = 16 * 4 * (size_t)(vbits / 8) + 16;
+    return sl * 8 + 256 + rc * stride + 256;
+}
+
 cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
-                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s) {
+                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s,
+                                 void *memo, bool clear_memo, uint64_t memo_chunks) {
     if (n_chunks == 0) return cudaSuccess;
     if (depth < 4 || depth > 10) return cudaErrorInvalidValue;
     OctArgs a{};
@@ -1041,6 +1677,20 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
     for (int k = 0; k <= depth - 5; ++k) {
         a.cnt_off[k] = cnts;
         cnts += (size_t)n_chunks << (3 * k);
+    }
+    if (memo) {
+        uint64_t sl, rc;
+        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, &sl, &rc);
+        char *m = static_cast<char *>(memo);
+        a.memo_slots = reinterpret_cast<unsigned long long *>(m);
+        a.memo_count = reinterpret_cast<unsigned int *>(m + sl * 8);
+        a.memo_recs = reinterpret_cast<unsigned char *>(m + sl * 8 + 256);
+        a.memo_mask = (uint32_t)(sl - 1);
+        a.memo_cap = (uint32_t)rc;
+        if (clear_memo) {
+            cudaError_t e = cudaMemsetAsync(m, 0, sl * 8 + 256, s);
+            if (e != cudaSuccess) return e;
+        }
     }
     char *base = static_cast<char *>(scratch);
     a.ids = reinterpret_cast<uint64_t *>(base);
@@ -1064,7 +1714,8 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)kOctWarps * kOctTiles * 4096 * es + (3 * kKeyCache + 256 + 2 * kOctWarps) * 8 + 64;
+    const size_t smem = (size_t)kOctWarps * kOctTiles * 4096 * es +
+                        (3 * kKeyCache + 256 + 2 * kOctWarps + 9 * kNodeCacheAlloc) * 8 + (kKeyCache + kNodeCacheAlloc) * 4 + 64;
     const uint64_t n_oct = (uint64_t)n_chunks << (3 * (depth - 4));
     auto launch = [&](auto kernel) -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <unordered_set>
 #include <vector>
@@ -35,6 +36,11 @@ struct vx_batch {
     bool has_fill = false;
     uint32_t fill = 0;
     bool has_patches = false;
+    // groups written since the last clear, in first-write order (the staging of an apply visits
+    // only these); all_touched after a dense fill, which writes every group
+    mutable std::vector<uint32_t> touched;
+    mutable bool touched_sorted = true;
+    bool all_touched = false;
 };
 
 namespace {
@@ -56,6 +62,35 @@ uint32_t morton_encode(int32_t x, int32_t y, int32_t z) {
 
 int depth_limit(uint32_t flags) { return (flags & VX_PATCH_P2) ? 11 : 7; }
 
+// Records group gi as touched (first write since the last clear).
+inline void batch_touch(vx_batch *b, uint64_t gi) {
+    if (b->all_touched || (b->set[gi] | b->clear[gi])) return;
+    if (!b->touched.empty() && b->touched.back() > gi) b->touched_sorted = false;
+    b->touched.push_back((uint32_t)gi);
+}
+
+uint64_t batch_touched_count(const vx_batch *b) {
+    if (!b->all_touched) return b->touched.size();
+    uint64_t n = 0;
+    for (uint64_t g = 0; g < b->groups; ++g) n += (b->set[g] | b->clear[g]) != 0;
+    return n;
+}
+
+// Calls f(g) for every group with a set or clear bit, in ascending group order.
+template <class F>
+void batch_for_each_touched(const vx_batch *b, F f) {
+    if (b->all_touched) {
+        for (uint64_t g = 0; g < b->groups; ++g)
+            if (b->set[g] | b->clear[g]) f(g);
+        return;
+    }
+    if (!b->touched_sorted) {
+        std::sort(b->touched.begin(), b->touched.end());
+        b->touched_sorted = true;
+    }
+    for (uint32_t g : b->touched) f((uint64_t)g);
+}
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -71,6 +106,28 @@ struct DevBuf {
     }
     void release() {
         if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+constexpr int kCopyPieces = 4;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = std::max(n + n / 4, (size_t)1 << 20);
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
         p = nullptr;
         bytes = 0;
     }
@@ -105,6 +162,8 @@ struct vx_interner {
     DevInterner dev{};
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;       // host-to-device copies that overlap device work
+    cudaEvent_t copy_events[kCopyPieces] = {};
     int num_sms = 148;
     int apply_threads = 256;       // launch shape of the batched-apply kernels (autotuned)
     int apply_blocks_per_sm = 8;
@@ -117,6 +176,7 @@ struct vx_interner {
     // device scratch
     DevBuf ws;
     DevBuf staging;  // host-memory arguments copied to the device
+    HostBuf pinned;  // pinned host memory for staging batched applies
     uint32_t *frontier = nullptr;  // 2 * capacity u32 (the single-thread queue aliases it under P3)
     uint64_t *seq_queue = nullptr;
     uint64_t seq_queue_cap = 0;
@@ -390,60 +450,95 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
     std::stable_sort(items.begin(), items.end(),
                      [&](const Item &a, const Item &b) { return it->tree_depth[a.tree] > it->tree_depth[b.tree]; });
     int max_depth = 0;
-    uint64_t R = 0;
-    for (auto &x : items) {
+    std::vector<uint64_t> off(n + 1, 0);  // first record of each item
+    for (uint32_t i = 0; i < n; ++i) {
+        const Item &x = items[i];
         max_depth = std::max(max_depth, (int)it->tree_depth[x.tree]);
-        const vx_batch *b = x.batch;
-        if (!b->has_patches) continue;
-        for (uint64_t g = 0; g < b->groups; ++g) R += (b->set[g] | b->clear[g]) != 0;
+        off[i + 1] = off[i] + (x.batch->has_patches ? batch_touched_count(x.batch) : 0);
     }
+    const uint64_t R = off[n];
     for (auto &x : items)
         if (x.batch->has_patches && it->tree_depth[x.tree] < 2)
             return set_err(it, VX_E_REF_PANIC, "batch apply needs max_depth >= 2 (usize underflow in the reference)");
     if (R >= 0xFFFFFFF0ull) return set_err(it, VX_E_UNSUPPORTED, "too many touched groups in one call");
-    bool any_clear = false;
 
-    // host staging (pinned would be faster; these buffers are O(records))
-    std::vector<uint32_t> it_tree(n), it_fill(n), rec_item(R), rec_group(R);
-    std::vector<uint8_t> it_depth(n), it_flags(n), rec_set(R), rec_clear(R);
-    std::vector<uint16_t> rec_vals(R * 8);
-    uint64_t r = 0;
+    // host staging in pinned memory: items, then the touched groups of every batch as records
+    // sorted by (item, group), filled by several threads over balanced record ranges
+    VX_CUDA(it->pinned.reserve(Carve::need({n * 4, n * 4, n, n, R * 4, R * 4, R, R, R * 16})));
+    Carve hc(it->pinned.p);
+    uint32_t *it_tree = hc.take<uint32_t>(n), *it_fill = hc.take<uint32_t>(n);
+    uint8_t *it_depth = hc.take<uint8_t>(n), *it_flags = hc.take<uint8_t>(n);
+    uint32_t *rec_item = hc.take<uint32_t>(R), *rec_group = hc.take<uint32_t>(R);
+    uint8_t *rec_set = hc.take<uint8_t>(R), *rec_clear = hc.take<uint8_t>(R);
+    uint16_t *rec_vals = hc.take<uint16_t>(R * 8);
     for (uint32_t i = 0; i < n; ++i) {
         const vx_batch *b = items[i].batch;
         it_tree[i] = items[i].tree;
         it_depth[i] = it->tree_depth[items[i].tree];
         it_flags[i] = (b->has_fill ? 1 : 0) | (b->has_patches ? 2 : 0);
         it_fill[i] = b->fill;
-        if (!b->has_patches) continue;
-        for (uint64_t g = 0; g < b->groups; ++g) {
-            if (!(b->set[g] | b->clear[g])) continue;
-            rec_item[r] = i;
-            rec_group[r] = (uint32_t)g;
-            rec_set[r] = b->set[g];
-            rec_clear[r] = b->clear[g];
-            any_clear |= b->clear[g] != 0;
-            for (int k = 0; k < 8; ++k)
-                rec_vals[8 * r + k] = b->vbits == 8 ? b->vals[8 * g + k]
-                                                    : reinterpret_cast<const uint16_t *>(b->vals.data())[8 * g + k];
-            ++r;
-        }
     }
+    auto fill_items = [&](uint32_t i0, uint32_t i1, bool *clear_seen) {
+        bool cs = false;
+        for (uint32_t i = i0; i < i1; ++i) {
+            const vx_batch *b = items[i].batch;
+            if (!b->has_patches) continue;
+            uint64_t r = off[i];
+            const bool wide = b->vbits != 8;
+            batch_for_each_touched(b, [&](uint64_t g) {
+                rec_item[r] = i;
+                rec_group[r] = (uint32_t)g;
+                rec_set[r] = b->set[g];
+                rec_clear[r] = b->clear[g];
+                cs |= b->clear[g] != 0;
+                if (wide) {
+                    std::memcpy(rec_vals + 8 * r, b->vals.data() + 16 * g, 16);
+                } else {
+                    for (int k = 0; k < 8; ++k) rec_vals[8 * r + k] = b->vals[8 * g + k];
+                }
+                ++r;
+            });
+        }
+        *clear_seen = cs;
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::max(1u, std::min(nt, 16u));
+    if (R < (1u << 16)) nt = 1;
+    std::vector<uint32_t> bounds(nt + 1, n);
+    bounds[0] = 0;
+    for (unsigned t = 1; t < nt; ++t)  // first item whose records start at or after t/nt of R
+        bounds[t] = (uint32_t)(std::lower_bound(off.begin(), off.end() - 1, R * t / nt) - off.begin());
+    std::vector<char> clears(nt, 0);
+    if (nt == 1) {
+        bool c0 = false;
+        fill_items(0, n, &c0);
+        clears[0] = c0;
+    } else {
+        std::vector<std::thread> pool;
+        bool cflags[16] = {false};
+        for (unsigned t = 0; t < nt; ++t)
+            pool.emplace_back([&, t] { fill_items(bounds[t], std::max(bounds[t], bounds[t + 1]), &cflags[t]); });
+        for (auto &th : pool) th.join();
+        for (unsigned t = 0; t < nt; ++t) clears[t] = cflags[t];
+    }
+    bool any_clear = false;
+    for (char c : clears) any_clear |= c != 0;
 
     ApplyArgs a{};
     int st0 = carve_apply(it, n, R, true, a);
     if (st0 != VX_OK) return st0;
     a.max_depth = max_depth;
     cudaStream_t s = it->stream;
-    VX_CUDA(cudaMemcpyAsync((void *)a.it_tree, it_tree.data(), n * 4, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync((void *)a.it_depth, it_depth.data(), n, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync((void *)a.it_flags, it_flags.data(), n, cudaMemcpyHostToDevice, s));
-    VX_CUDA(cudaMemcpyAsync((void *)a.it_fill, it_fill.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_tree, it_tree, n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_depth, it_depth, n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_flags, it_flags, n, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync((void *)a.it_fill, it_fill, n * 4, cudaMemcpyHostToDevice, s));
     if (R) {
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_item, rec_item.data(), R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_group, rec_group.data(), R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_set, rec_set.data(), R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear.data(), R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals.data(), R * 16, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_item, rec_item, R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_group, rec_group, R * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_set, rec_set, R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear, R, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals, R * 16, cudaMemcpyHostToDevice, s));
     }
     int st1 = apply_sequence(it, a, any_clear && (it->flags & VX_PATCH_P4));
     if (st1 != VX_OK) return st1;
@@ -460,6 +555,9 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
 
 // Batch filled from a dense [y][z][x] grid by just_set (batch.rs:145-172), in y, z, x order.
 void batch_from_dense(vx_batch *b, const void *grid) {
+    b->all_touched = true;  // every group is written
+    b->touched.clear();
+    b->touched_sorted = true;
     const int32_t n = 1 << b->depth;
     const int vb = b->vbits / 8;
     const uint8_t *g8 = static_cast<const uint8_t *>(grid);
@@ -497,9 +595,11 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
                int depth) {
     cudaStream_t s = it->stream;
     if (VX_DENSE_OCTANTS && depth >= 4) {
-        VX_CUDA(it->ws.reserve(dense_octant_scratch_bytes(n, depth)));
+        const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
         Phase ph(it, VX_PROF_DENSE);
-        VX_CUDA(launch_dense_octants(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s));
+        VX_CUDA(launch_dense_octants(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
+                                     static_cast<char *>(it->ws.p) + sb));
     } else if (depth > 5) {
         // 32^3 blocks, then one launch per level above them
         DenseArgs a{};
@@ -682,6 +782,7 @@ int vx_interner_destroy(vx_interner *it) {
         if (p) cudaFree(p);
     it->ws.release();
     it->staging.release();
+    it->pinned.release();
     if (it->h_ctr) cudaFreeHost(it->h_ctr);
     if (it->h_status) cudaFreeHost(it->h_status);
     if (it->h_live) cudaFreeHost(it->h_live);
@@ -690,6 +791,9 @@ int vx_interner_destroy(vx_interner *it) {
         cudaEventDestroy(m.second.second);
     }
     for (cudaEvent_t e : it->event_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : it->copy_events)
+        if (e) cudaEventDestroy(e);
+    if (it->copy_stream) cudaStreamDestroy(it->copy_stream);
     if (it->own_stream) cudaStreamDestroy(it->own_stream);
     delete it;
     return VX_OK;
@@ -960,6 +1064,7 @@ int vx_batch_set(vx_batch *b, int32_t x, int32_t y, int32_t z, uint32_t value) {
     const uint64_t gi = full >> 3;
     const unsigned idx = full & 7;
     const uint8_t bit = (uint8_t)(1u << idx);
+    batch_touch(b, gi);
     if (value) {
         b->set[gi] |= bit;
         b->clear[gi] &= (uint8_t)~bit;
@@ -986,9 +1091,21 @@ int vx_batch_set_many(vx_batch *b, uint64_t n, const int32_t *xyz, const uint32_
 
 int vx_batch_clear(vx_batch *b) {
     if (!b) return VX_E_INVALID_ARG;
-    std::fill(b->set.begin(), b->set.end(), 0);
-    std::fill(b->clear.begin(), b->clear.end(), 0);
-    std::fill(b->vals.begin(), b->vals.end(), 0);
+    if (b->all_touched) {
+        std::fill(b->set.begin(), b->set.end(), 0);
+        std::fill(b->clear.begin(), b->clear.end(), 0);
+        std::fill(b->vals.begin(), b->vals.end(), 0);
+    } else {
+        const size_t vb = b->vbits / 8;
+        for (uint32_t g : b->touched) {
+            b->set[g] = 0;
+            b->clear[g] = 0;
+            std::memset(b->vals.data() + (size_t)g * 8 * vb, 0, 8 * vb);
+        }
+    }
+    b->touched.clear();
+    b->touched_sorted = true;
+    b->all_touched = false;
     b->has_fill = false;
     b->fill = 0;
     b->has_patches = false;
@@ -1011,9 +1128,7 @@ int vx_batch_set_dense(vx_batch *b, const void *grid) {
 
 int vx_batch_size(const vx_batch *b, uint64_t *out) {
     if (!b || !out) return VX_E_INVALID_ARG;
-    uint64_t n = 0;
-    for (uint64_t g = 0; g < b->groups; ++g) n += (b->set[g] | b->clear[g]) != 0;
-    *out = n;
+    *out = batch_touched_count(b);
     return VX_OK;
 }
 
@@ -1153,6 +1268,54 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
             else
                 std::copy(ch.begin(), ch.end(), changed);
         }
+        return st;
+    }
+    if (mem == VX_MEM_HOST && VX_DENSE_OCTANTS && d >= 4 && n >= 2 * kCopyPieces) {
+        // pipelined: the grids go over in kCopyPieces pieces on a copy stream; piece k is built on
+        // the interner's stream as soon as its copy lands, while piece k+1 is still in flight
+        if (!it->copy_stream) {
+            VX_CUDA(cudaStreamCreateWithFlags(&it->copy_stream, cudaStreamNonBlocking));
+            for (auto &e : it->copy_events) VX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        VX_CUDA(it->staging.reserve(Carve::need({n * 4, per * n, n})));
+        Carve c(it->staging.p);
+        uint32_t *dt = c.take<uint32_t>(n);
+        uint8_t *dg = c.take<uint8_t>(per * n);
+        uint8_t *dc = c.take<uint8_t>(n);
+        const size_t sb = (dense_octant_scratch_bytes(n, d) + 255) & ~(size_t)255;
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, d, it->vbits)));
+        char *memo = static_cast<char *>(it->ws.p) + sb;
+        cudaStream_t s = it->stream;
+        {
+            Phase ph(it, VX_PROF_COPY);
+            VX_CUDA(cudaMemcpyAsync(dt, htrees.data(), n * 4, cudaMemcpyHostToDevice, s));
+            VX_CUDA(cudaMemsetAsync(dc, 0, n, s));
+            // the copy stream must not overwrite grids a previous call's kernels still read
+            VX_CUDA(cudaEventRecord(it->copy_events[0], s));
+            VX_CUDA(cudaStreamWaitEvent(it->copy_stream, it->copy_events[0], 0));
+        }
+        const uint32_t per_piece = (n + kCopyPieces - 1) / kCopyPieces;
+        for (int k = 0; k < kCopyPieces; ++k) {
+            const uint32_t c0 = k * per_piece, c1 = std::min(n, c0 + per_piece);
+            if (c0 >= c1) break;
+            VX_CUDA(cudaMemcpyAsync(dg + per * c0, static_cast<const uint8_t *>(grids) + per * c0, per * (c1 - c0),
+                                    cudaMemcpyHostToDevice, it->copy_stream));
+            VX_CUDA(cudaEventRecord(it->copy_events[k], it->copy_stream));
+            VX_CUDA(cudaStreamWaitEvent(s, it->copy_events[k], 0));
+            Phase ph(it, VX_PROF_DENSE);
+            VX_CUDA(launch_dense_octants(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p, it->num_sms, s,
+                                         memo, k == 0, n));
+        }
+        {
+            Phase ph(it, VX_PROF_REFCOUNT);
+            VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
+        }
+        if (changed) {
+            Phase ph(it, VX_PROF_COPY);
+            VX_CUDA(cudaMemcpyAsync(changed, dc, n, cudaMemcpyDeviceToHost, s));
+        }
+        const int st = sync_and_check(it);
+        for (vx_tree t : htrees) it->tree_maybe_nonempty[t] = 1;
         return st;
     }
     const uint32_t *d_trees;

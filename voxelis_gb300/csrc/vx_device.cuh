@@ -113,6 +113,21 @@ __device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
     return v;
 }
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) { return __ldcg((const unsigned long long *)p); }
+// Load of a hash-table slot while probing. Publishers write the node record, fence, then store the
+// slot; everything a prober reads after a slot (record words) is read from L2 (ld.global.cg) at an
+// address computed from the slot value. VX_PROBE_ACQUIRE=1 makes the slot load an acquire instead.
+#ifndef VX_PROBE_ACQUIRE
+#define VX_PROBE_ACQUIRE 1
+#endif
+__device__ __forceinline__ uint64_t ld_probe(const uint64_t *p) {
+    uint64_t v;
+#if VX_PROBE_ACQUIRE
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+#else
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+#endif
+    return v;
+}
 
 __device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
     unsigned int old = atomicOr(&I.ctr->error, bit);
@@ -250,7 +265,7 @@ static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner
         bool claimed = false;
         bool waiting = false;
         if (!done) {
-            uint64_t s = ld_acquire(I.table + pos);
+            uint64_t s = ld_probe(I.table + pos);
             if (s == SLOT_EMPTY) {
                 uint64_t prev = atomicCAS((unsigned long long *)(I.table + pos), SLOT_EMPTY, make_slot(tag, IDX_BUSY));
                 if (prev == SLOT_EMPTY)

@@ -29,9 +29,15 @@ cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int nu
 // Fused dense construction for chunk depths 4..10: warps take 16^3 octants (TMA tensor copies),
 // levels above octants are reduced by the last-arriving warp of each parent. `scratch` must hold
 // dense_octant_scratch_bytes(n, depth) bytes; it is cleared inside.
+// `memo` (optional, dense_octant_memo_bytes) holds the quad memo; it is cleared inside unless
+// clear_memo is false (later pieces of one build share the memo of the first: no release runs in
+// between, so every node it names is still alive). memo_chunks (0: n_chunks) sizes the memo and must
+// be the same for every piece that shares it.
 size_t dense_octant_scratch_bytes(uint64_t n_chunks, int depth);
+size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits);
 cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
-                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s);
+                                 int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s,
+                                 void *memo = nullptr, bool clear_memo = true, uint64_t memo_chunks = 0);
 // One level of fresh parents above the blocks: n_parents = n_chunks * 8^k.
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
                                uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
