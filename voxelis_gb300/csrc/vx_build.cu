@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
 // CTA already interned; only misses go to the global branch table, deduplicated within the warp.
 
 #ifndef VX_KEY_CACHE
-#define VX_KEY_CACHE 512
+#define VX_KEY_CACHE 128
 #endif
 #ifndef VX_OCT_TILES
 #define VX_OCT_TILES 1
@@ -765,7 +765,7 @@ __device__ __forceinline__ void reduce_tile16(const DevInterner &I, const T *til
 // reduce_tile16 and the global branch table.
 
 #ifndef VX_NODE_CACHE
-#define VX_NODE_CACHE 256
+#define VX_NODE_CACHE 64
 #endif
 constexpr int kNodeCache = VX_NODE_CACHE;  // entries (power of two)
 constexpr int kNodeCacheAlloc = VX_TILE_V2 ? kNodeCache : 0;  // entries with shared memory behind them
@@ -1059,11 +1059,16 @@ struct QuadWord {
     using type = typename std::conditional<sizeof(T) == 1, uint32_t, uint64_t>::type;
 };
 
-template <class T>
+// Row r = yy * 4 + zz of the quad at qbase in a tile of side S ([y][z][x], S voxels per row).
+template <class T, int S>
+__device__ __forceinline__ const typename QuadWord<T>::type *quad_row(const T *qbase, int r) {
+    return reinterpret_cast<const typename QuadWord<T>::type *>(qbase + ((r >> 2) * S + (r & 3)) * S);
+}
+
+template <class T, int S = 16>
 __device__ __forceinline__ void quad_rows(const T *qbase, typename QuadWord<T>::type w[16]) {
-    using W = typename QuadWord<T>::type;
 #pragma unroll
-    for (int r = 0; r < 16; ++r) w[r] = *reinterpret_cast<const W *>(qbase + ((r >> 2) * 16 + (r & 3)) * 16);
+    for (int r = 0; r < 16; ++r) w[r] = *quad_row<T, S>(qbase, r);
 }
 
 // Record r's address; the record's content is 16 row words of 4 voxels.
@@ -1072,7 +1077,7 @@ __device__ __forceinline__ unsigned char *memo_rec(const OctArgs &a, uint32_t r)
     return a.memo_recs + (size_t)r * (16 * 4 * sizeof(T) + 16);
 }
 
-template <class T>
+template <class T, int S = 16>
 __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T *qbase, uint64_t &id, uint32_t &lod) {
     using W = typename QuadWord<T>::type;
     const unsigned char *rec = memo_rec<T>(a, r);
@@ -1082,13 +1087,10 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
     for (int k = 0; k < 4 * (int)sizeof(T); ++k) {
         const uint4 x = __ldcg(rv + k);
         if (sizeof(T) == 1) {
-            eq = eq && x.x == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k) >> 2) * 16 + ((4 * k) & 3)) * 16) &&
-                 x.y == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 1) >> 2) * 16 + ((4 * k + 1) & 3)) * 16) &&
-                 x.z == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 2) >> 2) * 16 + ((4 * k + 2) & 3)) * 16) &&
-                 x.w == *reinterpret_cast<const uint32_t *>(qbase + (((4 * k + 3) >> 2) * 16 + ((4 * k + 3) & 3)) * 16);
+            eq = eq && x.x == (uint32_t)*quad_row<T, S>(qbase, 4 * k) && x.y == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 1) &&
+                 x.z == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 2) && x.w == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 3);
         } else {
-            const W a0 = *reinterpret_cast<const W *>(qbase + (((2 * k) >> 2) * 16 + ((2 * k) & 3)) * 16);
-            const W a1 = *reinterpret_cast<const W *>(qbase + (((2 * k + 1) >> 2) * 16 + ((2 * k + 1) & 3)) * 16);
+            const W a0 = *quad_row<T, S>(qbase, 2 * k), a1 = *quad_row<T, S>(qbase, 2 * k + 1);
             eq = eq && ((uint64_t)x.x | ((uint64_t)x.y << 32)) == (uint64_t)a0 &&
                  ((uint64_t)x.z | ((uint64_t)x.w << 32)) == (uint64_t)a1;
         }
@@ -1100,7 +1102,7 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
     return true;
 }
 
-template <class T>
+template <class T, int S = 16>
 __device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint32_t h2, const T *qbase, uint64_t id,
                                             uint32_t lod) {
     using W = typename QuadWord<T>::type;
@@ -1109,7 +1111,7 @@ __device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint3
     unsigned char *rec = memo_rec<T>(a, r);
     W *dst = reinterpret_cast<W *>(rec);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) dst[k] = *reinterpret_cast<const W *>(qbase + ((k >> 2) * 16 + (k & 3)) * 16);
+    for (int k = 0; k < 16; ++k) dst[k] = *quad_row<T, S>(qbase, k);
     *reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T)) = make_uint4((uint32_t)id, (uint32_t)(id >> 32), lod, 0u);
     __threadfence();
     uint32_t slot = h1 & a.memo_mask;
@@ -1121,13 +1123,80 @@ __device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint3
     }
 }
 
+// The 8 bottom groups of one quad (4^3 voxels at qbase in a tile of side S) reduced as Phase 1 and
+// Phase 2 do, then the quad's own node, which a non-uniform quad always is a branch. Warp-collective:
+// every lane calls it; lanes with active == false only take part in the ballots.
+template <class T, int S>
+__device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache &C, uint64_t *leaf_cache,
+                                            const T *qbase, bool active, uint64_t &qid, uint32_t &qval) {
+    const unsigned lane = threadIdx.x & 31u;
+    const bool wide = sizeof(T) == 2;
+    uint64_t c3[8];
+    uint32_t cv3[8];
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
+        const T *g = qbase + ((2 * gy) * S + 2 * gz) * S + 2 * gx;
+        uint64_t lo = 0, hi = 0;
+        if (sizeof(T) == 1) {
+            const uint32_t p0 = *reinterpret_cast<const uint16_t *>(g);
+            const uint32_t p1 = *reinterpret_cast<const uint16_t *>(g + S * S);
+            const uint32_t p2 = *reinterpret_cast<const uint16_t *>(g + S);
+            const uint32_t p3 = *reinterpret_cast<const uint16_t *>(g + S * S + S);
+            lo = (uint64_t)(p0 | (p1 << 16)) | ((uint64_t)(p2 | (p3 << 16)) << 32);
+        } else {
+            lo = (uint64_t)*reinterpret_cast<const uint32_t *>(g) |
+                 ((uint64_t)*reinterpret_cast<const uint32_t *>(g + S * S) << 32);
+            hi = (uint64_t)*reinterpret_cast<const uint32_t *>(g + S) |
+                 ((uint64_t)*reinterpret_cast<const uint32_t *>(g + S * S + S) << 32);
+        }
+        const uint32_t set = set_mask8<T>(lo, hi);
+        const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+        const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
+                                         : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
+        const bool is_branch = active && set != 0 && !(guni && set == 0xFFu);
+        uint32_t lod = 0;
+        uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
+        const bool need = is_branch && id == 0;
+        const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+        if (bm) {
+            uint32_t v[8];
+            unpack8<T>(lo, hi, v);
+            if (need) lod = calc_average8(v);
+            unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+            if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+            grp &= bm;
+            const int leader = need ? __ffs(grp) - 1 : (int)lane;
+            const bool lead = need && leader == (int)lane;
+            uint64_t c[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+            bool created;
+            uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+            nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+            if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+            if (need) id = nid;
+        }
+        if (set == 0) {
+            c3[k] = EMPTY_ID;
+            cv3[k] = 0;
+        } else if (!is_branch) {
+            c3[k] = active ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
+            cv3[k] = gv0;
+        } else {
+            c3[k] = id;
+            cv3[k] = lod;
+        }
+    }
+    reduce_parent(I, active, c3, cv3, qid, qval);
+}
+
 template <class T>
 __device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const OctArgs &a, const T *tile,
                                                  const KeyCache &C, const NodeCache &N, uint64_t *leaf_cache,
                                                  uint64_t &oct_id, uint32_t &oct_val) {
     using W = typename QuadWord<T>::type;
     const unsigned lane = threadIdx.x & 31u;
-    const bool wide = sizeof(T) == 2;
     const bool memo = a.memo_slots != nullptr;
     const T *qb[2];
     bool uni[2];
@@ -1200,71 +1269,13 @@ __device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const Oct
     for (int q = 0; q < 2; ++q) {
         const bool active = !uni[q] && qid[q] == 0;
         if (__any_sync(0xFFFFFFFFu, active)) {
-            const T *qbase = qb[q];
-            uint64_t c3[8];
-            uint32_t cv3[8];
-#pragma unroll 1
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
-                const T *g = qbase + ((2 * gy) * 16 + 2 * gz) * 16 + 2 * gx;
-                uint64_t lo = 0, hi = 0;
-                if (sizeof(T) == 1) {
-                    const uint32_t p0 = *reinterpret_cast<const uint16_t *>(g);
-                    const uint32_t p1 = *reinterpret_cast<const uint16_t *>(g + 256);
-                    const uint32_t p2 = *reinterpret_cast<const uint16_t *>(g + 16);
-                    const uint32_t p3 = *reinterpret_cast<const uint16_t *>(g + 272);
-                    lo = (uint64_t)(p0 | (p1 << 16)) | ((uint64_t)(p2 | (p3 << 16)) << 32);
-                } else {
-                    lo = (uint64_t)*reinterpret_cast<const uint32_t *>(g) |
-                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 256) << 32);
-                    hi = (uint64_t)*reinterpret_cast<const uint32_t *>(g + 16) |
-                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 272) << 32);
-                }
-                const uint32_t set = set_mask8<T>(lo, hi);
-                const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
-                const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
-                                                 : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
-                const bool is_branch = active && set != 0 && !(guni && set == 0xFFu);
-                uint32_t lod = 0;
-                uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
-                const bool need = is_branch && id == 0;
-                const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
-                if (bm) {
-                    uint32_t v[8];
-                    unpack8<T>(lo, hi, v);
-                    if (need) lod = calc_average8(v);
-                    unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
-                    if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
-                    grp &= bm;
-                    const int leader = need ? __ffs(grp) - 1 : (int)lane;
-                    const bool lead = need && leader == (int)lane;
-                    uint64_t c[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
-                    bool created;
-                    uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
-                    nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-                    if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
-                    if (need) id = nid;
-                }
-                if (set == 0) {
-                    c3[k] = EMPTY_ID;
-                    cv3[k] = 0;
-                } else if (!is_branch) {
-                    c3[k] = active ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
-                    cv3[k] = gv0;
-                } else {
-                    c3[k] = id;
-                    cv3[k] = lod;
-                }
-            }
             uint64_t pid;
             uint32_t pval;
-            reduce_parent(I, active, c3, cv3, pid, pval);
+            quad_groups<T, 16>(I, C, leaf_cache, qb[q], active, pid, pval);
             if (active) {
                 qid[q] = pid;
                 qval[q] = pval;
-                if (memo && pid != INVALID_ID) memo_insert<T>(a, h1[q], h2[q], qbase, pid, pval);
+                if (memo && pid != INVALID_ID) memo_insert<T>(a, h1[q], h2[q], qb[q], pid, pval);
             }
         }
         l3[q] = qid[q];
@@ -1434,6 +1445,281 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
             q >>= 3;
         }
         if (kOctTiles == 2) buf ^= 1;
+    }
+}
+
+// ---- 32^3 blocks, one CTA each, level-synchronous phases -------------------------------------------
+//
+// For chunk depths >= 5. A CTA takes 32^3 blocks in turn (4-D TMA tensor copy of the block into one
+// shared tile, mbarrier completion, bounded wait). Phase 1: each of the 256 threads takes two of the
+// block's 512 quads (4^3), tests uniformity on row words, and probes the device-wide quad memo, so
+// all 512 probes of the block are in flight together; memo misses run the bottom-group path
+// (quad_groups) warp by warp and are inserted. Quad results go to shared memory in Morton order and
+// the tile is released: the next block's copy starts while the upper levels run. Phase 2: 64 threads
+// reduce the 8^3 nodes; phase 3: warp 0 reduces the 8 16^3 nodes and the block root (shared cache of
+// parents by child ids first, then the global table), and climbs above the block with per-parent
+// arrival counters like the octant kernel.
+#ifndef VX_DENSE_CTA32
+#define VX_DENSE_CTA32 1
+#endif
+constexpr int kCtaThreads = 256;
+
+template <class T>
+struct Cta32Smem {
+    static constexpr size_t tile = 32768 * sizeof(T);
+    static constexpr size_t qid = tile;                            // 512 u64: quad nodes, Morton order
+    static constexpr size_t kc = qid + 512 * 8;                    // 3 * kKeyCache u64
+    static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;  // 256 u64
+    static constexpr size_t nc = leaf + 256 * 8;                    // 9 * kNodeCache u64
+    static constexpr size_t bar = nc + 9 * (size_t)kNodeCache * 8;  // 2 u64
+    static constexpr size_t lid = bar + 16;                         // 72 u64: level-2 nodes, then level 1
+    static constexpr size_t qval = lid + 72 * 8;                    // 512 u32
+    static constexpr size_t lval = qval + 512 * 4;                  // 72 u32
+    static constexpr size_t kcval = lval + 72 * 4;                  // kKeyCache u32
+    static constexpr size_t ncmeta = kcval + (size_t)kKeyCache * 4;  // kNodeCache u32
+    static constexpr size_t total = ncmeta + (size_t)kNodeCache * 4;
+};
+
+__device__ __forceinline__ uint32_t spread3b(uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4); }
+
+__device__ __forceinline__ void tma_load_block32(void *dst, const CUtensorMap *tmap, int x, int z, int y, int c,
+                                                 uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(z), "r"(y), "r"(c), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <class T>
+__global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I, OctArgs a,
+                                                                 const __grid_constant__ CUtensorMap tmap) {
+    using L = Cta32Smem<T>;
+    using W = typename QuadWord<T>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    T *tile = reinterpret_cast<T *>(smem);
+    uint64_t *qid_s = reinterpret_cast<uint64_t *>(smem + L::qid);
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + L::kc);
+    uint64_t *leaf_cache = reinterpret_cast<uint64_t *>(smem + L::leaf);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar);
+    uint64_t *lid = reinterpret_cast<uint64_t *>(smem + L::lid);
+    uint32_t *qval_s = reinterpret_cast<uint32_t *>(smem + L::qval);
+    uint32_t *lval = reinterpret_cast<uint32_t *>(smem + L::lval);
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
+    uint64_t *nc = reinterpret_cast<uint64_t *>(smem + L::nc);
+    NodeCache N{nc, nc + 8 * kNodeCache, reinterpret_cast<uint32_t *>(smem + L::ncmeta)};
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    for (unsigned k = tid; k < kNodeCache; k += blockDim.x) N.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int d = a.depth;
+    const int bb = 3 * (d - 5);  // block-index bits inside a chunk
+    const uint64_t n_blk = (uint64_t)a.n_chunks << bb;
+    const bool memo = a.memo_slots != nullptr;
+    auto issue = [&](uint64_t b) {
+        const uint32_t c = (uint32_t)(b >> bb);
+        const uint32_t q = (uint32_t)(b & ((1ull << bb) - 1));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bar, (uint32_t)L::tile);
+        tma_load_block32(tile, &tmap, (int)(compact3(q) * 32), (int)(compact3(q >> 2) * 32),
+                         (int)(compact3(q >> 1) * 32), (int)c, bar);
+    };
+    uint32_t phase = 0;
+    uint64_t blk = blockIdx.x;
+    if (tid == 0 && blk < n_blk) issue(blk);
+    for (; blk < n_blk; blk += gridDim.x) {
+        const uint64_t nxt = blk + gridDim.x;
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bar, phase))) break;
+        if (__syncthreads_or(!ok)) {  // give up together; drain the copy first
+            if (tid == 0) set_error(I, ERR_TIMEOUT, 27);
+            for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bar, phase); ++spin) {
+            }
+            return;
+        }
+        phase ^= 1u;
+        const uint32_t c = (uint32_t)(blk >> bb);
+        uint64_t q = blk & ((1ull << bb) - 1);
+        const uint32_t tree = a.trees[c];
+        if (tree >= I.tree_cap || I.depths[tree] != d) {  // the same answer in every thread
+            if (tid == 0) {
+                set_error(I, ERR_INVALID, 28);
+                if (nxt < n_blk) issue(nxt);
+            }
+            __syncthreads();
+            continue;
+        }
+
+        // ---- phase 1: quads (qx = lane & 7, qz = lane >> 3 (+4), qy = warp) ----
+        const T *qb[2];
+        uint32_t qm[2], h1[2], h2[2];
+        bool uni[2];
+        uint64_t qidv[2];
+        uint32_t qvalv[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p, qy = warp;
+            qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
+            qb[p] = tile + ((4 * qy) * 32 + 4 * qz) * 32 + 4 * qx;
+            W w[16];
+            quad_rows<T, 32>(qb[p], w);
+            const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
+            const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
+            bool u = true;
+            uint32_t x = 0x9E3779B9u, y = 0x7F4A7C15u;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                u = u && w[r] == splat;
+                x = x * 0x01000193u + (uint32_t)w[r];
+                y = (y ^ (uint32_t)w[r]) * 0x85EBCA6Bu;
+                if (sizeof(T) == 2) {
+                    x = x * 0x01000193u + (uint32_t)((uint64_t)w[r] >> 32);
+                    y = (y ^ (uint32_t)((uint64_t)w[r] >> 32)) * 0x85EBCA6Bu;
+                }
+            }
+            x ^= x >> 15;
+            x *= 0x2C1B3C6Du;
+            x ^= x >> 12;
+            y ^= y >> 16;
+            uni[p] = u;
+            h1[p] = x;
+            h2[p] = y;
+            qidv[p] = 0;
+            qvalv[p] = v0;
+            if (u) qidv[p] = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
+        }
+        {  // memo probes, both quads in flight
+            bool look[2];
+            uint32_t slot[2];
+            unsigned long long sv[2];
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                look[p] = memo && !uni[p];
+                slot[p] = h1[p] & a.memo_mask;
+                sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
+            }
+#pragma unroll 1
+            for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
+#pragma unroll
+                for (int p = 0; p < 2; ++p) {
+                    if (!look[p]) continue;
+                    if (sv[p] == 0ull) {
+                        look[p] = false;
+                    } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
+                               memo_match<T, 32>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
+                        look[p] = false;
+                    } else if (step == 3) {
+                        look[p] = false;
+                    } else {
+                        slot[p] = (slot[p] + 1) & a.memo_mask;
+                        sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
+                    }
+                }
+            }
+        }
+#pragma unroll 1
+        for (int p = 0; p < 2; ++p) {
+            const bool active = !uni[p] && qidv[p] == 0;
+            if (__any_sync(0xFFFFFFFFu, active)) {
+                uint64_t pid;
+                uint32_t pval;
+                quad_groups<T, 32>(I, C, leaf_cache, qb[p], active, pid, pval);
+                if (active) {
+                    qidv[p] = pid;
+                    qvalv[p] = pval;
+                    if (memo && pid != INVALID_ID) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
+                }
+            }
+            qid_s[qm[p]] = qidv[p];
+            qval_s[qm[p]] = qvalv[p];
+        }
+        __syncthreads();
+        if (tid == 0 && nxt < n_blk) issue(nxt);  // the tile is free: the next block's copy overlaps phases 2-3
+
+        // ---- phase 2: the 64 nodes of 8^3 voxels ----
+        if (warp < 2) {
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = qid_s[8 * tid + k];
+                cv[k] = qval_s[8 * tid + k];
+            }
+            uint64_t o;
+            uint32_t ov;
+            reduce_parent_cached(I, N, true, ch, cv, o, ov);
+            lid[tid] = o;
+            lval[tid] = ov;
+        }
+        __syncthreads();
+        // ---- phase 3 (warp 0): the 8 nodes of 16^3 voxels, the block root, then the climb ----
+        if (warp == 0) {
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = lane < 8 ? lid[8 * lane + k] : 0ull;
+                cv[k] = lane < 8 ? lval[8 * lane + k] : 0u;
+            }
+            uint64_t o1;
+            uint32_t v1;
+            reduce_parent_cached(I, N, lane < 8, ch, cv, o1, v1);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = __shfl_sync(0xFFFFFFFFu, o1, k);
+                cv[k] = __shfl_sync(0xFFFFFFFFu, v1, k);
+            }
+            uint64_t node;
+            uint32_t val;
+            reduce_parent_cached(I, N, lane == 0, ch, cv, node, val);
+            node = __shfl_sync(0xFFFFFFFFu, node, 0);
+            val = __shfl_sync(0xFFFFFFFFu, val, 0);
+            for (int k = d - 5;; --k) {
+                if (k == 0) {
+                    if (lane == 0) {
+                        if (node != EMPTY_ID) {
+                            I.roots[tree] = node;
+                            atomicAdd(I.refcount + id_index(node), 1u);
+                        }
+                        if (a.changed) a.changed[c] = node != EMPTY_ID;
+                    }
+                    break;
+                }
+                const uint64_t gi = a.lvl_off[k] + ((uint64_t)c << (3 * k)) + q;
+                if (lane == 0) {
+                    a.ids[gi] = node;
+                    a.vals[gi] = val;
+                }
+                __threadfence();
+                uint32_t arrived = 0;
+                if (lane == 0)
+                    arrived = atomicAdd(a.cnt + a.cnt_off[k - 1] + ((uint64_t)c << (3 * (k - 1))) + (q >> 3), 1u);
+                arrived = __shfl_sync(0xFFFFFFFFu, arrived, 0);
+                if (arrived != 7) break;
+                __threadfence();
+                const uint64_t sb = a.lvl_off[k] + ((uint64_t)c << (3 * k)) + (q & ~7ull);
+                const uint64_t sid = lane < 8 ? ld_cg(a.ids + sb + lane) : 0ull;
+                const uint32_t sval = lane < 8 ? __ldcg(a.vals + sb + lane) : 0u;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    ch[j] = __shfl_sync(0xFFFFFFFFu, sid, j);
+                    cv[j] = __shfl_sync(0xFFFFFFFFu, sval, j);
+                }
+                reduce_parent_cached(I, N, lane == 0, ch, cv, node, val);
+                node = __shfl_sync(0xFFFFFFFFu, node, 0);
+                val = __shfl_sync(0xFFFFFFFFu, val, 0);
+                q >>= 3;
+            }
+        }
+        __syncthreads();  // shared quad and level arrays are reused by the next block
     }
 }
 
@@ -1664,17 +1950,19 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                                  void *memo, bool clear_memo, uint64_t memo_chunks) {
     if (n_chunks == 0) return cudaSuccess;
     if (depth < 4 || depth > 10) return cudaErrorInvalidValue;
+    const bool cta32 = VX_DENSE_CTA32 && depth >= 5;
+    const int unit = cta32 ? 5 : 4;  // log2 of the side of the unit one CTA (or warp) reduces
     OctArgs a{};
     a.trees = trees;
     a.n_chunks = n_chunks;
     a.depth = depth;
     a.changed = changed;
     size_t ids = 0, cnts = 0;
-    for (int k = 1; k <= depth - 4; ++k) {
+    for (int k = 1; k <= depth - unit; ++k) {
         a.lvl_off[k] = ids;
         ids += (size_t)n_chunks << (3 * k);
     }
-    for (int k = 0; k <= depth - 5; ++k) {
+    for (int k = 0; k <= depth - unit - 1; ++k) {
         a.cnt_off[k] = cnts;
         cnts += (size_t)n_chunks << (3 * k);
     }
@@ -1707,7 +1995,8 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
     CUtensorMap tmap;
     cuuint64_t dims[4] = {side, side, side, n_chunks};
     cuuint64_t strides[3] = {side * es, side * side * es, side * side * side * es};
-    cuuint32_t box[4] = {16, 16, 16, 1};
+    const cuuint32_t bs = cta32 ? 32 : 16;
+    cuuint32_t box[4] = {bs, bs, bs, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
                         const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1730,6 +2019,23 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
         kernel<<<(unsigned)grid, kThreads, smem, s>>>(I, a, tmap);
         return cudaGetLastError();
     };
+    if (cta32) {
+        auto launch32 = [&](auto kernel, size_t smem32) -> cudaError_t {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+            if (e != cudaSuccess) return e;
+            int per_sm = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCtaThreads, smem32);
+            if (per_sm < 1) per_sm = 1;
+            uint64_t grid = (uint64_t)num_sms * per_sm;
+            const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
+            if (grid > need) grid = need;
+            count_launches(1);
+            kernel<<<(unsigned)grid, kCtaThreads, smem32, s>>>(I, a, tmap);
+            return cudaGetLastError();
+        };
+        if (es == 1) return launch32(dense_cta32_kernel<uint8_t>, Cta32Smem<uint8_t>::total);
+        return launch32(dense_cta32_kernel<uint16_t>, Cta32Smem<uint16_t>::total);
+    }
     if (es == 1) return launch(dense_octants_kernel<uint8_t>);
     return launch(dense_octants_kernel<uint16_t>);
 }
