@@ -853,7 +853,7 @@ __device__ __forceinline__ void reduce_parent_cached(const DevInterner &I, const
     if (__any_sync(0xFFFFFFFFu, need)) {
         if (need) lod = calc_average8(cv);
         bool created;
-        const uint64_t nid = warp_intern_branch(I, need, c, types, mask, lod, &created);
+        const uint64_t nid = warp_intern_branch_inl(I, need, c, types, mask, lod, &created);
         if (need) {
             id = nid;
             if (nid != INVALID_ID) nc_insert(N, c, 1u, nid, lod);
@@ -1723,6 +1723,182 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
     }
 }
 
+// ---- quads of 32^3 blocks, then one pass per level above them -------------------------------------
+//
+// The upper levels of a block are a chain of dependent probes (8^3 nodes, then 16^3, then the block
+// root), which leaves most of a CTA idle when one CTA walks it per block. Here the quad kernel only
+// reduces quads (phase 1 of dense_cta32_kernel: uniformity on row words, the device-wide quad memo,
+// the bottom-group path on misses) and writes them to global memory in per-chunk Morton order; every
+// level above is then one fresh_level_kernel pass over all chunks, one parent per thread, so the
+// probes of a whole level are in flight together. Tiles are double-buffered for 8-bit voxels: the
+// copy of block i+2 is issued when block i is done.
+template <class T>
+struct QuadSmem {
+    static constexpr int tiles = sizeof(T) == 1 ? 2 : 1;
+    static constexpr size_t tile = 32768 * sizeof(T);
+    static constexpr size_t kc = tiles * tile;                       // 3 * kKeyCache u64
+    static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;    // 256 u64
+    static constexpr size_t bar = leaf + 256 * 8;                    // 2 u64
+    static constexpr size_t kcval = bar + 16;                        // kKeyCache u32
+    static constexpr size_t total = kcval + (size_t)kKeyCache * 4;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kCtaThreads) dense_quads_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
+                                                                 uint32_t *q_vals,
+                                                                 const __grid_constant__ CUtensorMap tmap) {
+    using L = QuadSmem<T>;
+    using W = typename QuadWord<T>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + L::kc);
+    uint64_t *leaf_cache = reinterpret_cast<uint64_t *>(smem + L::leaf);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar);
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    if (tid == 0) {
+        for (int b = 0; b < L::tiles; ++b) mbar_init(bars + b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int d = a.depth;
+    const int bb = 3 * (d - 5);
+    const uint64_t n_blk = (uint64_t)a.n_chunks << bb;
+    const uint64_t per_chunk = 1ull << (3 * (d - 2));  // quads per chunk
+    const bool memo = a.memo_slots != nullptr;
+    auto issue = [&](uint64_t b, int buf) {
+        const uint32_t c = (uint32_t)(b >> bb);
+        const uint32_t q = (uint32_t)(b & ((1ull << bb) - 1));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bars + buf, (uint32_t)L::tile);
+        tma_load_block32(smem + buf * L::tile, &tmap, (int)(compact3(q) * 32), (int)(compact3(q >> 2) * 32),
+                         (int)(compact3(q >> 1) * 32), (int)c, bars + buf);
+    };
+    uint32_t phases = 0;  // bit b: parity of tile b
+    if (tid == 0)
+        for (int b = 0; b < L::tiles; ++b)
+            if (blockIdx.x + (uint64_t)b * gridDim.x < n_blk) issue(blockIdx.x + (uint64_t)b * gridDim.x, b);
+    int buf = 0;
+    for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x) {
+        const T *tile = reinterpret_cast<const T *>(smem + buf * L::tile);
+        const uint32_t par = (phases >> buf) & 1u;
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bars + buf, par))) break;
+        if (__syncthreads_or(!ok)) {  // give up together; drain every copy in flight first
+            if (tid == 0) set_error(I, ERR_TIMEOUT, 29);
+            for (int b = 0; b < L::tiles; ++b)
+                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bars + b, (phases >> b) & 1u); ++spin) {
+                }
+            return;
+        }
+        phases ^= 1u << buf;
+        const uint32_t c = (uint32_t)(blk >> bb);
+        const uint64_t q = blk & ((1ull << bb) - 1);
+        const uint32_t tree = a.trees[c];
+        const bool bad = tree >= I.tree_cap || I.depths[tree] != d;  // the same answer in every thread
+        if (bad && tid == 0) set_error(I, ERR_INVALID, 31);
+        uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 9);
+        uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 9);
+        if (!bad) {
+            const T *qb[2];
+            uint32_t qm[2], h1[2], h2[2];
+            bool uni[2];
+            uint64_t qidv[2];
+            uint32_t qvalv[2];
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p, qy = warp;
+                qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
+                qb[p] = tile + ((4 * qy) * 32 + 4 * qz) * 32 + 4 * qx;
+                W w[16];
+                quad_rows<T, 32>(qb[p], w);
+                const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
+                const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
+                bool u = true;
+                uint32_t x = 0x9E3779B9u, y = 0x7F4A7C15u;
+#pragma unroll
+                for (int r = 0; r < 16; ++r) {
+                    u = u && w[r] == splat;
+                    x = x * 0x01000193u + (uint32_t)w[r];
+                    y = (y ^ (uint32_t)w[r]) * 0x85EBCA6Bu;
+                    if (sizeof(T) == 2) {
+                        x = x * 0x01000193u + (uint32_t)((uint64_t)w[r] >> 32);
+                        y = (y ^ (uint32_t)((uint64_t)w[r] >> 32)) * 0x85EBCA6Bu;
+                    }
+                }
+                x ^= x >> 15;
+                x *= 0x2C1B3C6Du;
+                x ^= x >> 12;
+                y ^= y >> 16;
+                uni[p] = u;
+                h1[p] = x;
+                h2[p] = y;
+                qidv[p] = 0;
+                qvalv[p] = v0;
+                if (u) qidv[p] = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
+            }
+            {
+                bool look[2];
+                uint32_t slot[2];
+                unsigned long long sv[2];
+#pragma unroll
+                for (int p = 0; p < 2; ++p) {
+                    look[p] = memo && !uni[p];
+                    slot[p] = h1[p] & a.memo_mask;
+                    sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
+                }
+#pragma unroll 1
+                for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
+#pragma unroll
+                    for (int p = 0; p < 2; ++p) {
+                        if (!look[p]) continue;
+                        if (sv[p] == 0ull) {
+                            look[p] = false;
+                        } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
+                                   memo_match<T, 32>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
+                            look[p] = false;
+                        } else if (step == 3) {
+                            look[p] = false;
+                        } else {
+                            slot[p] = (slot[p] + 1) & a.memo_mask;
+                            sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
+                        }
+                    }
+                }
+            }
+#pragma unroll 1
+            for (int p = 0; p < 2; ++p) {
+                const bool active = !uni[p] && qidv[p] == 0;
+                if (__any_sync(0xFFFFFFFFu, active)) {
+                    uint64_t pid;
+                    uint32_t pval;
+                    quad_groups<T, 32>(I, C, leaf_cache, qb[p], active, pid, pval);
+                    if (active) {
+                        qidv[p] = pid;
+                        qvalv[p] = pval;
+                        if (memo && pid != INVALID_ID) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
+                    }
+                }
+                oid[qm[p]] = qidv[p];
+                oval[qm[p]] = qvalv[p];
+            }
+        } else {
+            for (unsigned k = tid; k < 512; k += blockDim.x) {
+                oid[k] = EMPTY_ID;
+                oval[k] = 0;
+            }
+        }
+        __syncthreads();  // the tile is free
+        const uint64_t ahead = blk + (uint64_t)L::tiles * gridDim.x;
+        if (tid == 0 && ahead < n_blk) issue(ahead, buf);
+        if (L::tiles == 2) buf ^= 1;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
@@ -1747,7 +1923,7 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
         const bool is_branch = in && mask != 0 && !same;
         const uint32_t lod = is_branch ? calc_average8(cv) : 0;
         bool created;
-        uint64_t id = warp_intern_branch(I, is_branch, c, types, mask, lod, &created);
+        uint64_t id = warp_intern_branch_inl(I, is_branch, c, types, mask, lod, &created);
         if (!in) continue;
         uint64_t out = mask == 0 ? EMPTY_ID : (same ? c[0] : id);
         uint32_t val = mask == 0 ? 0 : (same ? cv[0] : lod);
@@ -2038,6 +2214,86 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
     }
     if (es == 1) return launch(dense_octants_kernel<uint8_t>);
     return launch(dense_octants_kernel<uint16_t>);
+}
+
+size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth) {
+    if (depth < 5) return 0;
+    size_t nodes = 0;  // quads and every level above them except the roots
+    for (int k = 1; k <= depth - 2; ++k) nodes += (size_t)n_chunks << (3 * k);
+    return nodes * 12 + 512;
+}
+
+cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
+                               int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
+                               bool clear_memo, uint64_t memo_chunks) {
+    if (n_chunks == 0) return cudaSuccess;
+    if (depth < 5 || depth > 10) return cudaErrorInvalidValue;
+    OctArgs a{};
+    a.trees = trees;
+    a.n_chunks = n_chunks;
+    a.depth = depth;
+    a.changed = changed;
+    if (memo) {
+        uint64_t sl, rc;
+        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, &sl, &rc);
+        char *m = static_cast<char *>(memo);
+        a.memo_slots = reinterpret_cast<unsigned long long *>(m);
+        a.memo_count = reinterpret_cast<unsigned int *>(m + sl * 8);
+        a.memo_recs = reinterpret_cast<unsigned char *>(m + sl * 8 + 256);
+        a.memo_mask = (uint32_t)(sl - 1);
+        a.memo_cap = (uint32_t)rc;
+        if (clear_memo) {
+            cudaError_t e = cudaMemsetAsync(m, 0, sl * 8 + 256, s);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    // level k (k = 1 .. depth-2, quads at k = depth-2) holds n_chunks * 8^k nodes
+    size_t off[12] = {0}, total = 0;
+    for (int k = depth - 2; k >= 1; --k) {
+        off[k] = total;
+        total += (size_t)n_chunks << (3 * k);
+    }
+    uint64_t *ids = static_cast<uint64_t *>(scratch);
+    uint32_t *vals = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch) + total * 8);
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const uint64_t side = 1ull << depth;
+    const uint32_t es = (uint32_t)(I.vbits / 8);
+    CUtensorMap tmap;
+    cuuint64_t dims[4] = {side, side, side, n_chunks};
+    cuuint64_t strides[3] = {side * es, side * side * es, side * side * side * es};
+    cuuint32_t box[4] = {32, 32, 32, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                        const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    uint64_t *q_ids = ids + off[depth - 2];
+    uint32_t *q_vals = vals + off[depth - 2];
+    auto launchq = [&](auto kernel, size_t smem) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCtaThreads, smem);
+        if (per_sm < 1) per_sm = 1;
+        uint64_t grid = (uint64_t)num_sms * per_sm;
+        const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
+        if (grid > need) grid = need;
+        count_launches(1);
+        kernel<<<(unsigned)grid, kCtaThreads, smem, s>>>(I, a, q_ids, q_vals, tmap);
+        return cudaGetLastError();
+    };
+    cudaError_t e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
+                            : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
+    if (e != cudaSuccess) return e;
+    for (int k = depth - 3; k >= 0; --k) {
+        const uint64_t np = (uint64_t)n_chunks << (3 * k);
+        e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], k > 0 ? ids + off[k] : nullptr,
+                               k > 0 ? vals + off[k] : nullptr, np, k == 0, trees, changed, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,

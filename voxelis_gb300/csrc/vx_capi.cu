@@ -590,11 +590,20 @@ void batch_from_dense(vx_batch *b, const void *grid) {
 #ifndef VX_DENSE_OCTANTS
 #define VX_DENSE_OCTANTS 1
 #endif
+#ifndef VX_DENSE_SPLIT
+#define VX_DENSE_SPLIT 1  // depth >= 5: quad kernel + one pass per level (else the fused per-block kernel)
+#endif
 
 int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void *d_grids, uint8_t *d_changed,
                int depth) {
     cudaStream_t s = it->stream;
-    if (VX_DENSE_OCTANTS && depth >= 4) {
+    if (VX_DENSE_SPLIT && depth >= 5) {
+        const size_t sb = (dense_split_scratch_bytes(n, depth) + 255) & ~(size_t)255;
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
+        Phase ph(it, VX_PROF_DENSE);
+        VX_CUDA(launch_dense_split(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
+                                   static_cast<char *>(it->ws.p) + sb));
+    } else if (VX_DENSE_OCTANTS && depth >= 4) {
         const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
         Phase ph(it, VX_PROF_DENSE);
@@ -1282,7 +1291,9 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
         uint32_t *dt = c.take<uint32_t>(n);
         uint8_t *dg = c.take<uint8_t>(per * n);
         uint8_t *dc = c.take<uint8_t>(n);
-        const size_t sb = (dense_octant_scratch_bytes(n, d) + 255) & ~(size_t)255;
+        const bool split = VX_DENSE_SPLIT && d >= 5;
+        const size_t sb = ((split ? dense_split_scratch_bytes(n, d) : dense_octant_scratch_bytes(n, d)) + 255) &
+                          ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, d, it->vbits)));
         char *memo = static_cast<char *>(it->ws.p) + sb;
         cudaStream_t s = it->stream;
@@ -1303,8 +1314,12 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
             VX_CUDA(cudaEventRecord(it->copy_events[k], it->copy_stream));
             VX_CUDA(cudaStreamWaitEvent(s, it->copy_events[k], 0));
             Phase ph(it, VX_PROF_DENSE);
-            VX_CUDA(launch_dense_octants(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p, it->num_sms, s,
-                                         memo, k == 0, n));
+            if (split)
+                VX_CUDA(launch_dense_split(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p, it->num_sms,
+                                           s, memo, k == 0, n));
+            else
+                VX_CUDA(launch_dense_octants(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p,
+                                             it->num_sms, s, memo, k == 0, n));
         }
         {
             Phase ph(it, VX_PROF_REFCOUNT);

@@ -244,9 +244,9 @@ __device__ __forceinline__ bool key_equal(const DevInterner &I, uint32_t idx, co
 #ifndef VX_INTERN_INLINE
 #define VX_INTERN_INLINE __noinline__
 #endif
-static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner &I, bool active, const uint64_t c[8],
-                                                       uint32_t types, uint32_t mask, uint32_t lod, bool *created,
-                                                       uint64_t h_in = 0) {
+__device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I, bool active, const uint64_t c[8],
+                                                           uint32_t types, uint32_t mask, uint32_t lod, bool *created,
+                                                           uint64_t h_in = 0) {
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t tm = (types << 8) | mask;
     uint64_t h = 0;
@@ -329,6 +329,13 @@ static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner
         if (waiting) __nanosleep(32);
     }
     return result;
+}
+
+// The same, out of line (for call sites on rare paths, to keep kernels small).
+static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner &I, bool active, const uint64_t c[8],
+                                                       uint32_t types, uint32_t mask, uint32_t lod, bool *created,
+                                                       uint64_t h_in = 0) {
+    return warp_intern_branch_inl(I, active, c, types, mask, lod, created, h_in);
 }
 
 // Find-or-create of the leaf for value v (v != 0) through the direct-mapped leaf table.
