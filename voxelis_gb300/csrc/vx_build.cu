@@ -53,6 +53,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -635,6 +638,7 @@ struct OctArgs {
     uint32_t *cnt;   // arrival counts of levels 0 .. depth-5 at cnt_off[k]
     uint64_t lvl_off[12];
     uint64_t cnt_off[12];
+    const void *grids;               // the chunks' dense grids (for plain bulk copies)
     // quad memo (optional: slots == nullptr disables it)
     unsigned long long *memo_slots;  // tag:32 | (record + 1):32, 0 = empty
     unsigned int *memo_count;        // records handed out
@@ -1732,34 +1736,243 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
 // level above is then one fresh_level_kernel pass over all chunks, one parent per thread, so the
 // probes of a whole level are in flight together. Tiles are double-buffered for 8-bit voxels: the
 // copy of block i+2 is issued when block i is done.
+#ifndef VX_QUAD_BULK1D
+#define VX_QUAD_BULK1D 0
+#endif
+#ifndef VX_QUAD_CACHE
+#define VX_QUAD_CACHE 0
+#endif
+#ifndef VX_QUAD_DEDUP
+#define VX_QUAD_DEDUP 1  // identical quads of a warp are looked up once
+#endif
+#ifndef VX_LEVEL_DEDUP
+#define VX_LEVEL_DEDUP 1  // identical parents of a warp probe the table once
+#endif
+constexpr int kQuadCache = VX_QUAD_CACHE;  // entries of the CTA's quad cache (8-bit voxels; power of two)
+
 template <class T>
 struct QuadSmem {
     static constexpr int tiles = sizeof(T) == 1 ? 2 : 1;
+    static constexpr int qcache = sizeof(T) == 1 ? kQuadCache : 0;
     static constexpr size_t tile = 32768 * sizeof(T);
     static constexpr size_t kc = tiles * tile;                       // 3 * kKeyCache u64
     static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;    // 256 u64
-    static constexpr size_t bar = leaf + 256 * 8;                    // 2 u64
-    static constexpr size_t kcval = bar + 16;                        // kKeyCache u32
-    static constexpr size_t total = kcval + (size_t)kKeyCache * 4;
+    static constexpr size_t full = leaf + 256 * 8;                   // tiles u64: copy landed
+    static constexpr size_t empty = full + 16;                       // tiles u64: consumers done
+    static constexpr size_t qid = empty + 16;                        // qcache u64: node id (0 free, 1 busy)
+    static constexpr size_t qwords = qid + (size_t)qcache * 8;       // qcache x 16 u32: the quad's rows
+    static constexpr size_t kcval = qwords + (size_t)qcache * 64;    // kKeyCache u32
+    static constexpr size_t qtag = kcval + (size_t)kKeyCache * 4;    // qcache u32: second hash
+    static constexpr size_t qlod = qtag + (size_t)qcache * 4;        // qcache u32: LOD value
+    static constexpr size_t total = qlod + (size_t)qcache * 4;
+};
+
+// CTA-wide cache of quads (8-bit voxels) in front of the device-wide memo: popular quads hit here
+// instead of sending every warp of the GPU to the same L2 lines.
+struct QuadCache {
+    uint64_t *id;
+    uint32_t *words, *tag, *lod;
+    int n;  // entries (0: none)
 };
 
 template <class T>
-__global__ void __launch_bounds__(kCtaThreads) dense_quads_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
-                                                                 uint32_t *q_vals,
-                                                                 const __grid_constant__ CUtensorMap tmap) {
-    using L = QuadSmem<T>;
+__device__ __forceinline__ bool rows_equal32(const T *a, const T *b) {
+    bool eq = true;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) eq = eq && *quad_row<T, 32>(a, r) == *quad_row<T, 32>(b, r);
+    return eq;
+}
+
+template <class T>
+__device__ __forceinline__ uint64_t qc_lookup(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase,
+                                              uint32_t &lod) {
+    if (sizeof(T) != 1 || Q.n == 0) return 0;
+    uint32_t h = (h1 >> 7) & (Q.n - 1);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        const uint64_t id = *(volatile uint64_t *)(Q.id + h);
+        if (id == 0) return 0;
+        if (id > 1 && *(volatile uint32_t *)(Q.tag + h) == h2) {
+            bool eq = true;
+            const volatile uint32_t *w = Q.words + 16 * h;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) eq = eq && w[r] == (uint32_t)*quad_row<T, 32>(qbase, r);
+            if (eq) {
+                lod = *(volatile uint32_t *)(Q.lod + h);
+                return id;
+            }
+        }
+        h = (h + 1) & (Q.n - 1);
+    }
+    return 0;
+}
+
+template <class T>
+__device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase, uint64_t id,
+                                          uint32_t lod) {
+    if (sizeof(T) != 1 || Q.n == 0) return;
+    uint32_t h = (h1 >> 7) & (Q.n - 1);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        if (atomicCAS((unsigned long long *)(Q.id + h), 0ull, 1ull) == 0ull) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) Q.words[16 * h + r] = (uint32_t)*quad_row<T, 32>(qbase, r);
+            Q.tag[h] = h2;
+            Q.lod[h] = lod;
+            __threadfence_block();
+            *(volatile uint64_t *)(Q.id + h) = id;
+            return;
+        }
+        h = (h + 1) & (Q.n - 1);
+    }
+}
+constexpr int kQuadConsumers = 8;                         // warps reducing quads
+constexpr int kQuadThreads = (kQuadConsumers + 1) * 32;   // plus one warp issuing the copies
+
+// The 64 quads of slab `qy` (4 voxels thick in y) of a 32^3 tile, two per lane: uniformity on row
+// words, the quad memo, the bottom-group path on misses; results to oid/oval (Morton order).
+template <class T>
+__device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArgs &a, const T *tile, uint32_t qy,
+                                              const KeyCache &C, const QuadCache &Q, uint64_t *leaf_cache,
+                                              uint64_t *oid, uint32_t *oval) {
     using W = typename QuadWord<T>::type;
+    const unsigned lane = threadIdx.x & 31u;
+    const bool memo = a.memo_slots != nullptr;
+    const T *qb[2];
+    uint32_t qm[2], h1[2], h2[2];
+    bool uni[2];
+    uint64_t qidv[2];
+    uint32_t qvalv[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p;
+        qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
+        qb[p] = tile + ((4 * qy) * 32 + 4 * qz) * 32 + 4 * qx;
+        W w[16];
+        quad_rows<T, 32>(qb[p], w);
+        const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
+        const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
+        bool u = true;
+        uint32_t x = 0x9E3779B9u, y = 0x7F4A7C15u;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            u = u && w[r] == splat;
+            x = x * 0x01000193u + (uint32_t)w[r];
+            y = (y ^ (uint32_t)w[r]) * 0x85EBCA6Bu;
+            if (sizeof(T) == 2) {
+                x = x * 0x01000193u + (uint32_t)((uint64_t)w[r] >> 32);
+                y = (y ^ (uint32_t)((uint64_t)w[r] >> 32)) * 0x85EBCA6Bu;
+            }
+        }
+        x ^= x >> 15;
+        x *= 0x2C1B3C6Du;
+        x ^= x >> 12;
+        y ^= y >> 16;
+        uni[p] = u;
+        h1[p] = x;
+        h2[p] = y;
+        qidv[p] = 0;
+        qvalv[p] = v0;
+        if (u) qidv[p] = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
+    }
+    // identical quads of the warp: only the lowest lane of each set looks them up
+    int leader[2];
+    bool follow[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        const uint64_t hk = (uni[p] || !VX_QUAD_DEDUP) ? (~0ull - lane) : (((uint64_t)h2[p] << 32) | h1[p]);
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, hk);
+        leader[p] = __ffs(peers) - 1;
+        const T *lq = reinterpret_cast<const T *>(
+            __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(qb[p]), leader[p]));
+        follow[p] = !uni[p] && leader[p] != (int)lane && rows_equal32<T>(qb[p], lq);
+        if (!uni[p] && !follow[p]) qidv[p] = qc_lookup<T>(Q, h1[p], h2[p], qb[p], qvalv[p]);
+    }
+    {  // memo probes, both quads in flight
+        bool look[2];
+        uint32_t slot[2];
+        unsigned long long sv[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            look[p] = memo && !uni[p] && !follow[p] && qidv[p] == 0;
+            slot[p] = h1[p] & a.memo_mask;
+            sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
+        }
+#pragma unroll 1
+        for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                if (!look[p]) continue;
+                if (sv[p] == 0ull) {
+                    look[p] = false;
+                } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
+                           memo_match<T, 32>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
+                    look[p] = false;
+                    qc_insert<T>(Q, h1[p], h2[p], qb[p], qidv[p], qvalv[p]);
+                } else if (step == 3) {
+                    look[p] = false;
+                } else {
+                    slot[p] = (slot[p] + 1) & a.memo_mask;
+                    sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
+                }
+            }
+        }
+    }
+#pragma unroll 1
+    for (int p = 0; p < 2; ++p) {
+        const bool active = !uni[p] && !follow[p] && qidv[p] == 0;
+        if (__any_sync(0xFFFFFFFFu, active)) {
+            uint64_t pid;
+            uint32_t pval;
+            quad_groups<T, 32>(I, C, leaf_cache, qb[p], active, pid, pval);
+            if (active) {
+                qidv[p] = pid;
+                qvalv[p] = pval;
+                if (pid != INVALID_ID) {
+                    if (memo) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
+                    qc_insert<T>(Q, h1[p], h2[p], qb[p], pid, pval);
+                }
+            }
+        }
+        const uint64_t lid = __shfl_sync(0xFFFFFFFFu, qidv[p], leader[p]);
+        const uint32_t lval = __shfl_sync(0xFFFFFFFFu, qvalv[p], leader[p]);
+        if (follow[p]) {
+            qidv[p] = lid;
+            qvalv[p] = lval;
+        }
+        oid[qm[p]] = qidv[p];
+        oval[qm[p]] = qvalv[p];
+    }
+}
+
+// One CTA streams 32^3 blocks through its tiles: warp kQuadConsumers (the producer) issues the copy of
+// each block as soon as the tile it goes to has been released; every consumer warp waits for the copy,
+// reduces its slab and releases the tile (an mbarrier arrival), so consumer warps never wait on one
+// another and a warp slowed by memo misses only holds back the copy two blocks ahead.
+template <class T>
+__global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
+                                                                  uint32_t *q_vals,
+                                                                  const __grid_constant__ CUtensorMap tmap) {
+    using L = QuadSmem<T>;
     extern __shared__ __align__(128) unsigned char smem[];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint64_t *kc = reinterpret_cast<uint64_t *>(smem + L::kc);
     uint64_t *leaf_cache = reinterpret_cast<uint64_t *>(smem + L::leaf);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + L::full);
+    uint64_t *empty = reinterpret_cast<uint64_t *>(smem + L::empty);
     KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
+    QuadCache Q{reinterpret_cast<uint64_t *>(smem + L::qid), reinterpret_cast<uint32_t *>(smem + L::qwords),
+                reinterpret_cast<uint32_t *>(smem + L::qtag), reinterpret_cast<uint32_t *>(smem + L::qlod), L::qcache};
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (L::qcache)
+        for (unsigned k = tid; k < (unsigned)L::qcache; k += blockDim.x) Q.id[k] = 0;
     if (sizeof(T) == 1)
         for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
     if (tid == 0) {
-        for (int b = 0; b < L::tiles; ++b) mbar_init(bars + b, 1);
+        for (int b = 0; b < L::tiles; ++b) {
+            mbar_init(full + b, 1);
+            mbar_init(empty + b, kQuadConsumers);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -1768,134 +1981,67 @@ __global__ void __launch_bounds__(kCtaThreads) dense_quads_kernel(DevInterner I,
     const int bb = 3 * (d - 5);
     const uint64_t n_blk = (uint64_t)a.n_chunks << bb;
     const uint64_t per_chunk = 1ull << (3 * (d - 2));  // quads per chunk
-    const bool memo = a.memo_slots != nullptr;
-    auto issue = [&](uint64_t b, int buf) {
-        const uint32_t c = (uint32_t)(b >> bb);
-        const uint32_t q = (uint32_t)(b & ((1ull << bb) - 1));
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(bars + buf, (uint32_t)L::tile);
-        tma_load_block32(smem + buf * L::tile, &tmap, (int)(compact3(q) * 32), (int)(compact3(q >> 2) * 32),
-                         (int)(compact3(q >> 1) * 32), (int)c, bars + buf);
-    };
-    uint32_t phases = 0;  // bit b: parity of tile b
-    if (tid == 0)
-        for (int b = 0; b < L::tiles; ++b)
-            if (blockIdx.x + (uint64_t)b * gridDim.x < n_blk) issue(blockIdx.x + (uint64_t)b * gridDim.x, b);
-    int buf = 0;
-    for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x) {
-        const T *tile = reinterpret_cast<const T *>(smem + buf * L::tile);
-        const uint32_t par = (phases >> buf) & 1u;
+    if (warp == kQuadConsumers) {  // producer
+        if (lane != 0) return;
+        uint32_t j = 0;
+        for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x, ++j) {
+            const int b = (int)(j % L::tiles);
+            const uint32_t use = j / L::tiles;
+            if (use > 0) {  // wait until every consumer released this tile's previous block
+                bool ok = false;
+                for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+                    if ((ok = mbar_try_wait(empty + b, (use - 1) & 1u))) break;
+                if (!ok) {
+                    set_error(I, ERR_TIMEOUT, 32);
+                    return;  // no copy of this CTA is in flight: every issued one was consumed or waited
+                }
+            }
+            const uint32_t c = (uint32_t)(blk >> bb);
+            const uint32_t q = (uint32_t)(blk & ((1ull << bb) - 1));
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(full + b, (uint32_t)L::tile);
+            if (VX_QUAD_BULK1D && bb == 0)  // a MaxDepth-5 chunk is one contiguous 32^3 block
+                bulk_copy_g2s(smem + b * L::tile, static_cast<const unsigned char *>(a.grids) + (size_t)c * L::tile,
+                              (uint32_t)L::tile, full + b);
+            else
+                tma_load_block32(smem + b * L::tile, &tmap, (int)(compact3(q) * 32), (int)(compact3(q >> 2) * 32),
+                                 (int)(compact3(q >> 1) * 32), (int)c, full + b);
+        }
+        return;
+    }
+    uint32_t j = 0;
+    for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x, ++j) {
+        const int b = (int)(j % L::tiles);
+        const uint32_t use = j / L::tiles;
         bool ok = false;
         for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-            if ((ok = mbar_try_wait(bars + buf, par))) break;
-        if (__syncthreads_or(!ok)) {  // give up together; drain every copy in flight first
-            if (tid == 0) set_error(I, ERR_TIMEOUT, 29);
-            for (int b = 0; b < L::tiles; ++b)
-                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bars + b, (phases >> b) & 1u); ++spin) {
-                }
+            if ((ok = mbar_try_wait(full + b, use & 1u))) break;
+        if (!__all_sync(0xFFFFFFFFu, ok)) {
+            // give up: the copy may still land, so keep waiting for it (bounded) before leaving
+            if (lane == 0) set_error(I, ERR_TIMEOUT, 29);
+            for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(full + b, use & 1u); ++spin) {
+            }
             return;
         }
-        phases ^= 1u << buf;
         const uint32_t c = (uint32_t)(blk >> bb);
         const uint64_t q = blk & ((1ull << bb) - 1);
         const uint32_t tree = a.trees[c];
         const bool bad = tree >= I.tree_cap || I.depths[tree] != d;  // the same answer in every thread
-        if (bad && tid == 0) set_error(I, ERR_INVALID, 31);
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 9);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 9);
         if (!bad) {
-            const T *qb[2];
-            uint32_t qm[2], h1[2], h2[2];
-            bool uni[2];
-            uint64_t qidv[2];
-            uint32_t qvalv[2];
-#pragma unroll
-            for (int p = 0; p < 2; ++p) {
-                const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p, qy = warp;
-                qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
-                qb[p] = tile + ((4 * qy) * 32 + 4 * qz) * 32 + 4 * qx;
-                W w[16];
-                quad_rows<T, 32>(qb[p], w);
-                const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
-                const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
-                bool u = true;
-                uint32_t x = 0x9E3779B9u, y = 0x7F4A7C15u;
-#pragma unroll
-                for (int r = 0; r < 16; ++r) {
-                    u = u && w[r] == splat;
-                    x = x * 0x01000193u + (uint32_t)w[r];
-                    y = (y ^ (uint32_t)w[r]) * 0x85EBCA6Bu;
-                    if (sizeof(T) == 2) {
-                        x = x * 0x01000193u + (uint32_t)((uint64_t)w[r] >> 32);
-                        y = (y ^ (uint32_t)((uint64_t)w[r] >> 32)) * 0x85EBCA6Bu;
-                    }
-                }
-                x ^= x >> 15;
-                x *= 0x2C1B3C6Du;
-                x ^= x >> 12;
-                y ^= y >> 16;
-                uni[p] = u;
-                h1[p] = x;
-                h2[p] = y;
-                qidv[p] = 0;
-                qvalv[p] = v0;
-                if (u) qidv[p] = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
-            }
-            {
-                bool look[2];
-                uint32_t slot[2];
-                unsigned long long sv[2];
-#pragma unroll
-                for (int p = 0; p < 2; ++p) {
-                    look[p] = memo && !uni[p];
-                    slot[p] = h1[p] & a.memo_mask;
-                    sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
-                }
-#pragma unroll 1
-                for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
-#pragma unroll
-                    for (int p = 0; p < 2; ++p) {
-                        if (!look[p]) continue;
-                        if (sv[p] == 0ull) {
-                            look[p] = false;
-                        } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
-                                   memo_match<T, 32>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
-                            look[p] = false;
-                        } else if (step == 3) {
-                            look[p] = false;
-                        } else {
-                            slot[p] = (slot[p] + 1) & a.memo_mask;
-                            sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
-                        }
-                    }
-                }
-            }
-#pragma unroll 1
-            for (int p = 0; p < 2; ++p) {
-                const bool active = !uni[p] && qidv[p] == 0;
-                if (__any_sync(0xFFFFFFFFu, active)) {
-                    uint64_t pid;
-                    uint32_t pval;
-                    quad_groups<T, 32>(I, C, leaf_cache, qb[p], active, pid, pval);
-                    if (active) {
-                        qidv[p] = pid;
-                        qvalv[p] = pval;
-                        if (memo && pid != INVALID_ID) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
-                    }
-                }
-                oid[qm[p]] = qidv[p];
-                oval[qm[p]] = qvalv[p];
-            }
+            quads_of_slab<T>(I, a, reinterpret_cast<const T *>(smem + b * L::tile), warp, C, Q, leaf_cache, oid,
+                             oval);
         } else {
-            for (unsigned k = tid; k < 512; k += blockDim.x) {
-                oid[k] = EMPTY_ID;
-                oval[k] = 0;
+            if (tid == 0) set_error(I, ERR_INVALID, 31);
+            for (unsigned k = lane; k < 64; k += 32) {
+                const uint32_t qm = spread3b(k & 7u) | (spread3b(warp) << 1) | (spread3b(k >> 3) << 2);
+                oid[qm] = EMPTY_ID;
+                oval[qm] = 0;
             }
         }
-        __syncthreads();  // the tile is free
-        const uint64_t ahead = blk + (uint64_t)L::tiles * gridDim.x;
-        if (tid == 0 && ahead < n_blk) issue(ahead, buf);
-        if (L::tiles == 2) buf ^= 1;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty + b);
     }
 }
 
@@ -1921,12 +2067,24 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
 #pragma unroll
         for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
         const bool is_branch = in && mask != 0 && !same;
-        const uint32_t lod = is_branch ? calc_average8(cv) : 0;
+        // identical parents of the warp (common in repetitive terrain) probe the table once
+        const uint64_t h = is_branch ? branch_fingerprint(c, (types << 8) | mask) : 0ull;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, (is_branch && VX_LEVEL_DEDUP) ? h : (~0ull - threadIdx.x));
+        const int leader = __ffs(peers) - 1;
+        bool same_key = true;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) same_key = same_key && __shfl_sync(0xFFFFFFFFu, c[k], leader) == c[k];
+        const bool follow = is_branch && leader != (int)(threadIdx.x & 31u) && same_key;
+        const bool probe = is_branch && !follow;
+        const uint32_t lod = probe ? calc_average8(cv) : 0;
         bool created;
-        uint64_t id = warp_intern_branch_inl(I, is_branch, c, types, mask, lod, &created);
+        uint64_t id = warp_intern_branch_inl(I, probe, c, types, mask, lod, &created, h);
+        const uint64_t lead_id = __shfl_sync(0xFFFFFFFFu, id, leader);
+        const uint32_t lead_lod = __shfl_sync(0xFFFFFFFFu, lod, leader);
         if (!in) continue;
+        if (follow) id = lead_id;
         uint64_t out = mask == 0 ? EMPTY_ID : (same ? c[0] : id);
-        uint32_t val = mask == 0 ? 0 : (same ? cv[0] : lod);
+        uint32_t val = mask == 0 ? 0 : (same ? cv[0] : (follow ? lead_lod : lod));
         if (is_root) {
             const uint32_t tree = trees[p];
             if (tree >= I.tree_cap) {
@@ -2233,6 +2391,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     a.n_chunks = n_chunks;
     a.depth = depth;
     a.changed = changed;
+    a.grids = grids;
     if (memo) {
         uint64_t sl, rc;
         memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, &sl, &rc);
@@ -2275,13 +2434,13 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCtaThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kQuadThreads, smem);
         if (per_sm < 1) per_sm = 1;
         uint64_t grid = (uint64_t)num_sms * per_sm;
         const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
         if (grid > need) grid = need;
         count_launches(1);
-        kernel<<<(unsigned)grid, kCtaThreads, smem, s>>>(I, a, q_ids, q_vals, tmap);
+        kernel<<<(unsigned)grid, kQuadThreads, smem, s>>>(I, a, q_ids, q_vals, tmap);
         return cudaGetLastError();
     };
     cudaError_t e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
