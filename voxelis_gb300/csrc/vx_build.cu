@@ -2383,7 +2383,8 @@ size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth) {
 
 cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
-                               bool clear_memo, uint64_t memo_chunks) {
+                               bool clear_memo, uint64_t memo_chunks, void (*levels_begin)(void *),
+                               void *levels_ctx) {
     if (n_chunks == 0) return cudaSuccess;
     if (depth < 5 || depth > 10) return cudaErrorInvalidValue;
     OctArgs a{};
@@ -2446,6 +2447,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     cudaError_t e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
                             : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
     if (e != cudaSuccess) return e;
+    if (levels_begin) (*levels_begin)(levels_ctx);
     for (int k = depth - 3; k >= 0; --k) {
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
         e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], k > 0 ? ids + off[k] : nullptr,

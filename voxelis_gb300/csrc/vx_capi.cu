@@ -224,6 +224,21 @@ struct Phase {
     }
 };
 
+// Two back-to-back phases on the stream: `first` until next() is called, then `second` until the
+// object dies (next() is the host callback launch_dense_split runs between its two kernel groups).
+struct PhaseSwitch {
+    vx_interner *it;
+    int second;
+    Phase *cur;
+    PhaseSwitch(vx_interner *i, int first, int second_) : it(i), second(second_), cur(new Phase(i, first)) {}
+    static void next(void *self) {
+        PhaseSwitch *ps = static_cast<PhaseSwitch *>(self);
+        delete ps->cur;
+        ps->cur = new Phase(ps->it, ps->second);
+    }
+    ~PhaseSwitch() { delete cur; }
+};
+
 int set_err(vx_interner *it, int code, const std::string &msg) {
     if (it) it->last_error = msg;
     return code;
@@ -600,9 +615,9 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
     if (VX_DENSE_SPLIT && depth >= 5) {
         const size_t sb = (dense_split_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
-        Phase ph(it, VX_PROF_DENSE);
+        PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
         VX_CUDA(launch_dense_split(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
-                                   static_cast<char *>(it->ws.p) + sb));
+                                   static_cast<char *>(it->ws.p) + sb, true, 0, &PhaseSwitch::next, &ps));
     } else if (VX_DENSE_OCTANTS && depth >= 4) {
         const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
@@ -1313,13 +1328,15 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
                                     cudaMemcpyHostToDevice, it->copy_stream));
             VX_CUDA(cudaEventRecord(it->copy_events[k], it->copy_stream));
             VX_CUDA(cudaStreamWaitEvent(s, it->copy_events[k], 0));
-            Phase ph(it, VX_PROF_DENSE);
-            if (split)
+            if (split) {
+                PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
                 VX_CUDA(launch_dense_split(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p, it->num_sms,
-                                           s, memo, k == 0, n));
-            else
+                                           s, memo, k == 0, n, &PhaseSwitch::next, &ps));
+            } else {
+                Phase ph(it, VX_PROF_DENSE);
                 VX_CUDA(launch_dense_octants(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p,
                                              it->num_sms, s, memo, k == 0, n));
+            }
         }
         {
             Phase ph(it, VX_PROF_REFCOUNT);

@@ -40,10 +40,13 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                                  void *memo = nullptr, bool clear_memo = true, uint64_t memo_chunks = 0);
 // Dense construction for chunk depths 5..10 in passes: a quad kernel over 32^3 blocks, then one
 // fresh_level pass per level above the quads. `scratch` must hold dense_split_scratch_bytes.
+// levels_begin(levels_ctx), when given, runs on the host between the quad launch and the level
+// launches (the profiler marks its phases there).
 size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth);
 cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
-                               bool clear_memo = true, uint64_t memo_chunks = 0);
+                               bool clear_memo = true, uint64_t memo_chunks = 0,
+                               void (*levels_begin)(void *) = nullptr, void *levels_ctx = nullptr);
 // One level of fresh parents above the blocks: n_parents = n_chunks * 8^k.
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
                                uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
