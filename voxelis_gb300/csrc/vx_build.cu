@@ -23,6 +23,7 @@
 // the number of child slots of newly created nodes that name it, plus one per tree root. That sum is
 // computed once per epoch over the allocation log (launch_epoch_refcounts) instead of per lookup.
 #include <cuda.h>
+#include <mutex>
 #include <type_traits>
 #include <cudaTypedefs.h>
 
@@ -1075,10 +1076,30 @@ __device__ __forceinline__ void quad_rows(const T *qbase, typename QuadWord<T>::
     for (int r = 0; r < 16; ++r) w[r] = *quad_row<T, S>(qbase, r);
 }
 
+#ifndef VX_MEMO_L1
+#define VX_MEMO_L1 0
+#endif
+// Bytes of one memo record: 16 row words of 4 voxels, then id (8 B) and LOD value, padded to whole
+// 128-byte lines, so a record never shares a cache line with another.
+__host__ __device__ constexpr size_t memo_stride(size_t voxel_bytes) {
+    return ((16 * 4 * voxel_bytes + 16) + 127) & ~(size_t)127;
+}
+
+// A memo slot goes from 0 to its final value once and never changes again. With VX_MEMO_L1 a probe
+// first reads the slot through L1 (a nonzero value there is final) and only re-reads zero from L2.
+__device__ __forceinline__ uint64_t memo_slot_load(const unsigned long long *slots, uint32_t slot) {
+    const uint64_t *p = reinterpret_cast<const uint64_t *>(slots) + slot;
+    if (VX_MEMO_L1) {
+        const uint64_t v = *p;
+        if (v) return v;
+    }
+    return ld_probe(p);
+}
+
 // Record r's address; the record's content is 16 row words of 4 voxels.
 template <class T>
 __device__ __forceinline__ unsigned char *memo_rec(const OctArgs &a, uint32_t r) {
-    return a.memo_recs + (size_t)r * (16 * 4 * sizeof(T) + 16);
+    return a.memo_recs + (size_t)r * memo_stride(sizeof(T));
 }
 
 template <class T, int S = 16>
@@ -1089,7 +1110,7 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
     bool eq = true;
 #pragma unroll
     for (int k = 0; k < 4 * (int)sizeof(T); ++k) {
-        const uint4 x = __ldcg(rv + k);
+        const uint4 x = VX_MEMO_L1 ? rv[k] : __ldcg(rv + k);  // a published record never changes
         if (sizeof(T) == 1) {
             eq = eq && x.x == (uint32_t)*quad_row<T, S>(qbase, 4 * k) && x.y == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 1) &&
                  x.z == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 2) && x.w == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 3);
@@ -1100,7 +1121,8 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
         }
     }
     if (!eq) return false;
-    const uint4 tail = __ldcg(reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T)));
+    const uint4 tail = VX_MEMO_L1 ? *reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T))
+                                  : __ldcg(reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T)));
     id = (uint64_t)tail.x | ((uint64_t)tail.y << 32);
     lod = tail.z;
     return true;
@@ -1247,7 +1269,7 @@ __device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const Oct
     for (int q = 0; q < 2; ++q) {
         look[q] = memo && !uni[q];
         slot[q] = h1[q] & a.memo_mask;
-        sv[q] = look[q] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[q]) : 0ull;
+        sv[q] = look[q] ? memo_slot_load(a.memo_slots, slot[q]) : 0ull;
     }
 #pragma unroll 1
     for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
@@ -1263,7 +1285,7 @@ __device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const Oct
                 look[q] = false;
             } else {
                 slot[q] = (slot[q] + 1) & a.memo_mask;
-                sv[q] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[q]);
+                sv[q] = memo_slot_load(a.memo_slots, slot[q]);
             }
         }
     }
@@ -1608,7 +1630,7 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
             for (int p = 0; p < 2; ++p) {
                 look[p] = memo && !uni[p];
                 slot[p] = h1[p] & a.memo_mask;
-                sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
+                sv[p] = look[p] ? memo_slot_load(a.memo_slots, slot[p]) : 0ull;
             }
 #pragma unroll 1
             for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
@@ -1624,7 +1646,7 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
                         look[p] = false;
                     } else {
                         slot[p] = (slot[p] + 1) & a.memo_mask;
-                        sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
+                        sv[p] = memo_slot_load(a.memo_slots, slot[p]);
                     }
                 }
             }
@@ -1896,7 +1918,7 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
         for (int p = 0; p < 2; ++p) {
             look[p] = memo && !uni[p] && !follow[p] && qidv[p] == 0;
             slot[p] = h1[p] & a.memo_mask;
-            sv[p] = look[p] ? ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]) : 0ull;
+            sv[p] = look[p] ? memo_slot_load(a.memo_slots, slot[p]) : 0ull;
         }
 #pragma unroll 1
         for (int step = 0; step < 4 && (look[0] || look[1]); ++step) {
@@ -1913,7 +1935,7 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
                     look[p] = false;
                 } else {
                     slot[p] = (slot[p] + 1) & a.memo_mask;
-                    sv[p] = ld_probe(reinterpret_cast<const uint64_t *>(a.memo_slots) + slot[p]);
+                    sv[p] = memo_slot_load(a.memo_slots, slot[p]);
                 }
             }
         }
@@ -2045,6 +2067,54 @@ __global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I
     }
 }
 
+// One parent per lane from its 8 children: EMPTY, a collapsed leaf, or the interned branch.
+// Identical parents of the warp (common in repetitive terrain) probe the table once. Warp-collective:
+// every lane calls it; lanes with in == false only take part.
+__device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool in, const uint64_t c[8],
+                                                    const uint32_t cv[8], uint64_t &out, uint32_t &val) {
+    uint32_t types = 0, mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        mask |= (c[k] != 0 ? 1u : 0u) << k;
+        types |= (id_is_leaf(c[k]) ? 1u : 0u) << k;
+    }
+    bool same = types == 0xFF;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
+    const bool is_branch = in && mask != 0 && !same;
+    const uint64_t h = is_branch ? branch_fingerprint(c, (types << 8) | mask) : 0ull;
+    const unsigned peers =
+        __match_any_sync(0xFFFFFFFFu, (is_branch && VX_LEVEL_DEDUP) ? h : (~0ull - (threadIdx.x & 31u)));
+    const int leader = __ffs(peers) - 1;
+    bool same_key = true;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) same_key = same_key && __shfl_sync(0xFFFFFFFFu, c[k], leader) == c[k];
+    const bool follow = is_branch && leader != (int)(threadIdx.x & 31u) && same_key;
+    const bool probe = is_branch && !follow;
+    const uint32_t lod = probe ? calc_average8(cv) : 0;
+    bool created;
+    uint64_t id = warp_intern_branch_inl(I, probe, c, types, mask, lod, &created, h);
+    const uint64_t lead_id = __shfl_sync(0xFFFFFFFFu, id, leader);
+    const uint32_t lead_lod = __shfl_sync(0xFFFFFFFFu, lod, leader);
+    if (follow) id = lead_id;
+    out = mask == 0 ? EMPTY_ID : (same ? c[0] : id);
+    val = mask == 0 ? 0 : (same ? cv[0] : (follow ? lead_lod : lod));
+}
+
+__device__ __forceinline__ void commit_root(const DevInterner &I, const uint32_t *trees, uint8_t *changed, uint64_t p,
+                                            uint64_t out) {
+    const uint32_t tree = trees[p];
+    if (tree >= I.tree_cap) {
+        set_error(I, ERR_INVALID, 22);
+        return;
+    }
+    if (out != EMPTY_ID) {
+        I.roots[tree] = out;
+        atomicAdd(I.refcount + id_index(out), 1u);
+    }
+    if (changed) changed[p] = out != EMPTY_ID;
+}
+
 __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
@@ -2055,47 +2125,17 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
         const bool in = p < n_parents;
         uint64_t c[8];
         uint32_t cv[8];
-        uint32_t types = 0, mask = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             c[k] = in ? in_ids[8 * p + k] : 0;
             cv[k] = in ? in_vals[8 * p + k] : 0;
-            mask |= (c[k] != 0 ? 1u : 0u) << k;
-            types |= (id_is_leaf(c[k]) ? 1u : 0u) << k;
         }
-        bool same = types == 0xFF;
-#pragma unroll
-        for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
-        const bool is_branch = in && mask != 0 && !same;
-        // identical parents of the warp (common in repetitive terrain) probe the table once
-        const uint64_t h = is_branch ? branch_fingerprint(c, (types << 8) | mask) : 0ull;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, (is_branch && VX_LEVEL_DEDUP) ? h : (~0ull - threadIdx.x));
-        const int leader = __ffs(peers) - 1;
-        bool same_key = true;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) same_key = same_key && __shfl_sync(0xFFFFFFFFu, c[k], leader) == c[k];
-        const bool follow = is_branch && leader != (int)(threadIdx.x & 31u) && same_key;
-        const bool probe = is_branch && !follow;
-        const uint32_t lod = probe ? calc_average8(cv) : 0;
-        bool created;
-        uint64_t id = warp_intern_branch_inl(I, probe, c, types, mask, lod, &created, h);
-        const uint64_t lead_id = __shfl_sync(0xFFFFFFFFu, id, leader);
-        const uint32_t lead_lod = __shfl_sync(0xFFFFFFFFu, lod, leader);
+        uint64_t out;
+        uint32_t val;
+        reduce_parent_dedup(I, in, c, cv, out, val);
         if (!in) continue;
-        if (follow) id = lead_id;
-        uint64_t out = mask == 0 ? EMPTY_ID : (same ? c[0] : id);
-        uint32_t val = mask == 0 ? 0 : (same ? cv[0] : (follow ? lead_lod : lod));
         if (is_root) {
-            const uint32_t tree = trees[p];
-            if (tree >= I.tree_cap) {
-                set_error(I, ERR_INVALID, 22);
-                continue;
-            }
-            if (out != EMPTY_ID) {
-                I.roots[tree] = out;
-                atomicAdd(I.refcount + id_index(out), 1u);
-            }
-            if (changed) changed[p] = out != EMPTY_ID;
+            commit_root(I, trees, changed, p, out);
         } else {
             out_ids[p] = out;
             out_vals[p] = val;
@@ -2103,10 +2143,59 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
     }
 }
 
-// Adds one reference per child slot of every node created in this epoch. Leaf children of 8-bit
-// interners are first summed per value in shared memory (a handful of leaves is named by most
-// bottom branches).
-// Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
+// The three top levels of kTopChunks chunks per CTA (depths 2, 1 and 0: 64 + 8 + 1 nodes a chunk)
+// from their depth-3 nodes, level by level in shared memory: one launch instead of three, whose
+// latency chains overlap across the CTAs.
+constexpr int kTopChunks = 4;
+
+__global__ void __launch_bounds__(kThreads) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
+                                                             const uint32_t *in_vals, uint32_t n_chunks,
+                                                             const uint32_t *trees, uint8_t *changed) {
+    __shared__ uint64_t s2[64 * kTopChunks], s1[8 * kTopChunks];
+    __shared__ uint32_t v2[64 * kTopChunks], v1[8 * kTopChunks];
+    const unsigned t = threadIdx.x, warp = t >> 5, lane = t & 31u;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * kTopChunks; c0 < n_chunks; c0 += (uint64_t)gridDim.x * kTopChunks) {
+        {  // depth 2: thread t takes node t of the CTA's chunks
+            const uint64_t p = c0 * 64 + t;
+            const bool in = c0 + t / 64 < n_chunks;
+            uint64_t c[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                c[k] = in ? in_ids[8 * p + k] : 0;
+                cv[k] = in ? in_vals[8 * p + k] : 0;
+            }
+            reduce_parent_dedup(I, in, c, cv, s2[t], v2[t]);
+        }
+        __syncthreads();
+        if (warp == 0) {  // depth 1: lane l takes node l (chunk l / 8)
+            const bool in = c0 + lane / 8 < n_chunks;
+            uint64_t c[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                c[k] = s2[8 * lane + k];
+                cv[k] = v2[8 * lane + k];
+            }
+            reduce_parent_dedup(I, in, c, cv, s1[lane], v1[lane]);
+            __syncwarp();
+            // roots: lane l < kTopChunks takes chunk c0 + l
+            const bool rin = lane < kTopChunks && c0 + lane < n_chunks;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                c[k] = rin ? s1[(8 * lane + k) & (8 * kTopChunks - 1)] : 0;
+                cv[k] = rin ? v1[(8 * lane + k) & (8 * kTopChunks - 1)] : 0;
+            }
+            uint64_t out;
+            uint32_t val;
+            reduce_parent_dedup(I, rin, c, cv, out, val);
+            if (rin) commit_root(I, trees, changed, c0 + lane, out);
+        }
+        __syncthreads();
+    }
+}
+
+// Adds one reference per child slot of every node created in this epoch. Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
 // bottom groups), so they are summed per CTA before touching global memory: 8-bit leaves in a
 // 256-entry array indexed by value, wider leaves in an open-addressed shared table keyed by node
 // index (entries that find no slot within kLeafProbe steps go straight to global atomics).
@@ -2204,6 +2293,30 @@ __global__ void epoch_finalize_kernel(DevInterner I) {
 
 }  // namespace
 
+// Opts `kernel` in to `smem` bytes of dynamic shared memory and returns its resident CTAs per SM,
+// cached per (kernel, threads, smem): both calls cost host time on every launch otherwise.
+static int prepare_kernel(const void *kernel, int threads, size_t smem, cudaError_t *err) {
+    struct Entry {
+        const void *k;
+        int threads;
+        size_t smem;
+        int per_sm;
+    };
+    static Entry cache[32];
+    static int used = 0;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < used; ++i)
+        if (cache[i].k == kernel && cache[i].threads == threads && cache[i].smem == smem) return cache[i].per_sm;
+    *err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (*err != cudaSuccess) return 0;
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (used < 32) cache[used++] = Entry{kernel, threads, smem, per_sm};
+    return per_sm;
+}
+
 size_t dense32_smem_bytes(int vbytes) { return (size_t)32768 * vbytes + (3 * kKeyCache + 256 + 8) * 8 + 8 * 4 + 64; }
 
 size_t dense_smem_bytes(int bdepth, int vbytes) {
@@ -2217,17 +2330,16 @@ template <class K>
 static cudaError_t launch_persistent(K kernel, const DevInterner &I, const DenseArgs &a, size_t smem, int num_sms,
                                     cudaStream_t s) {
     const uint64_t total = (uint64_t)a.n_chunks * a.blocks_per_chunk;
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaSuccess;
+    const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kThreads, smem, &e);
     if (e != cudaSuccess) return e;
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
-    if (per_sm < 1) per_sm = 1;
     uint64_t grid = (uint64_t)num_sms * per_sm;
     if (grid > total) grid = total;
     count_launches(1);
     kernel<<<(unsigned)grid, kThreads, smem, s>>>(I, a);
     return cudaGetLastError();
 }
+
 
 cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s) {
     if ((uint64_t)a.n_chunks * a.blocks_per_chunk == 0) return cudaSuccess;
@@ -2275,7 +2387,7 @@ size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits) {
     if (depth < 4) return 0;
     uint64_t sl, rc;
     memo_geometry(n_chunks, depth, &sl, &rc);
-    const size_t stride = 16 * 4 * (size_t)(vbits / 8) + 16;
+    const size_t stride = memo_stride((size_t)(vbits / 8));
     return sl * 8 + 256 + rc * stride + 256;
 }
 
@@ -2341,11 +2453,9 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                         (3 * kKeyCache + 256 + 2 * kOctWarps + 9 * kNodeCacheAlloc) * 8 + (kKeyCache + kNodeCacheAlloc) * 4 + 64;
     const uint64_t n_oct = (uint64_t)n_chunks << (3 * (depth - 4));
     auto launch = [&](auto kernel) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaSuccess;
+        const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kThreads, smem, &e);
         if (e != cudaSuccess) return e;
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
-        if (per_sm < 1) per_sm = 1;
         uint64_t grid = (uint64_t)num_sms * per_sm;
         const uint64_t need = (n_oct + kOctWarps - 1) / kOctWarps;
         if (grid > need) grid = need;
@@ -2355,11 +2465,9 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
     };
     if (cta32) {
         auto launch32 = [&](auto kernel, size_t smem32) -> cudaError_t {
-            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+            cudaError_t e = cudaSuccess;
+            const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kCtaThreads, smem32, &e);
             if (e != cudaSuccess) return e;
-            int per_sm = 1;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCtaThreads, smem32);
-            if (per_sm < 1) per_sm = 1;
             uint64_t grid = (uint64_t)num_sms * per_sm;
             const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
             if (grid > need) grid = need;
@@ -2432,11 +2540,9 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     uint64_t *q_ids = ids + off[depth - 2];
     uint32_t *q_vals = vals + off[depth - 2];
     auto launchq = [&](auto kernel, size_t smem) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaSuccess;
+        const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQuadThreads, smem, &e);
         if (e != cudaSuccess) return e;
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kQuadThreads, smem);
-        if (per_sm < 1) per_sm = 1;
         uint64_t grid = (uint64_t)num_sms * per_sm;
         const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
         if (grid > need) grid = need;
@@ -2448,13 +2554,17 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
                             : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
     if (e != cudaSuccess) return e;
     if (levels_begin) (*levels_begin)(levels_ctx);
-    for (int k = depth - 3; k >= 0; --k) {
+    for (int k = depth - 3; k >= 3; --k) {
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
-        e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], k > 0 ? ids + off[k] : nullptr,
-                               k > 0 ? vals + off[k] : nullptr, np, k == 0, trees, changed, s);
+        e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], ids + off[k], vals + off[k], np, false, trees,
+                               changed, s);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    // depths 2, 1 and 0 in one launch
+    const unsigned top_blocks = (unsigned)((n_chunks + kTopChunks - 1) / kTopChunks);
+    count_launches(1);
+    fresh_top_kernel<<<top_blocks, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
