@@ -1772,12 +1772,25 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
 #endif
 constexpr int kQuadCache = VX_QUAD_CACHE;  // entries of the CTA's quad cache (8-bit voxels; power of two)
 
+constexpr int kQuadConsumers = 8;                         // warps reducing quads
+constexpr int kQuadThreads = (kQuadConsumers + 1) * 32;   // plus one warp issuing the copies
+
+#ifndef VX_QUAD_PRIVATE
+#define VX_QUAD_PRIVATE 0  // 1: 8-bit voxels are copied out of the tile per warp and the tile released at once
+#endif
+#ifndef VX_QUAD_TILES
+#define VX_QUAD_TILES 1
+#endif
+
 template <class T>
 struct QuadSmem {
-    static constexpr int tiles = sizeof(T) == 1 ? 2 : 1;
+    static constexpr bool priv = VX_QUAD_PRIVATE && sizeof(T) == 1;
+    static constexpr int tiles = priv ? VX_QUAD_TILES : (sizeof(T) == 1 ? 2 : 1);
+    static constexpr size_t slab = 4 * 32 * 32 * sizeof(T);  // one warp's 4 x 32 x 32 voxels
     static constexpr int qcache = sizeof(T) == 1 ? kQuadCache : 0;
     static constexpr size_t tile = 32768 * sizeof(T);
-    static constexpr size_t kc = tiles * tile;                       // 3 * kKeyCache u64
+    static constexpr size_t privs = tiles * tile;                    // kQuadConsumers private slabs
+    static constexpr size_t kc = privs + (priv ? kQuadConsumers * slab : 0);  // 3 * kKeyCache u64
     static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;    // 256 u64
     static constexpr size_t full = leaf + 256 * 8;                   // tiles u64: copy landed
     static constexpr size_t empty = full + 16;                       // tiles u64: consumers done
@@ -1848,13 +1861,12 @@ __device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint3
         h = (h + 1) & (Q.n - 1);
     }
 }
-constexpr int kQuadConsumers = 8;                         // warps reducing quads
-constexpr int kQuadThreads = (kQuadConsumers + 1) * 32;   // plus one warp issuing the copies
 
-// The 64 quads of slab `qy` (4 voxels thick in y) of a 32^3 tile, two per lane: uniformity on row
-// words, the quad memo, the bottom-group path on misses; results to oid/oval (Morton order).
+// The 64 quads of slab `qy` (4 voxels thick in y, [4][32][32] voxels at `slab`) of a 32^3 block, two
+// per lane: uniformity on row words, the quad memo, the bottom-group path on misses; results to
+// oid/oval (Morton order).
 template <class T>
-__device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArgs &a, const T *tile, uint32_t qy,
+__device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArgs &a, const T *slab, uint32_t qy,
                                               const KeyCache &C, const QuadCache &Q, uint64_t *leaf_cache,
                                               uint64_t *oid, uint32_t *oval) {
     using W = typename QuadWord<T>::type;
@@ -1869,7 +1881,7 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
     for (int p = 0; p < 2; ++p) {
         const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p;
         qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
-        qb[p] = tile + ((4 * qy) * 32 + 4 * qz) * 32 + 4 * qx;
+        qb[p] = slab + (4 * qz) * 32 + 4 * qx;
         W w[16];
         quad_rows<T, 32>(qb[p], w);
         const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
@@ -2051,9 +2063,18 @@ __global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I
         const bool bad = tree >= I.tree_cap || I.depths[tree] != d;  // the same answer in every thread
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 9);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 9);
+        const T *slab = reinterpret_cast<const T *>(smem + b * L::tile + warp * L::slab);
+        if (L::priv) {  // copy the slab out (4 KiB, 128 B a lane) and hand the tile back at once
+            const uint4 *src = reinterpret_cast<const uint4 *>(slab);
+            uint4 *dst = reinterpret_cast<uint4 *>(smem + L::privs + warp * L::slab);
+#pragma unroll
+            for (int k = 0; k < (int)(L::slab / 16 / 32); ++k) dst[k * 32 + lane] = src[k * 32 + lane];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + b);
+            slab = reinterpret_cast<const T *>(dst);
+        }
         if (!bad) {
-            quads_of_slab<T>(I, a, reinterpret_cast<const T *>(smem + b * L::tile), warp, C, Q, leaf_cache, oid,
-                             oval);
+            quads_of_slab<T>(I, a, slab, warp, C, Q, leaf_cache, oid, oval);
         } else {
             if (tid == 0) set_error(I, ERR_INVALID, 31);
             for (unsigned k = lane; k < 64; k += 32) {
@@ -2063,7 +2084,7 @@ __global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I
             }
         }
         __syncwarp();
-        if (lane == 0) mbar_arrive(empty + b);
+        if (!L::priv && lane == 0) mbar_arrive(empty + b);
     }
 }
 
