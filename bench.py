@@ -50,9 +50,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    p.add_argument("--workload", default="dunes", choices=["dunes", "edits", "serve", "large"],
+    p.add_argument("--workload", default="dunes", choices=["dunes", "edits", "serve", "large", "mesh"],
                    help="dunes: batched dense build of 4096 32^3 chunks (default); edits: uneven batched edits")
     p.add_argument("--check", action="store_true", help="large: compare with the CPU oracle after every step")
+    p.add_argument("--edits-chunks", type=int, default=512,
+                   help="edits: chunks per depth (512 is the benchmark; fewer for profiling)")
     p.add_argument("--quick", action="store_true",
                    help="timed build steps and gets only (no per-chunk, e2e or CPU legs); for profiling")
     return p.parse_args()
@@ -476,6 +478,10 @@ def main():
         from voxelis_gb300 import bench_large
 
         bench_large.run(args, check=args.check)
+    elif args.workload == "mesh":
+        from voxelis_gb300 import bench_mesh
+
+        bench_mesh.run(args)
     elif args.workload == "serve":
         from voxelis_gb300 import bench_serve
 

@@ -236,6 +236,20 @@ int vx_stage_spheres(int chunk_depth, int32_t nx, int32_t ny, int32_t nz, uint32
 int vx_world_get_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
                        uint8_t *found_dev, void *values_dev);
 
+/* Occupancy masks for greedy meshing (generate_occupancy_masks + fill_masks_for_region,
+ * utils/mesh.rs:418-597; OccupancyDataBuilder, mesh.rs:181-193): the non-default voxels of n_trees
+ * trees of one MaxDepth d (1..6) placed into one 64^3 builder, tree k at voxel offset
+ * offsets[3k..3k+2] (x, y, z), each within 0..64-2^d. Host outputs:
+ *   global[3 * 4096]  planes YZ ([y][z] -> bits of x), XZ ([z][x] -> bits of y), XY ([y][x] -> bits of z)
+ *   active[6]         occupied y, z (YZ rows/cols), z, x (XZ), y, x (XY)
+ *   n_materials       distinct material ids (voxel values) present
+ *   material_ids[k], material_counts[k] (voxels), material_masks[k][3 * 4096] for k < max_materials,
+ *                     in ascending material order (the builder's HashMaps, ordered)
+ * VX_E_BUFFER (with *n_materials set) when more materials are present than max_materials. */
+int vx_occupancy_masks(vx_interner *it, uint32_t n_trees, const vx_tree *trees, const uint32_t *offsets,
+                       uint64_t *global, uint64_t *active, uint32_t max_materials, uint32_t *n_materials,
+                       uint32_t *material_ids, uint64_t *material_counts, uint64_t *material_masks);
+
 /* ---- verification helpers (not on the timed path) ---------------------------------------- */
 /* Canonical DFS export of the DAG reachable from `trees` (see vx_canonical). On VX_E_BUFFER
  * *n_nodes holds the required capacity. */

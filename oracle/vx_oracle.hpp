@@ -26,6 +26,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <map>
 #include <vector>
 
 namespace vxo {
@@ -614,6 +615,50 @@ inline bool get_at_depth(const Interner<T> &it, uint64_t node, int32_t x, int32_
 }
 
 // ---- VoxTree<T> (spatial/voxtree.rs:108-1118) ----------------------------------------------------
+// OccupancyDataBuilder (utils/mesh.rs:181-193) and fill_masks_for_region (mesh.rs:418-511): a 64^3
+// space, three planes of 64 x 64 u64 words (YZ: [y][z] -> x bits, XZ: [z][x] -> y bits, XY: [y][x]
+// -> z bits), global and per material, six active row/column masks and voxel counts per material.
+struct Occupancy {
+    static constexpr uint32_t kAxis = 64, kPlane = 64 * 64, kAll = 3 * 64 * 64;
+    static constexpr uint32_t kYZ = 0, kXZ = kPlane, kXY = 2 * kPlane;
+    std::vector<uint64_t> global = std::vector<uint64_t>(kAll, 0);
+    uint64_t active[6] = {0, 0, 0, 0, 0, 0};
+    std::map<uint32_t, std::vector<uint64_t>> per_material;
+    std::map<uint32_t, uint64_t> materials;
+
+    void fill_region(uint32_t sx, uint32_t sy, uint32_t sz, uint32_t side, uint32_t material) {
+        materials[material] += (uint64_t)side * side * side;
+        if (side != kAxis) {
+            auto &pm = per_material[material];
+            if (pm.empty()) pm.assign(kAll, 0);
+            const uint64_t run = (1ull << side) - 1;
+            const uint64_t xm = run << sx, ym = run << sy, zm = run << sz;
+            active[0] |= ym;
+            active[1] |= zm;
+            active[2] |= zm;
+            active[3] |= xm;
+            active[4] |= ym;
+            active[5] |= xm;
+            for (uint32_t i = 0; i < side; ++i) {
+                const uint32_t z = sz + i, y = sy + i;
+                const uint32_t by = kXZ + z * kAxis + sx, bz = kXY + y * kAxis + sx, bx = kYZ + y * kAxis + sz;
+                for (uint32_t j = 0; j < side; ++j) {
+                    global[by + j] |= ym;
+                    pm[by + j] |= ym;
+                    global[bz + j] |= zm;
+                    pm[bz + j] |= zm;
+                    global[bx + j] |= xm;
+                    pm[bx + j] |= xm;
+                }
+            }
+        } else {
+            per_material[material].assign(kAll, ~0ull);
+            std::fill(global.begin(), global.end(), ~0ull);
+            for (auto &a : active) a = ~0ull;
+        }
+    }
+};
+
 template <class T>
 class Tree {
    public:
@@ -751,6 +796,43 @@ class Tree {
                         T *row = data + yy * n * n + zz * n + e.x;
                         for (size_t xx = 0; xx < side; ++xx) row[xx] = v;
                     }
+            }
+        }
+    }
+
+    // generate_occupancy_masks (utils/mesh.rs:515-597): the same traversal as to_vec, each
+    // non-default leaf region passed to fill_masks_for_region at `offset` inside the 64^3 builder.
+    template <class B>
+    void occupancy_masks(const Interner<T> &it, B &builder, uint32_t ox, uint32_t oy, uint32_t oz) const {
+        if (bid::is_empty(root_)) return;
+        const uint32_t md = (uint32_t)max_depth_;
+        if (!bid::is_branch(root_)) {
+            T v = it.get_value(root_);
+            if (v != T(0)) builder.fill_region(ox, oy, oz, 1u << md, (uint32_t)v);
+            return;
+        }
+        struct E {
+            uint64_t id;
+            uint32_t x, y, z, depth;
+        };
+        std::vector<E> stack;
+        stack.push_back({root_, 0, 0, 0, 0});
+        while (!stack.empty()) {
+            E e = stack.back();
+            stack.pop_back();
+            if (bid::is_branch(e.id) && e.depth < md) {
+                const uint32_t half = 1u << (md - e.depth - 1);
+                const Children &ch = it.get_children(e.id);
+                for (int i = 7; i >= 0; --i) {
+                    uint64_t c = ch[i];
+                    if (bid::is_empty(c)) continue;
+                    stack.push_back({c, e.x + (i & 1) * half, e.y + ((i >> 1) & 1) * half,
+                                     e.z + ((i >> 2) & 1) * half, e.depth + 1});
+                }
+            } else {
+                T v = it.get_value(e.id);
+                if (v == T(0)) continue;
+                builder.fill_region(ox + e.x, oy + e.y, oz + e.z, 1u << (md - e.depth), (uint32_t)v);
             }
         }
     }

@@ -477,6 +477,36 @@ int vxo_tree_to_dense(void *h, uint32_t tree, void *out) {
     });
 }
 
+int vxo_occupancy_masks(void *h, uint32_t n_trees, const uint32_t *trees, const uint32_t *offsets, uint64_t *global,
+                        uint64_t *active, uint32_t max_materials, uint32_t *n_materials, uint32_t *material_ids,
+                        uint64_t *material_counts, uint64_t *material_masks) {
+    return with_interner(h, [&](auto &o) {
+        if (!n_trees || !trees || !offsets || !global || !active || !n_materials) return VX_E_INVALID_ARG;
+        vxo::Occupancy b;
+        for (uint32_t k = 0; k < n_trees; ++k) {
+            auto *t = o.tree(trees[k]);
+            const uint32_t side = 1u << t->max_depth();
+            for (int a = 0; a < 3; ++a)
+                if (offsets[3 * k + a] + side > 64) return fail(&o, VX_E_OOB, "tree outside the 64^3 builder");
+            t->occupancy_masks(o.it, b, offsets[3 * k], offsets[3 * k + 1], offsets[3 * k + 2]);
+        }
+        std::copy(b.global.begin(), b.global.end(), global);
+        std::copy(b.active, b.active + 6, active);
+        *n_materials = (uint32_t)b.materials.size();
+        uint32_t k = 0;
+        for (auto &kv : b.materials) {
+            if (k >= max_materials) break;
+            material_ids[k] = kv.first;
+            material_counts[k] = kv.second;
+            const auto &pm = b.per_material[kv.first];
+            std::copy(pm.begin(), pm.end(), material_masks + (size_t)k * vxo::Occupancy::kAll);
+            ++k;
+        }
+        return b.materials.size() > max_materials ? fail(&o, VX_E_BUFFER, "more materials than max_materials")
+                                                  : VX_OK;
+    });
+}
+
 // The UB fence: every child reachable from the trees has a matching generation and a positive
 // refcount.
 int vxo_validate(void *h, uint32_t n, const uint32_t *trees) {

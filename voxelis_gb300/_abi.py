@@ -132,6 +132,7 @@ SIGNATURES = {
     "export_canonical": [_P, _U32, _P, C.POINTER(vx_canonical), _PU64],
     "tree_to_dense": [_P, _U32, _P],
     "validate": [_P, _U32, _P],
+    "occupancy_masks": [_P, _U32, _P, _P, _P, _P, _U32, _P, _P, _P, _P],
 }
 
 # entry points only the GPU library has

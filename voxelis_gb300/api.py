@@ -131,6 +131,24 @@ class VoxInterner:
         self._call("trees_to_dense", len(trees), _np_ptr(handles), _np_ptr(out), VX_MEM_HOST)
         return out
 
+    def occupancy_masks(self, trees, offsets, max_materials=256):
+        """generate_occupancy_masks into one 64^3 builder (utils/mesh.rs:418-597): tree k at voxel
+        offset offsets[k] = (x, y, z). Returns dict(global=[3, 64, 64] u64 planes YZ/XZ/XY,
+        active=[6] u64, materials={id: (count, [3, 64, 64] u64 masks)})."""
+        handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)
+        offs = np.ascontiguousarray(offsets, dtype=np.uint32).reshape(-1, 3)
+        glob = np.zeros(3 * 4096, np.uint64)
+        active = np.zeros(6, np.uint64)
+        n_mat = C.c_uint32()
+        ids = np.zeros(max_materials, np.uint32)
+        counts = np.zeros(max_materials, np.uint64)
+        masks = np.zeros((max_materials, 3 * 4096), np.uint64)
+        self._call("occupancy_masks", len(trees), _np_ptr(handles), _np_ptr(offs), _np_ptr(glob), _np_ptr(active),
+                   max_materials, C.byref(n_mat), _np_ptr(ids), _np_ptr(counts), _np_ptr(masks))
+        k = n_mat.value
+        mats = {int(ids[i]): (int(counts[i]), masks[i].reshape(3, 64, 64)) for i in range(k)}
+        return {"global": glob.reshape(3, 64, 64), "active": active, "materials": mats}
+
     def apply_batches(self, trees, batches):
         """n apply_batch calls in one batched device pass; returns the changed flags."""
         n = len(trees)

@@ -29,14 +29,15 @@ BUDGET = 8 << 30
 PATCHES = VX_PATCH_P1 | VX_PATCH_P2
 
 
-def make_world():
-    """Dense u16 grids per depth ([512][s][s][s]) and the items' edit records (deepest first)."""
-    grids = {d: W.dune_world_chunks(32, 16, depth=d, seed=1234 + d, dtype=np.uint16, **W.terrain_params(d))
-             for d in DEPTHS}
+def make_world(per_depth=PER_DEPTH):
+    """Dense u16 grids per depth ([per_depth][s][s][s]) and the items' edit records (deepest first)."""
+    nz = max(1, per_depth // 32)
+    grids = {d: W.dune_world_chunks(per_depth // nz, nz, depth=d, seed=1234 + d, dtype=np.uint16,
+                                    **W.terrain_params(d)) for d in DEPTHS}
     recs, edits = [], []
     i = 0
     for d in DEPTHS:
-        for _ in range(PER_DEPTH):
+        for _ in range(per_depth):
             xyz, vals = W.random_edits(d, DENSITIES[i % 3], 7000 + i, max_material=4095)
             g, sm, cm, vv = W.edits_to_groups(d, xyz, vals)
             recs.append((np.full(len(g), i, np.uint32), g, sm, cm, vv))
@@ -54,7 +55,8 @@ def run(args):
     lib = gpu_lib()
     dev = torch.device("cuda", 0)
     t0 = time.time()
-    grids_np, recs, edits = make_world()
+    per_depth = getattr(args, "edits_chunks", PER_DEPTH)
+    grids_np, recs, edits = make_world(per_depth)
     gen_s = time.time() - t0
     n = len(recs)
     n_edits = int(sum(len(v) for _, v in edits))
@@ -62,11 +64,12 @@ def run(args):
     R = len(item)
 
     h = C.c_void_p()
-    lib.call("interner_create", C.c_uint64(BUDGET), 16, PATCHES, 0, C.byref(h))
+    budget = max(512 << 20, BUDGET * per_depth // PER_DEPTH)
+    lib.call("interner_create", C.c_uint64(budget), 16, PATCHES, 0, C.byref(h))
     call = lambda name, *a: lib.call(name, h, *a, handle=h)  # noqa: E731
     stream = torch.cuda.Stream(device=dev)
     call("interner_set_stream", C.c_void_p(stream.cuda_stream))
-    depths = np.concatenate([np.full(PER_DEPTH, d, np.uint8) for d in DEPTHS])
+    depths = np.concatenate([np.full(per_depth, d, np.uint8) for d in DEPTHS])
     trees = np.zeros(n, np.uint32)
     call("trees_create", n, depths.ctypes.data, trees.ctypes.data)
 
@@ -88,8 +91,8 @@ def run(args):
         call("interner_reset")
         off = 0
         for d in DEPTHS:
-            call("build_dense_async", PER_DEPTH, C.c_void_p(t_d.data_ptr() + 4 * off), P(g_d[d]), None, d)
-            off += PER_DEPTH
+            call("build_dense_async", per_depth, C.c_void_p(t_d.data_ptr() + 4 * off), P(g_d[d]), None, d)
+            off += per_depth
         call("interner_sync")
 
     def apply_all():
@@ -118,19 +121,21 @@ def run(args):
     call("profile_enable", 1)
     call("profile_collect", prof_ms, prof_n)
     ms = []
-    launches0 = lib.kernel_launches()
+    launches = 0
     phases = {}
     for _ in range(args.steps):
         call("profile_enable", 0)
         rebuild()
         call("profile_enable", 1)
+        l0 = lib.kernel_launches()
         ms.append(timed(apply_all))
+        launches += lib.kernel_launches() - l0
         call("interner_sync")
         call("profile_collect", prof_ms, prof_n)
         for k in range(VX_PROF_N):
             if prof_n[k]:
                 phases[VX_PROF_NAMES[k]] = phases.get(VX_PROF_NAMES[k], 0.0) + prof_ms[k]
-    launches = (lib.kernel_launches() - launches0) / args.steps - 3 * 2  # minus the rebuild launches
+    launches = launches / args.steps
     call("profile_enable", 0)
     apply_ms = statistics.median(ms)
     from ._abi import vx_interner_stats
@@ -192,13 +197,13 @@ def run(args):
     ol = B.oracle_lib()
     oh = C.c_void_p()
     ol.call("interner_create", C.c_uint64(1 << 30), 16, PATCHES, 0, C.byref(oh))
-    sample = [k * PER_DEPTH + j for k in range(len(DEPTHS)) for j in (0, 2)]
+    sample = [k * per_depth + j for k in range(len(DEPTHS)) for j in (0, 2)]
     cpu_s, cpu_edits = 0.0, 0
     for i in sample:
         out = C.c_uint32()
         ol.call("tree_create", oh, int(depths[i]), C.byref(out))
         d = int(depths[i])
-        g = np.ascontiguousarray(grids_np[d][i % PER_DEPTH])
+        g = np.ascontiguousarray(grids_np[d][i % per_depth])
         tr = np.array([out.value], np.uint32)
         ol.call("build_dense", oh, 1, C.c_void_p(tr.ctypes.data), C.c_void_p(g.ctypes.data), None, 0)
         b = Batch(d, 16, PATCHES, lib=ol)
@@ -220,7 +225,7 @@ def run(args):
         "vs_baseline": None, "dtype": "u16", "data": "synthetic",
         "config": {"workload": "uneven batched edits: 1536 chunks u16 (512 each MaxDepth 7/6/5), one batch per chunk "
                                "at density 0.001/0.01/0.1, 85% set / 15% clear, P1+P2",
-                   "edits": n_edits, "touched_groups": R, "chunks": n, "budget_bytes": BUDGET,
+                   "edits": n_edits, "touched_groups": R, "chunks": n, "budget_bytes": budget,
                    "l2": "inputs and records larger than L2 (records %.0f MB)" % (R * 26 / 1e6)},
         "chunks_per_s": n / (apply_ms * 1e-3),
         "autotune": tune,

@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(512) bottom_kernel(DevInterner I, ApplyArgs a)
             }
         }
         bool created;
-        const uint64_t id = warp_intern_branch(I, want_branch, c, types, mask, lod, &created);
+        const uint64_t id = warp_intern_branch_inl(I, want_branch, c, types, mask, lod, &created);
         if (want_branch) out = id;
         if (r < a.n_records) {
             a.flags[r] = changed;
@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a
             }
             }
         bool created;
-        const uint64_t id = warp_intern_branch(I, want_branch, c, types, mask, lod, &created);
+        const uint64_t id = warp_intern_branch_inl(I, want_branch, c, types, mask, lod, &created);
         if (!in) continue;
         if (want_branch) {
             out = id;

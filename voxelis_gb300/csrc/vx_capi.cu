@@ -1571,6 +1571,72 @@ int vx_trees_to_dense(vx_interner *it, uint32_t n, const vx_tree *trees, void *o
     return sync_and_check(it);
 }
 
+int vx_occupancy_masks(vx_interner *it, uint32_t n_trees, const vx_tree *trees, const uint32_t *offsets,
+                       uint64_t *global, uint64_t *active, uint32_t max_materials, uint32_t *n_materials,
+                       uint32_t *material_ids, uint64_t *material_counts, uint64_t *material_masks) {
+    if (!it || !n_trees || !trees || !offsets || !global || !active || !n_materials ||
+        (max_materials && (!material_ids || !material_counts || !material_masks)))
+        return VX_E_INVALID_ARG;
+    const int d = tree_ok(it, trees[0]) ? (int)it->tree_depth[trees[0]] : -1;
+    if (d < 1 || d > 6) return set_err(it, VX_E_INVALID_ARG, "occupancy masks need trees of MaxDepth 1..6");
+    const uint32_t S = 1u << d;
+    for (uint32_t k = 0; k < n_trees; ++k) {
+        if (!tree_ok(it, trees[k]) || it->tree_depth[trees[k]] != d)
+            return set_err(it, VX_E_INVALID_ARG, "trees of one builder share a MaxDepth");
+        for (int a = 0; a < 3; ++a)
+            if (offsets[3 * k + a] > 64 - S) return set_err(it, VX_E_OOB, "tree outside the 64^3 builder");
+    }
+    const size_t vb = it->vbits / 8;
+    const uint32_t n_values = 1u << it->vbits;
+    const size_t per = (size_t)S * S * S * vb;
+    const size_t plane = 3 * 4096;
+    VX_CUDA(it->staging.reserve(Carve::need({(size_t)n_trees * 4, (size_t)n_trees * 12, per * n_trees,
+                                             (size_t)n_values * 8, (size_t)n_values * 4, (size_t)n_values * 4,
+                                             (size_t)n_values * 8, 64, plane * 8, 64,
+                                             (size_t)max_materials * plane * 8})));
+    Carve c(it->staging.p);
+    uint32_t *dt = c.take<uint32_t>(n_trees);
+    uint32_t *doff = c.take<uint32_t>((size_t)n_trees * 3);
+    uint8_t *dg = c.take<uint8_t>(per * n_trees);
+    unsigned long long *counts = c.take<unsigned long long>(n_values);
+    uint32_t *slot = c.take<uint32_t>(n_values);
+    uint32_t *ids = c.take<uint32_t>(n_values);
+    unsigned long long *mcounts = c.take<unsigned long long>(n_values);
+    uint32_t *nm = c.take<uint32_t>(16);
+    unsigned long long *dglobal = c.take<unsigned long long>(plane);
+    unsigned long long *dactive = c.take<unsigned long long>(8);
+    unsigned long long *dmat = c.take<unsigned long long>((size_t)max_materials * plane);
+    cudaStream_t s = it->stream;
+    VX_CUDA(cudaMemcpyAsync(dt, trees, (size_t)n_trees * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(doff, offsets, (size_t)n_trees * 12, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemsetAsync(counts, 0, (size_t)n_values * 8, s));
+    VX_CUDA(cudaMemsetAsync(dglobal, 0, plane * 8, s));
+    if (max_materials) VX_CUDA(cudaMemsetAsync(dmat, 0, (size_t)max_materials * plane * 8, s));
+    {
+        Phase ph(it, VX_PROF_GET);
+        const int lc = d < 5 ? d : 5;
+        VX_CUDA(launch_to_dense(it->dev, dt, d, 0, (uint64_t)n_trees << (3 * (d - lc)), dg, it->num_sms, s));
+        VX_CUDA(launch_occupancy(it->dev, dg, n_trees, d, doff, counts, slot, ids, mcounts, nm, max_materials,
+                                 dglobal, dmat, dactive, it->num_sms, s));
+    }
+    uint32_t n_mat = 0;
+    VX_CUDA(cudaMemcpyAsync(&n_mat, nm, 4, cudaMemcpyDeviceToHost, s));
+    VX_CUDA(cudaMemcpyAsync(global, dglobal, plane * 8, cudaMemcpyDeviceToHost, s));
+    VX_CUDA(cudaMemcpyAsync(active, dactive, 48, cudaMemcpyDeviceToHost, s));
+    int st = sync_and_check(it);
+    if (st != VX_OK) return st;
+    *n_materials = n_mat;
+    const uint32_t k = std::min(n_mat, max_materials);
+    if (k) {
+        VX_CUDA(cudaMemcpyAsync(material_ids, ids, (size_t)k * 4, cudaMemcpyDeviceToHost, s));
+        VX_CUDA(cudaMemcpyAsync(material_counts, mcounts, (size_t)k * 8, cudaMemcpyDeviceToHost, s));
+        VX_CUDA(cudaMemcpyAsync(material_masks, dmat, (size_t)k * plane * 8, cudaMemcpyDeviceToHost, s));
+        st = sync_and_check(it);
+        if (st != VX_OK) return st;
+    }
+    return n_mat > max_materials ? set_err(it, VX_E_BUFFER, "more materials than max_materials") : VX_OK;
+}
+
 int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid) {
     return vx_trees_to_dense(it, 1, &tree, out_grid, VX_MEM_HOST);
 }

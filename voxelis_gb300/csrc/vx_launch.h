@@ -114,6 +114,12 @@ cudaError_t launch_get_many(const DevInterner &I, uint64_t n, const uint32_t *tr
 size_t to_dense_smem_bytes(int d, int vbits);
 cudaError_t launch_to_dense(const DevInterner &I, const uint32_t *trees, int d, uint64_t cube_begin,
                             uint64_t n_cubes, void *out, int num_sms, cudaStream_t s);
+// Occupancy masks of n_trees dense grids of side 2^d placed at offsets (x, y, z) of a 64^3 builder:
+// counts[2^bits] and global/per_mat/active must be zero on entry; slot/ids/mcounts/n_mat are written.
+cudaError_t launch_occupancy(const DevInterner &I, const void *grids, uint32_t n_trees, int d, const uint32_t *offsets,
+                             unsigned long long *counts, uint32_t *slot, uint32_t *ids, unsigned long long *mcounts,
+                             uint32_t *n_mat, uint32_t mat_cap, unsigned long long *global, unsigned long long *per_mat,
+                             unsigned long long *active, int num_sms, cudaStream_t s);
 // Releases the roots listed in `list` (count at ctr->scratch[SC_RELEASE]) with `rounds`
 // breadth-first rounds, using two frontier buffers of `frontier_cap` entries.
 cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,

@@ -669,6 +669,124 @@ __global__ void __launch_bounds__(kDenseOutThreads) to_dense_kernel(DevInterner 
 }  // namespace
 
 
+// ---- occupancy masks for greedy meshing (utils/mesh.rs:418-597) ----------------------------------
+// From the trees' dense grids ([tree][y][z][x], side 2^d <= 64): voxel counts per value, the sorted
+// list of present values, then the bits of every non-default voxel in the 64^3 builder's three
+// planes (YZ [y][z] -> x bits, XZ [z][x] -> y bits, XY [y][x] -> z bits), globally and per material.
+// OR-ing voxel bits equals fill_masks_for_region's region fills (each region is a cube of voxels).
+constexpr uint32_t kOccAll = 3 * 64 * 64;
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) occupancy_hist_kernel(const T *grids, uint64_t n_vox,
+                                                                   unsigned long long *counts) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_vox; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const uint32_t v = i < n_vox ? (uint32_t)grids[i] : 0u;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, v);
+        if (v != 0 && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(counts + v, (unsigned long long)__popc(peers));
+    }
+}
+
+// One CTA: slot[v] = rank of v among the present values (ascending), or ~0u.
+__global__ void __launch_bounds__(1024) occupancy_index_kernel(const unsigned long long *counts, uint32_t n_values,
+                                                               uint32_t *slot, uint32_t *ids,
+                                                               unsigned long long *mcounts, uint32_t *n_out) {
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (n_values + blockDim.x - 1) / blockDim.x;
+    const uint32_t v0 = threadIdx.x * per;
+    uint32_t c = 0;
+    for (uint32_t v = v0; v < v0 + per && v < n_values; ++v) c += (v != 0 && counts[v] != 0) ? 1u : 0u;
+    part[threadIdx.x] = c;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {  // inclusive scan (Hillis-Steele)
+        const uint32_t y = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += y;
+        __syncthreads();
+    }
+    uint32_t r = part[threadIdx.x] - c;
+    for (uint32_t v = v0; v < v0 + per && v < n_values; ++v) {
+        if (v != 0 && counts[v] != 0) {
+            slot[v] = r;
+            ids[r] = v;
+            mcounts[r] = counts[v];
+            ++r;
+        } else {
+            slot[v] = ~0u;
+        }
+    }
+    if (threadIdx.x == blockDim.x - 1) *n_out = part[threadIdx.x];
+}
+
+__device__ __forceinline__ void or_bits_warp(unsigned long long *target, uint64_t bits, bool on) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long key = on ? (unsigned long long)target : ~0ull - lane;
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t lo = __reduce_or_sync(peers, (uint32_t)bits), hi = __reduce_or_sync(peers, (uint32_t)(bits >> 32));
+    if (on && lane == (unsigned)(__ffs(peers) - 1)) atomicOr(target, ((unsigned long long)hi << 32) | lo);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) occupancy_masks_kernel(const T *grids, uint32_t n_trees, int d,
+                                                                   const uint32_t *offsets, const uint32_t *slot,
+                                                                   uint32_t mat_cap, unsigned long long *global,
+                                                                   unsigned long long *per_mat) {
+    const uint32_t S = 1u << d;
+    const uint64_t per_tree = (uint64_t)S * S * S;
+    const uint64_t n_vox = per_tree * n_trees;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_vox; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const bool in = i < n_vox;
+        uint32_t v = 0, X = 0, Y = 0, Z = 0;
+        if (in) {
+            v = (uint32_t)grids[i];
+            const uint32_t t = (uint32_t)(i / per_tree), w = (uint32_t)(i % per_tree);
+            X = offsets[3 * t] + (w & (S - 1));
+            Z = offsets[3 * t + 2] + ((w >> d) & (S - 1));
+            Y = offsets[3 * t + 1] + (w >> (2 * d));
+        }
+        const bool on = in && v != 0;
+        const uint32_t m = on ? slot[v] : ~0u;
+        const bool pm = on && m < mat_cap;
+        unsigned long long *mb = per_mat + (size_t)(pm ? m : 0) * kOccAll;
+        or_bits_warp(global + 0 * 4096 + Y * 64 + Z, 1ull << X, on);   // YZ: x bits
+        or_bits_warp(global + 1 * 4096 + Z * 64 + X, 1ull << Y, on);   // XZ: y bits
+        or_bits_warp(global + 2 * 4096 + Y * 64 + X, 1ull << Z, on);   // XY: z bits
+        or_bits_warp(mb + 0 * 4096 + Y * 64 + Z, 1ull << X, pm);
+        or_bits_warp(mb + 1 * 4096 + Z * 64 + X, 1ull << Y, pm);
+        or_bits_warp(mb + 2 * 4096 + Y * 64 + X, 1ull << Z, pm);
+    }
+}
+
+// active[0..5] (mesh.rs:453-463): the occupied y, z, z, x, y, x coordinates.
+__global__ void __launch_bounds__(kThreads) occupancy_active_kernel(const unsigned long long *global,
+                                                                    unsigned long long *active) {
+    __shared__ unsigned long long acc[3];
+    if (threadIdx.x < 3) acc[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long xs = 0, ys = 0, zs = 0;
+    for (uint32_t k = threadIdx.x; k < 4096; k += blockDim.x) {
+        xs |= global[k];         // YZ words hold x bits
+        ys |= global[4096 + k];  // XZ words hold y bits
+        zs |= global[8192 + k];  // XY words hold z bits
+    }
+    atomicOr(&acc[0], xs);
+    atomicOr(&acc[1], ys);
+    atomicOr(&acc[2], zs);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        active[0] = acc[1];  // YZ rows: y
+        active[1] = acc[2];  // YZ cols: z
+        active[2] = acc[2];  // XZ rows: z
+        active[3] = acc[0];  // XZ cols: x
+        active[4] = acc[1];  // XY rows: y
+        active[5] = acc[0];  // XY cols: x
+    }
+}
+
 size_t to_dense_smem_bytes(int d, int vbits) {
     const int lc = d < 5 ? d : 5;
     const size_t tile = ((size_t)1 << (3 * lc)) * (vbits / 8);
@@ -695,6 +813,30 @@ cudaError_t launch_to_dense(const DevInterner &I, const uint32_t *trees, int d, 
         to_dense_kernel<uint16_t><<<(unsigned)blocks, kDenseOutThreads, smem, s>>>(I, trees, d, lc, cube_begin,
                                                                                    n_cubes, (uint16_t *)out);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy(const DevInterner &I, const void *grids, uint32_t n_trees, int d, const uint32_t *offsets,
+                             unsigned long long *counts, uint32_t *slot, uint32_t *ids, unsigned long long *mcounts,
+                             uint32_t *n_mat, uint32_t mat_cap, unsigned long long *global, unsigned long long *per_mat,
+                             unsigned long long *active, int num_sms, cudaStream_t s) {
+    const uint64_t n_vox = ((uint64_t)n_trees) << (3 * d);
+    uint64_t blocks = (n_vox + kThreads - 1) / kThreads;
+    if (blocks > (uint64_t)num_sms * 16) blocks = (uint64_t)num_sms * 16;
+    const uint32_t n_values = 1u << I.vbits;
+    count_launches(4);
+    if (I.vbits == 8)
+        occupancy_hist_kernel<uint8_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint8_t *)grids, n_vox, counts);
+    else
+        occupancy_hist_kernel<uint16_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint16_t *)grids, n_vox, counts);
+    occupancy_index_kernel<<<1, 1024, 0, s>>>(counts, n_values, slot, ids, mcounts, n_mat);
+    if (I.vbits == 8)
+        occupancy_masks_kernel<uint8_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint8_t *)grids, n_trees, d,
+                                                                             offsets, slot, mat_cap, global, per_mat);
+    else
+        occupancy_masks_kernel<uint16_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint16_t *)grids, n_trees, d,
+                                                                              offsets, slot, mat_cap, global, per_mat);
+    occupancy_active_kernel<<<1, kThreads, 0, s>>>(global, active);
     return cudaGetLastError();
 }
 
