@@ -250,6 +250,31 @@ int vx_occupancy_masks(vx_interner *it, uint32_t n_trees, const vx_tree *trees, 
                        uint64_t *global, uint64_t *active, uint32_t max_materials, uint32_t *n_materials,
                        uint32_t *material_ids, uint64_t *material_counts, uint64_t *material_masks);
 
+/* Batched, asynchronous form of vx_occupancy_masks for 8-bit voxels, all arguments in device
+ * memory: tree t goes to builder builder_of[t] at offsets[3t..3t+2]; every tree has MaxDepth
+ * max_depth. Outputs are indexed by builder b: global[b][3 * 4096], active[b][6], n_materials[b],
+ * material_ids[b][max_materials], material_counts[b][max_materials],
+ * material_masks[b][max_materials][3 * 4096] (materials beyond max_materials are counted in
+ * n_materials[b] but not stored). A tree outside its builder or a builder index >= n_builders
+ * reports VX_E_OOB at the next sync. */
+int vx_occupancy_masks_async(vx_interner *it, uint32_t n_builders, uint32_t n_trees, const vx_tree *trees_dev,
+                             const uint32_t *builder_of_dev, const uint32_t *offsets_dev, int max_depth,
+                             uint32_t max_materials, uint64_t *global_dev, uint64_t *active_dev,
+                             uint32_t *n_materials_dev, uint32_t *material_ids_dev, uint64_t *material_counts_dev,
+                             uint64_t *material_masks_dev);
+
+/* Model serialisation (VoxModel::serialize, world/voxmodel.rs:177-282, with serialize_chunk,
+ * world/voxchunk.rs:382-405, for each chunk): the interner's live leaves and branches renumbered in
+ * slot-index order (leaves 1..L, then branches), written as
+ *   u32 L, L x (varint id, value), u32 B, B x (varint id, u8 mask, varint child ids, LOD value),
+ *   u32 n_chunks, n_chunks x ("VoxTreeChunk", i32 x, y, z, varint root id)
+ * (u32/i32/values big-endian, varints LEB128), chunk k = trees[k] at positions[3k..3k+2] in the given
+ * order. This is the payload of a VTM file; the file header, MD5 and zstd stage of
+ * export_model_to_vtm (io/export.rs:90-151) are not included. With out == NULL only *size is set;
+ * VX_E_BUFFER when capacity < *size. */
+int vx_serialize_model(vx_interner *it, uint32_t n_chunks, const vx_tree *trees, const int32_t *positions,
+                       uint8_t *out, uint64_t capacity, uint64_t *size);
+
 /* ---- verification helpers (not on the timed path) ---------------------------------------- */
 /* Canonical DFS export of the DAG reachable from `trees` (see vx_canonical). On VX_E_BUFFER
  * *n_nodes holds the required capacity. */

@@ -325,6 +325,11 @@ class Interner {
     size_t capacity() const { return capacity_; }
     uint32_t next_index() const { return next_index_; }
     size_t free_count() const { return free_indices_.size(); }
+    // The ids of the interned patterns: kind 0 branches (including EMPTY), 1 leaves (mod.rs:1031-1038).
+    template <class F>
+    void for_each_pattern(int kind, F f) const {
+        patterns_[kind].for_each([&](uint64_t, uint64_t id) { f(id); });
+    }
     size_t branch_patterns() const { return patterns_[0].size(); }
     size_t leaf_patterns() const { return patterns_[1].size(); }
     uint64_t collisions = 0;  // hash hits whose stored key differs (reference would alias)

@@ -507,6 +507,69 @@ int vxo_occupancy_masks(void *h, uint32_t n_trees, const uint32_t *trees, const 
     });
 }
 
+// VoxModel::serialize (world/voxmodel.rs:177-282) with serialize_chunk (world/voxchunk.rs:382-405)
+// for the given chunks, in the given order; varints as io/varint.rs:5-30.
+static void put_varint(std::vector<uint8_t> &o, uint32_t v) {
+    while (v >= 0x80) {
+        o.push_back((uint8_t)((v & 0x7F) | 0x80));
+        v >>= 7;
+    }
+    o.push_back((uint8_t)v);
+}
+static void put_u32(std::vector<uint8_t> &o, uint32_t v) {
+    for (int s = 24; s >= 0; s -= 8) o.push_back((uint8_t)(v >> s));
+}
+
+int vxo_serialize_model(void *h, uint32_t n_chunks, const uint32_t *trees, const int32_t *positions, uint8_t *out,
+                        uint64_t capacity, uint64_t *size) {
+    return with_interner(h, [&](auto &o) {
+        using T = std::decay_t<decltype(o.it.get_value(0))>;
+        if (!size || (n_chunks && (!trees || !positions))) return VX_E_INVALID_ARG;
+        std::vector<uint64_t> leaves, branches;
+        o.it.for_each_pattern(1, [&](uint64_t id) { leaves.push_back(id); });
+        o.it.for_each_pattern(0, [&](uint64_t id) { branches.push_back(id); });
+        auto by_index = [](uint64_t a, uint64_t b) { return vxo::bid::index(a) < vxo::bid::index(b); };
+        std::sort(leaves.begin(), leaves.end(), by_index);
+        std::sort(branches.begin(), branches.end(), by_index);
+        std::unordered_map<uint32_t, uint32_t> id_map;
+        id_map[0] = 0;
+        uint32_t next = 1;
+        for (uint64_t id : leaves) id_map[vxo::bid::index(id)] = next++;
+        for (uint64_t id : branches)
+            if (vxo::bid::index(id) != 0) id_map[vxo::bid::index(id)] = next++;
+        std::vector<uint8_t> b;
+        auto put_value = [&](T v) {
+            for (int s = 8 * ((int)sizeof(T) - 1); s >= 0; s -= 8) b.push_back((uint8_t)((uint32_t)v >> s));
+        };
+        put_u32(b, (uint32_t)leaves.size());
+        for (uint64_t id : leaves) {
+            put_varint(b, id_map.at(vxo::bid::index(id)));
+            put_value(o.it.get_value(id));
+        }
+        put_u32(b, (uint32_t)branches.size() - 1);
+        for (uint64_t id : branches) {
+            if (vxo::bid::index(id) == 0) continue;
+            put_varint(b, id_map.at(vxo::bid::index(id)));
+            b.push_back((uint8_t)vxo::bid::mask(id));
+            for (uint64_t c : o.it.get_children(id))
+                if (!vxo::bid::is_empty(c)) put_varint(b, id_map.at(vxo::bid::index(c)));
+            put_value(o.it.get_value(id));
+        }
+        put_u32(b, n_chunks);
+        static const char magic[12] = {'V', 'o', 'x', 'T', 'r', 'e', 'e', 'C', 'h', 'u', 'n', 'k'};
+        for (uint32_t k = 0; k < n_chunks; ++k) {
+            b.insert(b.end(), magic, magic + 12);
+            for (int a = 0; a < 3; ++a) put_u32(b, (uint32_t)positions[3 * k + a]);
+            put_varint(b, id_map.at(vxo::bid::index(o.tree(trees[k])->root())));
+        }
+        *size = b.size();
+        if (!out) return VX_OK;
+        if (capacity < b.size()) return fail(&o, VX_E_BUFFER, "output buffer smaller than the serialised model");
+        std::copy(b.begin(), b.end(), out);
+        return VX_OK;
+    });
+}
+
 // The UB fence: every child reachable from the trees has a matching generation and a positive
 // refcount.
 int vxo_validate(void *h, uint32_t n, const uint32_t *trees) {

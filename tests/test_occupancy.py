@@ -90,3 +90,51 @@ def test_gpu_occupancy_matches_oracle(oracle_lib, gpu_lib):
             it.build_dense(trees, np.stack(grids)) if d >= 2 else None
             res.append(it.occupancy_masks(trees, offs))
         same(res[0], res[1])
+
+
+@pytest.mark.gpu
+def test_batched_builders_equal_one_call_per_builder(gpu_lib):
+    import ctypes as C
+
+    import torch
+
+    it = VoxInterner(64 << 20, 8, VX_PATCH_P1, lib=gpu_lib)
+    grids = W.dune_world_chunks(4, 4, depth=5, seed=8)
+    trees = [VoxTree(5) for _ in range(16)]
+    it.build_dense(trees, grids)
+    # builder b takes chunks 4b .. 4b+3 at the four x/z quadrants; builder 4 stays empty
+    n_b, mm = 5, 8
+    builder_of = np.repeat(np.arange(4, dtype=np.uint32), 4)
+    offs = np.array([(32 * (k & 1), 0, 32 * (k >> 1)) for k in range(4)] * 4, np.uint32)
+    handles = np.array([t._bind(it) for t in trees], np.uint32)
+    dev = torch.device("cuda", 0)
+    T = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(dev)  # noqa: E731
+    t_d, b_d, o_d = T(handles), T(builder_of), T(offs.ravel().copy())
+    glob = torch.zeros(n_b * 3 * 4096, dtype=torch.int64, device=dev)
+    act = torch.zeros(n_b * 6, dtype=torch.int64, device=dev)
+    nm = torch.zeros(n_b, dtype=torch.int32, device=dev)
+    ids = torch.zeros(n_b * mm, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(n_b * mm, dtype=torch.int64, device=dev)
+    masks = torch.zeros(n_b * mm * 3 * 4096, dtype=torch.int64, device=dev)
+    P = lambda x: C.c_void_p(x.data_ptr())  # noqa: E731
+    torch.cuda.synchronize()
+    it._call("occupancy_masks_async", n_b, 16, P(t_d), P(b_d), P(o_d), 5, mm, P(glob), P(act), P(nm), P(ids), P(cnt),
+             P(masks))
+    it.sync()
+    glob = glob.cpu().numpy().view(np.uint64).reshape(n_b, 3, 64, 64)
+    act = act.cpu().numpy().view(np.uint64).reshape(n_b, 6)
+    nm, ids = nm.cpu().numpy(), ids.cpu().numpy().reshape(n_b, mm)
+    cnt = cnt.cpu().numpy().reshape(n_b, mm)
+    masks = masks.cpu().numpy().view(np.uint64).reshape(n_b, mm, 3, 64, 64)
+    for b in range(n_b):
+        sel = [k for k in range(16) if builder_of[k] == b]
+        if not sel:
+            assert nm[b] == 0 and not glob[b].any() and not act[b].any()
+            continue
+        one = it.occupancy_masks([trees[k] for k in sel], offs[sel], max_materials=mm)
+        np.testing.assert_array_equal(glob[b], one["global"])
+        np.testing.assert_array_equal(act[b], one["active"])
+        assert nm[b] == len(one["materials"])
+        for k, m in enumerate(sorted(one["materials"])):
+            assert ids[b, k] == m and cnt[b, k] == one["materials"][m][0]
+            np.testing.assert_array_equal(masks[b, k], one["materials"][m][1])

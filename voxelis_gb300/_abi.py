@@ -133,6 +133,7 @@ SIGNATURES = {
     "tree_to_dense": [_P, _U32, _P],
     "validate": [_P, _U32, _P],
     "occupancy_masks": [_P, _U32, _P, _P, _P, _P, _U32, _P, _P, _P, _P],
+    "serialize_model": [_P, _U32, _P, _P, _P, _U64, _PU64],
 }
 
 # entry points only the GPU library has
@@ -152,6 +153,7 @@ GPU_SIGNATURES = {
     "tune_get": [_P, _PI, _PI],
     "trees_to_dense": [_P, _U32, _P, _P, _I],
     "trees_to_dense_async": [_P, _U32, _P, _I, _P],
+    "occupancy_masks_async": [_P, _U32, _U32, _P, _P, _P, _I, _U32, _P, _P, _P, _P, _P, _P],
 }
 
 

@@ -149,6 +149,17 @@ class VoxInterner:
         mats = {int(ids[i]): (int(counts[i]), masks[i].reshape(3, 64, 64)) for i in range(k)}
         return {"global": glob.reshape(3, 64, 64), "active": active, "materials": mats}
 
+    def serialize_model(self, trees, positions):
+        """VoxModel::serialize payload (world/voxmodel.rs:177-282) for chunks trees[k] at positions[k]."""
+        handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)
+        pos = np.ascontiguousarray(positions, dtype=np.int32).reshape(-1, 3)
+        size = C.c_uint64()
+        self._call("serialize_model", len(trees), _np_ptr(handles), _np_ptr(pos), None, C.c_uint64(0), C.byref(size))
+        out = np.zeros(size.value, np.uint8)
+        self._call("serialize_model", len(trees), _np_ptr(handles), _np_ptr(pos), _np_ptr(out),
+                   C.c_uint64(size.value), C.byref(size))
+        return out.tobytes()
+
     def apply_batches(self, trees, batches):
         """n apply_batch calls in one batched device pass; returns the changed flags."""
         n = len(trees)

@@ -1637,6 +1637,80 @@ int vx_occupancy_masks(vx_interner *it, uint32_t n_trees, const vx_tree *trees, 
     return n_mat > max_materials ? set_err(it, VX_E_BUFFER, "more materials than max_materials") : VX_OK;
 }
 
+int vx_occupancy_masks_async(vx_interner *it, uint32_t n_builders, uint32_t n_trees, const vx_tree *trees_dev,
+                             const uint32_t *builder_of_dev, const uint32_t *offsets_dev, int max_depth,
+                             uint32_t max_materials, uint64_t *global_dev, uint64_t *active_dev,
+                             uint32_t *n_materials_dev, uint32_t *material_ids_dev, uint64_t *material_counts_dev,
+                             uint64_t *material_masks_dev) {
+    if (!it || !n_builders || !n_trees || !trees_dev || !builder_of_dev || !offsets_dev || !global_dev || !active_dev ||
+        !n_materials_dev || (max_materials && (!material_ids_dev || !material_counts_dev || !material_masks_dev)))
+        return VX_E_INVALID_ARG;
+    if (it->vbits != 8) return set_err(it, VX_E_UNSUPPORTED, "the batched occupancy masks take 8-bit voxels");
+    if (max_depth < 1 || max_depth > 6) return set_err(it, VX_E_INVALID_ARG, "occupancy masks need MaxDepth 1..6");
+    const size_t per = (size_t)1 << (3 * max_depth);
+    const size_t plane = 3 * 4096;
+    VX_CUDA(it->ws.reserve(Carve::need({per * n_trees, (size_t)n_builders * 256 * 4, (size_t)n_builders * 256 * 4})));
+    Carve c(it->ws.p);
+    uint8_t *dg = c.take<uint8_t>(per * n_trees);
+    unsigned int *counts = c.take<unsigned int>((size_t)n_builders * 256);
+    uint32_t *slot = c.take<uint32_t>((size_t)n_builders * 256);
+    cudaStream_t s = it->stream;
+    VX_CUDA(cudaMemsetAsync(counts, 0, (size_t)n_builders * 256 * 4, s));
+    VX_CUDA(cudaMemsetAsync(global_dev, 0, (size_t)n_builders * plane * 8, s));
+    if (max_materials) VX_CUDA(cudaMemsetAsync(material_masks_dev, 0, (size_t)n_builders * max_materials * plane * 8, s));
+    Phase ph(it, VX_PROF_GET);
+    const int lc = max_depth < 5 ? max_depth : 5;
+    VX_CUDA(launch_to_dense(it->dev, trees_dev, max_depth, 0, (uint64_t)n_trees << (3 * (max_depth - lc)), dg,
+                            it->num_sms, s));
+    VX_CUDA(launch_occupancy_many(it->dev, dg, n_trees, max_depth, builder_of_dev, offsets_dev, n_builders, counts,
+                                  slot, max_materials, material_ids_dev,
+                                  reinterpret_cast<unsigned long long *>(material_counts_dev), n_materials_dev,
+                                  reinterpret_cast<unsigned long long *>(global_dev),
+                                  reinterpret_cast<unsigned long long *>(material_masks_dev),
+                                  reinterpret_cast<unsigned long long *>(active_dev), it->num_sms, s));
+    return VX_OK;
+}
+
+int vx_serialize_model(vx_interner *it, uint32_t n_chunks, const vx_tree *trees, const int32_t *positions,
+                       uint8_t *out, uint64_t capacity, uint64_t *size) {
+    if (!it || !size || (n_chunks && (!trees || !positions))) return VX_E_INVALID_ARG;
+    for (uint32_t k = 0; k < n_chunks; ++k)
+        if (!tree_ok(it, trees[k])) return set_err(it, VX_E_INVALID_ARG, "unknown tree handle");
+    const size_t words = serialize_scratch_words(it->dev);
+    const size_t tmpw = scan_tmp_words(it->capacity) * 4;  // the recursive scan's block sums
+    VX_CUDA(it->ws.reserve(Carve::need({words * 4, tmpw * 4, (size_t)n_chunks * 4 + 4, (size_t)n_chunks * 12 + 4, 64})));
+    Carve c(it->ws.p);
+    uint32_t *w = c.take<uint32_t>(words);
+    uint32_t *tmp = c.take<uint32_t>(tmpw);
+    uint32_t *dt = c.take<uint32_t>((size_t)n_chunks + 1);
+    int32_t *dp = c.take<int32_t>((size_t)n_chunks * 3 + 1);
+    unsigned long long *dtotal = c.take<unsigned long long>(2);
+    cudaStream_t s = it->stream;
+    if (n_chunks) {
+        VX_CUDA(cudaMemcpyAsync(dt, trees, (size_t)n_chunks * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(dp, positions, (size_t)n_chunks * 12, cudaMemcpyHostToDevice, s));
+    }
+    unsigned long long total = 0;
+    {
+        Phase ph(it, VX_PROF_GET);
+        VX_CUDA(launch_serialize_plan(it->dev, w, tmp, n_chunks, dt, dtotal, it->num_sms, s));
+    }
+    VX_CUDA(cudaMemcpyAsync(&total, dtotal, 8, cudaMemcpyDeviceToHost, s));
+    int st = sync_and_check(it);
+    if (st != VX_OK) return st;
+    *size = total;
+    if (!out) return VX_OK;
+    if (capacity < total) return set_err(it, VX_E_BUFFER, "output buffer smaller than the serialised model");
+    VX_CUDA(it->staging.reserve(total + 256));
+    uint8_t *dout = static_cast<uint8_t *>(it->staging.p);
+    {
+        Phase ph(it, VX_PROF_GET);
+        VX_CUDA(launch_serialize_write(it->dev, w, n_chunks, dt, dp, dout, dtotal, it->num_sms, s));
+    }
+    VX_CUDA(cudaMemcpyAsync(out, dout, total, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(it);
+}
+
 int vx_tree_to_dense(vx_interner *it, vx_tree tree, void *out_grid) {
     return vx_trees_to_dense(it, 1, &tree, out_grid, VX_MEM_HOST);
 }

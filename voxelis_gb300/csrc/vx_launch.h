@@ -103,6 +103,7 @@ enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_RE
 
 // Inclusive-to-exclusive scan of n u32 flags (n from the host) into pos; pos[n] = total.
 cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s);
+// Block sums of one scan level; `tmp` must hold 4 x scan_tmp_words(n) words for the recursion.
 size_t scan_tmp_words(uint32_t n);
 
 // ---- reads, releases, single-voxel operations, maintenance (vx_ops.cu) -------------------------
@@ -120,6 +121,22 @@ cudaError_t launch_occupancy(const DevInterner &I, const void *grids, uint32_t n
                              unsigned long long *counts, uint32_t *slot, uint32_t *ids, unsigned long long *mcounts,
                              uint32_t *n_mat, uint32_t mat_cap, unsigned long long *global, unsigned long long *per_mat,
                              unsigned long long *active, int num_sms, cudaStream_t s);
+// Batched occupancy masks, 8-bit voxels: tree t goes to builder builder_of[t]; counts (256 per
+// builder), global, per_mat must be zero on entry.
+cudaError_t launch_occupancy_many(const DevInterner &I, const uint8_t *grids, uint32_t n_trees, int d,
+                                  const uint32_t *builder_of, const uint32_t *offsets, uint32_t n_builders,
+                                  unsigned int *counts, uint32_t *slot, uint32_t max_mat, uint32_t *ids,
+                                  unsigned long long *mcounts, uint32_t *n_mat, unsigned long long *global,
+                                  unsigned long long *per_mat, unsigned long long *active, int num_sms, cudaStream_t s);
+// Model serialisation: plan (renumbering, record sizes, offsets, total bytes into *total), then
+// write (records, counts and chunk records into `out`, which holds *total bytes). `w` holds
+// serialize_scratch_words(I) u32 and is shared by both steps.
+size_t serialize_scratch_words(const DevInterner &I);
+cudaError_t launch_serialize_plan(const DevInterner &I, uint32_t *w, uint32_t *tmp_scan, uint32_t n_chunks,
+                                  const uint32_t *trees, unsigned long long *total, int num_sms, cudaStream_t s);
+cudaError_t launch_serialize_write(const DevInterner &I, uint32_t *w, uint32_t n_chunks, const uint32_t *trees,
+                                   const int32_t *pos, uint8_t *out, unsigned long long *total, int num_sms,
+                                   cudaStream_t s);
 // Releases the roots listed in `list` (count at ctr->scratch[SC_RELEASE]) with `rounds`
 // breadth-first rounds, using two frontier buffers of `frontier_cap` entries.
 cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,

@@ -720,50 +720,151 @@ __global__ void __launch_bounds__(1024) occupancy_index_kernel(const unsigned lo
     if (threadIdx.x == blockDim.x - 1) *n_out = part[threadIdx.x];
 }
 
-__device__ __forceinline__ void or_bits_warp(unsigned long long *target, uint64_t bits, bool on) {
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned long long key = on ? (unsigned long long)target : ~0ull - lane;
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
-    const uint32_t lo = __reduce_or_sync(peers, (uint32_t)bits), hi = __reduce_or_sync(peers, (uint32_t)(bits >> 32));
-    if (on && lane == (unsigned)(__ffs(peers) - 1)) atomicOr(target, ((unsigned long long)hi << 32) | lo);
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) occupancy_masks_kernel(const T *grids, uint32_t n_trees, int d,
-                                                                   const uint32_t *offsets, const uint32_t *slot,
-                                                                   uint32_t mat_cap, unsigned long long *global,
-                                                                   unsigned long long *per_mat) {
-    const uint32_t S = 1u << d;
-    const uint64_t per_tree = (uint64_t)S * S * S;
+// Batched form for 8-bit voxels: tree t belongs to builder builder_of[t]; per-builder value counts
+// (256 bins), ranks, planes and masks, indexed by builder.
+__global__ void __launch_bounds__(kThreads) occupancy_hist_many_kernel(const uint8_t *grids, uint32_t n_trees, int d,
+                                                                        const uint32_t *builder_of, uint32_t n_builders,
+                                                                        unsigned int *counts) {
+    const uint64_t per_tree = 1ull << (3 * d);
     const uint64_t n_vox = per_tree * n_trees;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_vox; base += stride) {
         const uint64_t i = base + threadIdx.x;
         const bool in = i < n_vox;
-        uint32_t v = 0, X = 0, Y = 0, Z = 0;
-        if (in) {
-            v = (uint32_t)grids[i];
-            const uint32_t t = (uint32_t)(i / per_tree), w = (uint32_t)(i % per_tree);
-            X = offsets[3 * t] + (w & (S - 1));
-            Z = offsets[3 * t + 2] + ((w >> d) & (S - 1));
-            Y = offsets[3 * t + 1] + (w >> (2 * d));
-        }
-        const bool on = in && v != 0;
-        const uint32_t m = on ? slot[v] : ~0u;
-        const bool pm = on && m < mat_cap;
-        unsigned long long *mb = per_mat + (size_t)(pm ? m : 0) * kOccAll;
-        or_bits_warp(global + 0 * 4096 + Y * 64 + Z, 1ull << X, on);   // YZ: x bits
-        or_bits_warp(global + 1 * 4096 + Z * 64 + X, 1ull << Y, on);   // XZ: y bits
-        or_bits_warp(global + 2 * 4096 + Y * 64 + X, 1ull << Z, on);   // XY: z bits
-        or_bits_warp(mb + 0 * 4096 + Y * 64 + Z, 1ull << X, pm);
-        or_bits_warp(mb + 1 * 4096 + Z * 64 + X, 1ull << Y, pm);
-        or_bits_warp(mb + 2 * 4096 + Y * 64 + X, 1ull << Z, pm);
+        const uint32_t v = in ? grids[i] : 0u;
+        const uint32_t b = (in && v) ? builder_of[(uint32_t)(i / per_tree)] : 0u;
+        const bool on = in && v && b < n_builders;
+        const uint32_t key = on ? b * 256u + v : 0xFFFFFFFFu - lane;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (on && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(counts + key, (unsigned)__popc(peers));
     }
+}
+
+// One warp per builder: ranks of the present values 1..255 (ascending).
+__global__ void occupancy_index_many_kernel(const unsigned int *counts, uint32_t n_builders, uint32_t *slot,
+                                            uint32_t max_mat, uint32_t *ids, unsigned long long *mcounts,
+                                            uint32_t *n_mat) {
+    const uint32_t b = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const unsigned lane = threadIdx.x & 31u;
+    if (b >= n_builders) return;
+    uint32_t r = 0;
+    for (uint32_t v0 = 0; v0 < 256; v0 += 32) {
+        const uint32_t v = v0 + lane;
+        const unsigned c = counts[b * 256 + v];
+        const bool present = v != 0 && c != 0;
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, present);
+        const uint32_t k = r + __popc(bal & ((1u << lane) - 1u));
+        slot[b * 256 + v] = present ? k : ~0u;
+        if (present && k < max_mat) {
+            ids[(size_t)b * max_mat + k] = v;
+            mcounts[(size_t)b * max_mat + k] = c;
+        }
+        r += __popc(bal);
+    }
+    if (lane == 0) n_mat[b] = r;
+}
+
+// Column form of the mask kernels: one thread per line of a tree's grid (a row along x, a column
+// along y or along z; orientation o = 0, 1, 2 for the YZ, XZ and XY planes), which builds the line's
+// occupancy bits in registers and ORs them into the builder's plane word with one atomic; the same for
+// each material present on the line (up to kLineMats tracked in registers, else every material of the
+// builder in turn).
+constexpr int kLineMats = 6;
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) occupancy_lines_kernel(DevInterner I, const T *grids, uint32_t n_trees,
+                                                                    int d, const uint32_t *builder_of,
+                                                                    uint32_t n_builders, const uint32_t *offsets,
+                                                                    const uint32_t *slot, uint32_t slot_stride,
+                                                                    const uint32_t *n_mat, uint32_t mat_cap,
+                                                                    unsigned long long *global,
+                                                                    unsigned long long *per_mat) {
+    const uint32_t S = 1u << d;
+    const uint64_t lines_per_tree = 3ull * S * S;
+    const uint64_t n_lines = lines_per_tree * n_trees;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_lines; i += stride) {
+        const uint32_t t = (uint32_t)(i / lines_per_tree), w = (uint32_t)(i % lines_per_tree);
+        const uint32_t o = w / (S * S), ab = w % (S * S), a = ab / S, bb = ab % S;
+        const uint32_t b = builder_of ? builder_of[t] : 0u;
+        const uint32_t ox = offsets[3 * t], oy = offsets[3 * t + 1], oz = offsets[3 * t + 2];
+        if (b >= n_builders || ox + S > 64 || oy + S > 64 || oz + S > 64) {
+            bad = true;
+            continue;
+        }
+        const T *g = grids + (uint64_t)t * S * S * S;
+        // line origin and step in the [y][z][x] grid, target word and the line's bit offset
+        uint64_t base, step;
+        uint32_t word, shift;
+        if (o == 0) {  // YZ[y][z] <- x bits: a = y, bb = z
+            base = ((uint64_t)a * S + bb) * S;
+            step = 1;
+            word = 0 * 4096 + (oy + a) * 64 + (oz + bb);
+            shift = ox;
+        } else if (o == 1) {  // XZ[z][x] <- y bits: a = z, bb = x
+            base = (uint64_t)a * S + bb;
+            step = (uint64_t)S * S;
+            word = 1 * 4096 + (oz + a) * 64 + (ox + bb);
+            shift = oy;
+        } else {  // XY[y][x] <- z bits: a = y, bb = x
+            base = (uint64_t)a * S * S + bb;
+            step = S;
+            word = 2 * 4096 + (oy + a) * 64 + (ox + bb);
+            shift = oz;
+        }
+        uint64_t occ = 0;
+        uint32_t mv[kLineMats];
+        uint64_t mm[kLineMats];
+        int nm = 0;
+        bool overflow = false;
+        for (uint32_t k = 0; k < S; ++k) {
+            const uint32_t v = g[base + k * step];
+            if (!v) continue;
+            occ |= 1ull << k;
+            int j = 0;
+            while (j < nm && mv[j] != v) ++j;
+            if (j == nm) {
+                if (nm < kLineMats) {
+                    mv[nm] = v;
+                    mm[nm] = 0;
+                    ++nm;
+                } else {
+                    overflow = true;
+                    continue;
+                }
+            }
+            mm[j] |= 1ull << k;
+        }
+        if (!occ) continue;
+        unsigned long long *gb = global + (size_t)b * kOccAll;
+        atomicOr(gb + word, (unsigned long long)(occ << shift));
+        if (!overflow) {
+            for (int j = 0; j < nm; ++j) {
+                const uint32_t m = slot[(size_t)b * slot_stride + mv[j]];
+                if (m < mat_cap) atomicOr(per_mat + ((size_t)b * mat_cap + m) * kOccAll + word, (unsigned long long)(mm[j] << shift));
+            }
+        } else {  // more materials on this line than tracked: one pass per material of the builder
+            const uint32_t nmb = n_mat[b] < mat_cap ? n_mat[b] : mat_cap;
+            for (uint32_t m = 0; m < nmb; ++m) {
+                uint64_t bits = 0;
+                for (uint32_t k = 0; k < S; ++k) {
+                    const uint32_t v = g[base + k * step];
+                    if (v && slot[(size_t)b * slot_stride + v] == m) bits |= 1ull << k;
+                }
+                if (bits) atomicOr(per_mat + ((size_t)b * mat_cap + m) * kOccAll + word, (unsigned long long)(bits << shift));
+            }
+        }
+    }
+    if (bad) set_error(I, ERR_OOB, 54);
 }
 
 // active[0..5] (mesh.rs:453-463): the occupied y, z, z, x, y, x coordinates.
 __global__ void __launch_bounds__(kThreads) occupancy_active_kernel(const unsigned long long *global,
                                                                     unsigned long long *active) {
+    global += (size_t)blockIdx.x * kOccAll;  // one CTA per builder
+    active += (size_t)blockIdx.x * 6;
     __shared__ unsigned long long acc[3];
     if (threadIdx.x < 3) acc[threadIdx.x] = 0;
     __syncthreads();
@@ -785,6 +886,127 @@ __global__ void __launch_bounds__(kThreads) occupancy_active_kernel(const unsign
         active[4] = acc[1];  // XY rows: y
         active[5] = acc[0];  // XY cols: x
     }
+}
+
+// ---- model serialisation (VoxModel::serialize, world/voxmodel.rs:177-282; serialize_chunk,
+// world/voxchunk.rs:382-405) ------------------------------------------------------------------------
+// Live leaves and live branches other than EMPTY are renumbered in slot-index order (leaves 1..L,
+// then branches L+1..), each record's byte length is computed in parallel, exclusive scans place
+// the records, and every node writes its own record: varint(new id) then the value (leaves), or
+// varint(new id), mask, varint(new id) of each non-empty child and the LOD value (branches); values
+// big-endian. Chunk records: "VoxTreeChunk", position (3 x i32 BE), varint(new id of the root).
+__device__ __forceinline__ uint32_t varint_len(uint32_t v) {
+    uint32_t n = 1;
+    while (v >= 0x80u) {
+        v >>= 7;
+        ++n;
+    }
+    return n;
+}
+
+__device__ __forceinline__ uint8_t *put_varint(uint8_t *p, uint32_t v) {
+    while (v >= 0x80u) {
+        *p++ = (uint8_t)((v & 0x7Fu) | 0x80u);
+        v >>= 7;
+    }
+    *p++ = (uint8_t)v;
+    return p;
+}
+
+__device__ __forceinline__ uint8_t *put_value_be(uint8_t *p, uint32_t v, int vb) {
+    if (vb == 2) *p++ = (uint8_t)(v >> 8);
+    *p++ = (uint8_t)v;
+    return p;
+}
+
+__global__ void ser_classify_kernel(DevInterner I, uint32_t *leaf_flag, uint32_t *branch_flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < I.capacity; i += gridDim.x * blockDim.x) {
+        const uint64_t id = I.ids[i];
+        leaf_flag[i] = (id != 0 && id_is_leaf(id)) ? 1u : 0u;
+        branch_flag[i] = (id != 0 && !id_is_leaf(id) && i != 0) ? 1u : 0u;
+    }
+}
+
+__global__ void ser_newid_kernel(DevInterner I, const uint32_t *leaf_flag, const uint32_t *leaf_rank,
+                                 const uint32_t *branch_flag, const uint32_t *branch_rank, uint32_t *new_id) {
+    const uint32_t L = leaf_rank[I.capacity];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < I.capacity; i += gridDim.x * blockDim.x)
+        new_id[i] = leaf_flag[i] ? leaf_rank[i] + 1 : (branch_flag[i] ? L + 1 + branch_rank[i] : 0u);
+}
+
+__global__ void ser_size_kernel(DevInterner I, const uint32_t *leaf_flag, const uint32_t *branch_flag,
+                                const uint32_t *new_id, uint32_t *leaf_size, uint32_t *branch_size) {
+    const int vb = I.vbits / 8;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < I.capacity; i += gridDim.x * blockDim.x) {
+        uint32_t ls = 0, bs = 0;
+        if (leaf_flag[i]) ls = varint_len(new_id[i]) + vb;
+        if (branch_flag[i]) {
+            bs = varint_len(new_id[i]) + 1 + vb;
+            const uint64_t *c = I.children + 8ull * i;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (c[k] != EMPTY_ID) bs += varint_len(new_id[id_index(c[k])]);
+        }
+        leaf_size[i] = ls;
+        branch_size[i] = bs;
+    }
+}
+
+// out = [u32 L][leaf records][u32 B][branch records][u32 n_chunks][chunk records]
+__global__ void ser_write_kernel(DevInterner I, const uint32_t *leaf_flag, const uint32_t *leaf_off,
+                                 const uint32_t *branch_flag, const uint32_t *branch_off, const uint32_t *new_id,
+                                 uint8_t *out) {
+    const int vb = I.vbits / 8;
+    const uint64_t leaf_base = 4, branch_base = 8 + (uint64_t)leaf_off[I.capacity];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < I.capacity; i += gridDim.x * blockDim.x) {
+        if (leaf_flag[i]) {
+            uint8_t *p = out + leaf_base + leaf_off[i];
+            p = put_varint(p, new_id[i]);
+            put_value_be(p, node_value(I, i), vb);
+        } else if (branch_flag[i]) {
+            uint8_t *p = out + branch_base + branch_off[i];
+            const uint64_t id = I.ids[i];
+            p = put_varint(p, new_id[i]);
+            *p++ = (uint8_t)id_mask(id);
+            const uint64_t *c = I.children + 8ull * i;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (c[k] != EMPTY_ID) p = put_varint(p, new_id[id_index(c[k])]);
+            put_value_be(p, node_value(I, i), vb);
+        }
+    }
+}
+
+__device__ __forceinline__ void put_u32_be(uint8_t *p, uint32_t v) {
+    p[0] = (uint8_t)(v >> 24);
+    p[1] = (uint8_t)(v >> 16);
+    p[2] = (uint8_t)(v >> 8);
+    p[3] = (uint8_t)v;
+}
+
+// One thread: the three counts, then the chunk records in the caller's order.
+__global__ void ser_tail_kernel(DevInterner I, const uint32_t *leaf_rank, const uint32_t *branch_rank,
+                                const uint32_t *leaf_off, const uint32_t *branch_off, const uint32_t *new_id,
+                                uint32_t n_chunks, const uint32_t *trees, const int32_t *pos, uint8_t *out,
+                                unsigned long long *total) {
+    const uint32_t L = leaf_rank[I.capacity], B = branch_rank[I.capacity];
+    put_u32_be(out, L);
+    const uint64_t bh = 4 + (uint64_t)leaf_off[I.capacity];
+    put_u32_be(out + bh, B);  // branch_patterns without EMPTY (the reference writes its size - 1)
+    uint64_t o = bh + 4 + branch_off[I.capacity];
+    put_u32_be(out + o, n_chunks);
+    o += 4;
+    const char magic[12] = {'V', 'o', 'x', 'T', 'r', 'e', 'e', 'C', 'h', 'u', 'n', 'k'};
+    for (uint32_t k = 0; k < n_chunks; ++k) {
+        for (int j = 0; j < 12; ++j) out[o + j] = (uint8_t)magic[j];
+        o += 12;
+        for (int a = 0; a < 3; ++a) put_u32_be(out + o + 4 * a, (uint32_t)pos[3 * k + a]);
+        o += 12;
+        const uint32_t t = trees[k];
+        const uint64_t root = t < I.tree_cap ? I.roots[t] : EMPTY_ID;
+        o = (uint64_t)(put_varint(out + o, new_id[id_index(root)]) - out);
+    }
+    *total = o;
 }
 
 size_t to_dense_smem_bytes(int d, int vbits) {
@@ -830,13 +1052,95 @@ cudaError_t launch_occupancy(const DevInterner &I, const void *grids, uint32_t n
     else
         occupancy_hist_kernel<uint16_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint16_t *)grids, n_vox, counts);
     occupancy_index_kernel<<<1, 1024, 0, s>>>(counts, n_values, slot, ids, mcounts, n_mat);
+    uint64_t lblocks = ((3ull * n_trees << (2 * d)) + kThreads - 1) / kThreads;
+    if (lblocks > (uint64_t)num_sms * 16) lblocks = (uint64_t)num_sms * 16;
     if (I.vbits == 8)
-        occupancy_masks_kernel<uint8_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint8_t *)grids, n_trees, d,
-                                                                             offsets, slot, mat_cap, global, per_mat);
+        occupancy_lines_kernel<uint8_t><<<(unsigned)lblocks, kThreads, 0, s>>>(
+            I, (const uint8_t *)grids, n_trees, d, nullptr, 1, offsets, slot, 0, n_mat, mat_cap, global, per_mat);
     else
-        occupancy_masks_kernel<uint16_t><<<(unsigned)blocks, kThreads, 0, s>>>((const uint16_t *)grids, n_trees, d,
-                                                                              offsets, slot, mat_cap, global, per_mat);
+        occupancy_lines_kernel<uint16_t><<<(unsigned)lblocks, kThreads, 0, s>>>(
+            I, (const uint16_t *)grids, n_trees, d, nullptr, 1, offsets, slot, 0, n_mat, mat_cap, global, per_mat);
     occupancy_active_kernel<<<1, kThreads, 0, s>>>(global, active);
+    return cudaGetLastError();
+}
+
+// Scratch of the serialisation: nine arrays of capacity + 1 u32.
+size_t serialize_scratch_words(const DevInterner &I) { return 9 * ((size_t)I.capacity + 1) + 64; }
+
+namespace {
+struct SerBufs {
+    uint32_t *leaf_flag, *branch_flag, *leaf_rank, *branch_rank, *new_id, *leaf_size, *branch_size, *leaf_off,
+        *branch_off;
+    SerBufs(uint32_t *w, uint32_t n) {
+        uint32_t **all[9] = {&leaf_flag, &branch_flag, &leaf_rank, &branch_rank, &new_id,
+                             &leaf_size, &branch_size, &leaf_off, &branch_off};
+        for (int k = 0; k < 9; ++k) *all[k] = w + (size_t)k * (n + 1);
+    }
+};
+
+__global__ void ser_total_kernel(DevInterner I, SerBufs b, uint32_t n_chunks, const uint32_t *trees,
+                                 unsigned long long *total) {
+    unsigned long long t = 12ull + b.leaf_off[I.capacity] + b.branch_off[I.capacity];
+    for (uint32_t k = 0; k < n_chunks; ++k) {
+        const uint32_t tr = trees[k];
+        const uint64_t root = tr < I.tree_cap ? I.roots[tr] : EMPTY_ID;
+        t += 24 + varint_len(b.new_id[id_index(root)]);
+    }
+    *total = t;
+}
+}  // namespace
+
+cudaError_t launch_serialize_plan(const DevInterner &I, uint32_t *w, uint32_t *tmp_scan, uint32_t n_chunks,
+                                  const uint32_t *trees, unsigned long long *total, int num_sms, cudaStream_t s) {
+    const uint32_t n = I.capacity;
+    SerBufs b(w, n);
+    const unsigned g = (unsigned)num_sms * 8;
+    count_launches(1);
+    ser_classify_kernel<<<g, kThreads, 0, s>>>(I, b.leaf_flag, b.branch_flag);
+    cudaError_t e = launch_scan(b.leaf_flag, b.leaf_rank, tmp_scan, n, s);
+    if (e == cudaSuccess) e = launch_scan(b.branch_flag, b.branch_rank, tmp_scan, n, s);
+    if (e != cudaSuccess) return e;
+    count_launches(2);
+    ser_newid_kernel<<<g, kThreads, 0, s>>>(I, b.leaf_flag, b.leaf_rank, b.branch_flag, b.branch_rank, b.new_id);
+    ser_size_kernel<<<g, kThreads, 0, s>>>(I, b.leaf_flag, b.branch_flag, b.new_id, b.leaf_size, b.branch_size);
+    e = launch_scan(b.leaf_size, b.leaf_off, tmp_scan, n, s);
+    if (e == cudaSuccess) e = launch_scan(b.branch_size, b.branch_off, tmp_scan, n, s);
+    if (e != cudaSuccess) return e;
+    count_launches(1);
+    ser_total_kernel<<<1, 1, 0, s>>>(I, b, n_chunks, trees, total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_serialize_write(const DevInterner &I, uint32_t *w, uint32_t n_chunks, const uint32_t *trees,
+                                   const int32_t *pos, uint8_t *out, unsigned long long *total, int num_sms,
+                                   cudaStream_t s) {
+    SerBufs b(w, I.capacity);
+    const unsigned g = (unsigned)num_sms * 8;
+    count_launches(2);
+    ser_write_kernel<<<g, kThreads, 0, s>>>(I, b.leaf_flag, b.leaf_off, b.branch_flag, b.branch_off, b.new_id, out);
+    ser_tail_kernel<<<1, 1, 0, s>>>(I, b.leaf_rank, b.branch_rank, b.leaf_off, b.branch_off, b.new_id, n_chunks, trees,
+                                    pos, out, total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy_many(const DevInterner &I, const uint8_t *grids, uint32_t n_trees, int d,
+                                  const uint32_t *builder_of, const uint32_t *offsets, uint32_t n_builders,
+                                  unsigned int *counts, uint32_t *slot, uint32_t max_mat, uint32_t *ids,
+                                  unsigned long long *mcounts, uint32_t *n_mat, unsigned long long *global,
+                                  unsigned long long *per_mat, unsigned long long *active, int num_sms, cudaStream_t s) {
+    const uint64_t n_vox = ((uint64_t)n_trees) << (3 * d);
+    uint64_t blocks = (n_vox + kThreads - 1) / kThreads;
+    if (blocks > (uint64_t)num_sms * 16) blocks = (uint64_t)num_sms * 16;
+    count_launches(4);
+    occupancy_hist_many_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(grids, n_trees, d, builder_of, n_builders, counts);
+    occupancy_index_many_kernel<<<(n_builders + 7) / 8, 256, 0, s>>>(counts, n_builders, slot, max_mat, ids, mcounts,
+                                                                     n_mat);
+    uint64_t lblocks = ((3ull * n_trees << (2 * d)) + kThreads - 1) / kThreads;
+    if (lblocks > (uint64_t)num_sms * 16) lblocks = (uint64_t)num_sms * 16;
+    occupancy_lines_kernel<uint8_t><<<(unsigned)lblocks, kThreads, 0, s>>>(I, grids, n_trees, d, builder_of, n_builders,
+                                                                          offsets, slot, 256, n_mat, max_mat, global,
+                                                                          per_mat);
+    occupancy_active_kernel<<<n_builders, kThreads, 0, s>>>(global, active);
     return cudaGetLastError();
 }
 
