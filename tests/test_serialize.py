@@ -15,71 +15,7 @@ from voxelis_gb300._abi import VX_PATCH_P1
 from voxelis_gb300.api import VoxInterner, VoxTree
 
 
-def read_varint(b, p):
-    v = s = 0
-    while True:
-        c = b[p]
-        p += 1
-        v |= (c & 0x7F) << s
-        s += 7
-        if c < 0x80:
-            return v, p
-
-
-def decode(b, vb):
-    """The stream as leaves {id: value}, branches {id: (mask, [child ids], lod)}, chunks [(pos, root)]."""
-    p = 0
-    u32 = lambda q: (int.from_bytes(b[q:q + 4], "big"), q + 4)  # noqa: E731
-    n, p = u32(p)
-    leaves = {}
-    for _ in range(n):
-        i, p = read_varint(b, p)
-        leaves[i] = int.from_bytes(b[p:p + vb], "big")
-        p += vb
-    n, p = u32(p)
-    branches = {}
-    for _ in range(n):
-        i, p = read_varint(b, p)
-        m = b[p]
-        p += 1
-        ch = []
-        for k in range(8):
-            if (m >> k) & 1:
-                c, p = read_varint(b, p)
-                ch.append(c)
-        lod = int.from_bytes(b[p:p + vb], "big")
-        p += vb
-        branches[i] = (m, ch, lod)
-    n, p = u32(p)
-    chunks = []
-    for _ in range(n):
-        assert b[p:p + 12] == b"VoxTreeChunk"
-        p += 12
-        pos = tuple(int.from_bytes(b[p + 4 * a:p + 4 * a + 4], "big", signed=True) for a in range(3))
-        p += 12
-        r, p = read_varint(b, p)
-        chunks.append((pos, r))
-    assert p == len(b)
-    return leaves, branches, chunks
-
-
-def canonical(leaves, branches, chunks):
-    memo = {}
-
-    def form(i):
-        if i == 0:
-            return ("E",)
-        if i in memo:
-            return memo[i]
-        if i in leaves:
-            f = ("L", leaves[i])
-        else:
-            m, ch, lod = branches[i]
-            f = ("B", m, lod, tuple(form(c) for c in ch))
-        memo[i] = f
-        return f
-
-    return [(pos, form(r)) for pos, r in chunks], len(leaves), len(branches)
+from voxelis_gb300.vtm import canonical, decode  # noqa: E402
 
 
 def single_voxel_world(lib, bits):

@@ -10,7 +10,8 @@ chunk high; the reference packs up to 8 chunks of 32^3, utils/mesh.rs:1195-1225)
   cpu_baseline the oracle's restatement of generate_occupancy_masks, one thread, on a sample
 
 Every builder of the batched result is compared with the per-builder call, and a sample of builders
-with the oracle.
+with the oracle. Also timed on the same world: vx_serialize_model of all 4096 chunks (the
+VoxModel::serialize payload, host output) against the oracle's restatement of it.
 """
 import ctypes as C
 import json
@@ -176,7 +177,44 @@ def run(args):
             np.array_equal(i_h[b, :k], o_ids[:k]) and np.array_equal(c_h[b, :k], o_cnt[:k]) and \
             np.array_equal(m_h[b, :k].ravel(), o_mask[:k * plane])
     ol.status("interner_destroy", oh)
+
+    # model serialisation of the whole world (VoxModel::serialize payload), GPU vs oracle
+    pos = np.array([(c % N_SIDE, 0, c // N_SIDE) for c in range(n)], np.int32)
+    size = C.c_uint64()
+    call("serialize_model", n, C.c_void_p(trees.ctypes.data), C.c_void_p(pos.ctypes.data), None, C.c_uint64(0),
+         C.byref(size))
+    blob = np.zeros(size.value, np.uint8)
+    ser = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        call("serialize_model", n, C.c_void_p(trees.ctypes.data), C.c_void_p(pos.ctypes.data),
+             C.c_void_p(blob.ctypes.data), C.c_uint64(size.value), C.byref(size))
+        ser.append(time.perf_counter() - t0)
+    ser_ms = statistics.median(ser) * 1e3
+    oh = C.c_void_p()
+    ol.call("interner_create", C.c_uint64(256 << 20), 8, 0, 0, C.byref(oh))
+    o_trees = np.zeros(n, np.uint32)
+    for c in range(n):
+        out = C.c_uint32()
+        ol.call("tree_create", oh, 5, C.byref(out))
+        o_trees[c] = out.value
+    ol.call("build_dense", oh, n, C.c_void_p(o_trees.ctypes.data), C.c_void_p(grids.ctypes.data), None, 0)
+    o_size = C.c_uint64()
+    ol.call("serialize_model", oh, n, C.c_void_p(o_trees.ctypes.data), C.c_void_p(pos.ctypes.data), None, C.c_uint64(0),
+            C.byref(o_size))
+    o_blob = np.zeros(o_size.value, np.uint8)
+    t0 = time.perf_counter()
+    ol.call("serialize_model", oh, n, C.c_void_p(o_trees.ctypes.data), C.c_void_p(pos.ctypes.data),
+            C.c_void_p(o_blob.ctypes.data), C.c_uint64(o_size.value), C.byref(o_size))
+    o_ms = (time.perf_counter() - t0) * 1e3
+    ol.status("interner_destroy", oh)
     call("interner_destroy")
+    from .vtm import canonical, decode
+
+    same_model = canonical(*decode(blob.tobytes(), 1)) == canonical(*decode(o_blob.tobytes(), 1))
+    serialize = {"bytes": int(size.value), "ms": ser_ms, "MB_per_s": size.value / (ser_ms * 1e-3) / 1e6,
+                 "same_model_as_oracle": bool(same_model),
+                 "cpu_baseline": {"ms": o_ms, "cores": 1, "kind": "port", "sample": "the same 4096-chunk world"}}
     line = {"metric": "chunks/s (occupancy masks, 4 chunks of 32^3 per 64^3 builder)",
             "value": n / (dev_ms * 1e-3), "unit": "chunks/s", "higher_is_better": True, "dtype": "u8",
             "config": {"workload": "occupancy masks of the 4096 dune chunks, 1024 builders, one batched call",
@@ -185,7 +223,7 @@ def run(args):
             "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "chunks/s", "ms": e2e_ms, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(out_bytes)},
             "per_builder_gpu": {"value": n / per_builder_s, "unit": "chunks/s", "same_as_batched": bool(same)},
-            "checked_against_oracle": bool(ok),
+            "checked_against_oracle": bool(ok), "serialize_model": serialize,
             "cpu_baseline": {"value": 4 * len(sample) / cpu_s, "unit": "chunks/s", "cores": 1, "kind": "port",
                              "sample": "%d builders (generate_occupancy_masks per chunk, one thread)" % len(sample)}}
     print(json.dumps(line))

@@ -1810,15 +1810,15 @@ struct QuadCache {
     int n;  // entries (0: none)
 };
 
-template <class T>
-__device__ __forceinline__ bool rows_equal32(const T *a, const T *b) {
+template <class T, int S>
+__device__ __forceinline__ bool rows_equal(const T *a, const T *b) {
     bool eq = true;
 #pragma unroll
-    for (int r = 0; r < 16; ++r) eq = eq && *quad_row<T, 32>(a, r) == *quad_row<T, 32>(b, r);
+    for (int r = 0; r < 16; ++r) eq = eq && *quad_row<T, S>(a, r) == *quad_row<T, S>(b, r);
     return eq;
 }
 
-template <class T>
+template <class T, int S>
 __device__ __forceinline__ uint64_t qc_lookup(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase,
                                               uint32_t &lod) {
     if (sizeof(T) != 1 || Q.n == 0) return 0;
@@ -1831,7 +1831,7 @@ __device__ __forceinline__ uint64_t qc_lookup(const QuadCache &Q, uint32_t h1, u
             bool eq = true;
             const volatile uint32_t *w = Q.words + 16 * h;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) eq = eq && w[r] == (uint32_t)*quad_row<T, 32>(qbase, r);
+            for (int r = 0; r < 16; ++r) eq = eq && w[r] == (uint32_t)*quad_row<T, S>(qbase, r);
             if (eq) {
                 lod = *(volatile uint32_t *)(Q.lod + h);
                 return id;
@@ -1842,7 +1842,7 @@ __device__ __forceinline__ uint64_t qc_lookup(const QuadCache &Q, uint32_t h1, u
     return 0;
 }
 
-template <class T>
+template <class T, int S>
 __device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase, uint64_t id,
                                           uint32_t lod) {
     if (sizeof(T) != 1 || Q.n == 0) return;
@@ -1851,7 +1851,7 @@ __device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint3
     for (int p = 0; p < 4; ++p) {
         if (atomicCAS((unsigned long long *)(Q.id + h), 0ull, 1ull) == 0ull) {
 #pragma unroll
-            for (int r = 0; r < 16; ++r) Q.words[16 * h + r] = (uint32_t)*quad_row<T, 32>(qbase, r);
+            for (int r = 0; r < 16; ++r) Q.words[16 * h + r] = (uint32_t)*quad_row<T, S>(qbase, r);
             Q.tag[h] = h2;
             Q.lod[h] = lod;
             __threadfence_block();
@@ -1862,11 +1862,11 @@ __device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint3
     }
 }
 
-// The 64 quads of slab `qy` (4 voxels thick in y, [4][32][32] voxels at `slab`) of a 32^3 block, two
-// per lane: uniformity on row words, the quad memo, the bottom-group path on misses; results to
-// oid/oval (Morton order).
-template <class T>
-__device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArgs &a, const T *slab, uint32_t qy,
+// 64 quads reduced by one warp, two per lane: uniformity on row words, the quad memo, the bottom-group
+// path on misses; results to oid/oval in Morton order. S = 32: the quads of slab `qy` (4 voxels thick
+// in y, [4][32][32] voxels at `tile`) of a 32^3 block; S = 16: all quads of the 16^3 octant at `tile`.
+template <class T, int S>
+__device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArgs &a, const T *tile, uint32_t qy,
                                               const KeyCache &C, const QuadCache &Q, uint64_t *leaf_cache,
                                               uint64_t *oid, uint32_t *oval) {
     using W = typename QuadWord<T>::type;
@@ -1879,11 +1879,17 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
     uint32_t qvalv[2];
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
-        const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p;
-        qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
-        qb[p] = slab + (4 * qz) * 32 + 4 * qx;
+        if (S == 32) {
+            const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p;
+            qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
+            qb[p] = tile + (4 * qz) * 32 + 4 * qx;
+        } else {
+            const uint32_t q = lane + 32u * p, qx = compact3(q), qyy = compact3(q >> 1), qz = compact3(q >> 2);
+            qm[p] = q;
+            qb[p] = tile + ((4 * qyy) * 16 + 4 * qz) * 16 + 4 * qx;
+        }
         W w[16];
-        quad_rows<T, 32>(qb[p], w);
+        quad_rows<T, S>(qb[p], w);
         const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
         const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
         bool u = true;
@@ -1919,8 +1925,8 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
         leader[p] = __ffs(peers) - 1;
         const T *lq = reinterpret_cast<const T *>(
             __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(qb[p]), leader[p]));
-        follow[p] = !uni[p] && leader[p] != (int)lane && rows_equal32<T>(qb[p], lq);
-        if (!uni[p] && !follow[p]) qidv[p] = qc_lookup<T>(Q, h1[p], h2[p], qb[p], qvalv[p]);
+        follow[p] = !uni[p] && leader[p] != (int)lane && rows_equal<T, S>(qb[p], lq);
+        if (!uni[p] && !follow[p]) qidv[p] = qc_lookup<T, S>(Q, h1[p], h2[p], qb[p], qvalv[p]);
     }
     {  // memo probes, both quads in flight
         bool look[2];
@@ -1940,9 +1946,9 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
                 if (sv[p] == 0ull) {
                     look[p] = false;
                 } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
-                           memo_match<T, 32>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
+                           memo_match<T, S>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
                     look[p] = false;
-                    qc_insert<T>(Q, h1[p], h2[p], qb[p], qidv[p], qvalv[p]);
+                    qc_insert<T, S>(Q, h1[p], h2[p], qb[p], qidv[p], qvalv[p]);
                 } else if (step == 3) {
                     look[p] = false;
                 } else {
@@ -1958,13 +1964,13 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
         if (__any_sync(0xFFFFFFFFu, active)) {
             uint64_t pid;
             uint32_t pval;
-            quad_groups<T, 32>(I, C, leaf_cache, qb[p], active, pid, pval);
+            quad_groups<T, S>(I, C, leaf_cache, qb[p], active, pid, pval);
             if (active) {
                 qidv[p] = pid;
                 qvalv[p] = pval;
                 if (pid != INVALID_ID) {
-                    if (memo) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
-                    qc_insert<T>(Q, h1[p], h2[p], qb[p], pid, pval);
+                    if (memo) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
+                    qc_insert<T, S>(Q, h1[p], h2[p], qb[p], pid, pval);
                 }
             }
         }
@@ -1976,6 +1982,101 @@ __device__ __forceinline__ void quads_of_slab(const DevInterner &I, const OctArg
         }
         oid[qm[p]] = qidv[p];
         oval[qm[p]] = qvalv[p];
+    }
+}
+
+// ---- quads of 16^3 octants, one warp each, with no coupling between warps ----------------------------
+// Each warp streams its own octants through its own two tiles (4-D TMA box of 16^3, the copy of octant
+// i+2 issued as soon as octant i has been reduced), so a warp slowed by memo misses holds back nobody.
+#ifndef VX_QUADS16
+#define VX_QUADS16 0
+#endif
+#ifndef VX_Q16_TILES
+#define VX_Q16_TILES 2
+#endif
+constexpr int kQ16Warps = 8;
+
+template <class T>
+struct Q16Smem {
+    static constexpr size_t tile = 4096 * sizeof(T);
+    static constexpr size_t kc = (size_t)kQ16Warps * VX_Q16_TILES * tile;  // 3 * kKeyCache u64
+    static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;        // 256 u64
+    static constexpr size_t bars = leaf + 256 * 8;                         // VX_Q16_TILES per warp
+    static constexpr size_t kcval = bars + (size_t)kQ16Warps * VX_Q16_TILES * 8;
+    static constexpr size_t total = kcval + (size_t)kKeyCache * 4;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kQ16Warps * 32) dense_quads16_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
+                                                                       uint32_t *q_vals,
+                                                                       const __grid_constant__ CUtensorMap tmap) {
+    using L = Q16Smem<T>;
+    constexpr int NT = VX_Q16_TILES;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + L::kc);
+    uint64_t *leaf_cache = reinterpret_cast<uint64_t *>(smem + L::leaf);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars) + warp * NT;
+    T *tiles = reinterpret_cast<T *>(smem + (size_t)warp * NT * L::tile);
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
+    QuadCache Q{nullptr, nullptr, nullptr, nullptr, 0};
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    if (lane == 0) {
+        for (int b = 0; b < NT; ++b) mbar_init(bars + b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    const int d = a.depth;
+    const int ob = 3 * (d - 4);
+    const uint64_t n_oct = (uint64_t)a.n_chunks << ob;
+    const uint64_t per_chunk = 1ull << (3 * (d - 2));
+    const uint64_t total = (uint64_t)gridDim.x * kQ16Warps;
+    const uint64_t gw = (uint64_t)blockIdx.x * kQ16Warps + warp;
+    auto issue = [&](uint64_t o, int b) {
+        const uint32_t c = (uint32_t)(o >> ob);
+        const uint32_t q = (uint32_t)(o & ((1ull << ob) - 1));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bars + b, (uint32_t)L::tile);
+        tma_load_octant(tiles + (size_t)b * 4096, &tmap, (int)(compact3(q) * 16), (int)(compact3(q >> 2) * 16),
+                        (int)(compact3(q >> 1) * 16), (int)c, bars + b);
+    };
+    if (lane == 0)
+        for (int b = 0; b < NT; ++b)
+            if (gw + b * total < n_oct) issue(gw + b * total, b);
+    uint32_t j = 0;
+    for (uint64_t o = gw; o < n_oct; o += total, ++j) {
+        const int b = (int)(j % NT);
+        const uint32_t use = j / NT;
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bars + b, use & 1u))) break;
+        if (!__all_sync(0xFFFFFFFFu, ok)) {  // give up: wait (bounded) for this warp's copies, then leave
+            if (lane == 0) set_error(I, ERR_TIMEOUT, 33);
+            for (int bb = 0; bb < NT; ++bb)
+                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bars + bb, ((j + bb) / NT) & 1u); ++spin) {
+                }
+            return;
+        }
+        const uint32_t c = (uint32_t)(o >> ob);
+        const uint64_t q = o & ((1ull << ob) - 1);
+        const uint32_t tree = a.trees[c];
+        uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 6);
+        uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 6);
+        if (tree < I.tree_cap && I.depths[tree] == d) {
+            quads_of_tile<T, 16>(I, a, tiles + (size_t)b * 4096, 0, C, Q, leaf_cache, oid, oval);
+        } else {
+            if (lane == 0) set_error(I, ERR_INVALID, 34);
+            for (unsigned k = lane; k < 64; k += 32) {
+                oid[k] = EMPTY_ID;
+                oval[k] = 0;
+            }
+        }
+        __syncwarp();
+        const uint64_t ahead = o + (uint64_t)NT * total;
+        if (lane == 0 && ahead < n_oct) issue(ahead, b);
     }
 }
 
@@ -2074,7 +2175,7 @@ __global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I
             slab = reinterpret_cast<const T *>(dst);
         }
         if (!bad) {
-            quads_of_slab<T>(I, a, slab, warp, C, Q, leaf_cache, oid, oval);
+            quads_of_tile<T, 32>(I, a, slab, warp, C, Q, leaf_cache, oid, oval);
         } else {
             if (tid == 0) set_error(I, ERR_INVALID, 31);
             for (unsigned k = lane; k < 64; k += 32) {
@@ -2571,8 +2672,31 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
         kernel<<<(unsigned)grid, kQuadThreads, smem, s>>>(I, a, q_ids, q_vals, tmap);
         return cudaGetLastError();
     };
-    cudaError_t e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
-                            : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
+    cudaError_t e = cudaSuccess;
+    if (VX_QUADS16) {
+        CUtensorMap tmap16;
+        cuuint32_t box16[4] = {16, 16, 16, 1};
+        r = encode(&tmap16, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                   const_cast<void *>(grids), dims, strides, box16, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+        auto launch16 = [&](auto kernel, size_t smem) -> cudaError_t {
+            cudaError_t e2 = cudaSuccess;
+            const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQ16Warps * 32, smem, &e2);
+            if (e2 != cudaSuccess) return e2;
+            uint64_t grid = (uint64_t)num_sms * per_sm;
+            const uint64_t need = (((uint64_t)n_chunks << (3 * (depth - 4))) + kQ16Warps - 1) / kQ16Warps;
+            if (grid > need) grid = need;
+            count_launches(1);
+            kernel<<<(unsigned)grid, kQ16Warps * 32, smem, s>>>(I, a, q_ids, q_vals, tmap16);
+            return cudaGetLastError();
+        };
+        e = es == 1 ? launch16(dense_quads16_kernel<uint8_t>, Q16Smem<uint8_t>::total)
+                    : launch16(dense_quads16_kernel<uint16_t>, Q16Smem<uint16_t>::total);
+    } else {
+        e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
+                    : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
+    }
     if (e != cudaSuccess) return e;
     if (levels_begin) (*levels_begin)(levels_ctx);
     for (int k = depth - 3; k >= 3; --k) {
