@@ -1863,12 +1863,14 @@ __device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint3
 }
 
 // 64 quads reduced by one warp, two per lane: uniformity on row words, the quad memo, the bottom-group
-// path on misses; results to oid/oval in Morton order. S = 32: the quads of slab `qy` (4 voxels thick
+// path on misses; results to oid/oval in Morton order (when given) and to lane_out/lane_val[p] for
+// the lane's quad p (when given). S = 32: the quads of slab `qy` (4 voxels thick
 // in y, [4][32][32] voxels at `tile`) of a 32^3 block; S = 16: all quads of the 16^3 octant at `tile`.
 template <class T, int S>
 __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArgs &a, const T *tile, uint32_t qy,
                                               const KeyCache &C, const QuadCache &Q, uint64_t *leaf_cache,
-                                              uint64_t *oid, uint32_t *oval) {
+                                              uint64_t *oid, uint32_t *oval, uint64_t *lane_out = nullptr,
+                                              uint32_t *lane_val = nullptr) {
     using W = typename QuadWord<T>::type;
     const unsigned lane = threadIdx.x & 31u;
     const bool memo = a.memo_slots != nullptr;
@@ -1980,19 +1982,34 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             qidv[p] = lid;
             qvalv[p] = lval;
         }
-        oid[qm[p]] = qidv[p];
-        oval[qm[p]] = qvalv[p];
+        if (oid) {
+            oid[qm[p]] = qidv[p];
+            oval[qm[p]] = qvalv[p];
+        }
+        if (lane_out) {
+            lane_out[p] = qidv[p];
+            lane_val[p] = qvalv[p];
+        }
     }
 }
+
+__device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool in, const uint64_t c[8],
+                                                    const uint32_t cv[8], uint64_t &out, uint32_t &val);
 
 // ---- quads of 16^3 octants, one warp each, with no coupling between warps ----------------------------
 // Each warp streams its own octants through its own two tiles (4-D TMA box of 16^3, the copy of octant
 // i+2 issued as soon as octant i has been reduced), so a warp slowed by memo misses holds back nobody.
 #ifndef VX_QUADS16
-#define VX_QUADS16 0
+#define VX_QUADS16 1
 #endif
 #ifndef VX_Q16_TILES
-#define VX_Q16_TILES 2
+#define VX_Q16_TILES 1  // 1: more resident warps beat prefetching within a warp (measured)
+#endif
+#ifndef VX_Q16_LEVELS
+#define VX_Q16_LEVELS 0  // 1: the warp also reduces its octant's 8^3 nodes and the octant node
+#endif
+#ifndef VX_Q16_MINB
+#define VX_Q16_MINB 4  // resident CTAs per SM the register allocation must allow
 #endif
 constexpr int kQ16Warps = 8;
 
@@ -2007,7 +2024,7 @@ struct Q16Smem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kQ16Warps * 32) dense_quads16_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
+__global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
                                                                        uint32_t *q_vals,
                                                                        const __grid_constant__ CUtensorMap tmap) {
     using L = Q16Smem<T>;
@@ -2065,7 +2082,45 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_quads16_kernel(DevIntern
         const uint32_t tree = a.trees[c];
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 6);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 6);
-        if (tree < I.tree_cap && I.depths[tree] == d) {
+        if (VX_Q16_LEVELS) {  // q_ids / q_vals hold octant nodes: n_chunks x 8^(d-4)
+            uint64_t qid2[2];
+            uint32_t qval2[2];
+            const bool ok_tree = tree < I.tree_cap && I.depths[tree] == d;
+            if (ok_tree) {
+                quads_of_tile<T, 16>(I, a, tiles + (size_t)b * 4096, 0, C, Q, leaf_cache, nullptr, nullptr, qid2,
+                                     qval2);
+            } else {
+                if (lane == 0) set_error(I, ERR_INVALID, 34);
+                qid2[0] = qid2[1] = EMPTY_ID;
+                qval2[0] = qval2[1] = 0;
+            }
+            // 8^3 nodes: lane j < 8 takes quads 8j .. 8j+7 (pass j >> 2)
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int src = (8 * lane + k) & 31;
+                const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, qid2[0], src), a1 = __shfl_sync(0xFFFFFFFFu, qid2[1], src);
+                const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, qval2[0], src), b1 = __shfl_sync(0xFFFFFFFFu, qval2[1], src);
+                ch[k] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
+                cv[k] = lane < 4 ? b0 : b1;
+            }
+            uint64_t o2;
+            uint32_t v2;
+            reduce_parent_dedup(I, lane < 8, ch, cv, o2, v2);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = __shfl_sync(0xFFFFFFFFu, o2, k);
+                cv[k] = __shfl_sync(0xFFFFFFFFu, v2, k);
+            }
+            uint64_t o1;
+            uint32_t v1;
+            reduce_parent_dedup(I, lane == 0, ch, cv, o1, v1);
+            if (lane == 0) {
+                q_ids[((uint64_t)c << ob) + q] = o1;
+                q_vals[((uint64_t)c << ob) + q] = v1;
+            }
+        } else if (tree < I.tree_cap && I.depths[tree] == d) {
             quads_of_tile<T, 16>(I, a, tiles + (size_t)b * 4096, 0, C, Q, leaf_cache, oid, oval);
         } else {
             if (lane == 0) set_error(I, ERR_INVALID, 34);
@@ -2659,8 +2714,9 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-    uint64_t *q_ids = ids + off[depth - 2];
-    uint32_t *q_vals = vals + off[depth - 2];
+    const bool oct_levels = VX_QUADS16 && VX_Q16_LEVELS;
+    uint64_t *q_ids = ids + off[oct_levels ? depth - 4 : depth - 2];
+    uint32_t *q_vals = vals + off[oct_levels ? depth - 4 : depth - 2];
     auto launchq = [&](auto kernel, size_t smem) -> cudaError_t {
         cudaError_t e = cudaSuccess;
         const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQuadThreads, smem, &e);
@@ -2699,6 +2755,15 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     }
     if (e != cudaSuccess) return e;
     if (levels_begin) (*levels_begin)(levels_ctx);
+    if (oct_levels) {  // passes above the octant nodes, the last one commits the roots
+        for (int k = depth - 5; k >= 0; --k) {
+            const uint64_t np = (uint64_t)n_chunks << (3 * k);
+            e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], k > 0 ? ids + off[k] : nullptr,
+                                   k > 0 ? vals + off[k] : nullptr, np, k == 0, trees, changed, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
     for (int k = depth - 3; k >= 3; --k) {
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
         e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], ids + off[k], vals + off[k], np, false, trees,
