@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
 // CTA already interned; only misses go to the global branch table, deduplicated within the warp.
 
 #ifndef VX_KEY_CACHE
-#define VX_KEY_CACHE 128
+#define VX_KEY_CACHE 256
 #endif
 #ifndef VX_OCT_TILES
 #define VX_OCT_TILES 1
