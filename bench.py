@@ -65,6 +65,22 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(ms, world, device=None):
+    """The step time of the whole job: the slowest replica's (all-reduce MAX; NCCL on GPUs, gloo on CPU)."""
+    if world <= 1:
+        return ms
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, ms):
+    """Whole-job units/s of `world` replicas that each processed units_per_rank in `ms` (max over ranks)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def config(extra=None):
     c = {"workload": WORKLOAD, "chunks": CHUNKS_X * CHUNKS_Z, "max_depth": DEPTH, "voxel": "u8",
          "seed": SEED, "budget_bytes": BUDGET, "gets": N_GETS,
@@ -309,11 +325,7 @@ def run_ours(args):
     phases = {VX_PROF_NAMES[k]: {"ms_total": prof_ms[k], "count": int(prof_n[k])} for k in range(VX_PROF_N)
               if prof_n[k]}
     dense_ms = prof_ms[0] / max(1, prof_n[0])
-    ms = statistics.mean(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(step_ms), world, dev)
 
     # DAG size after the last timed step
     from voxelis_gb300._abi import vx_interner_stats
@@ -406,7 +418,7 @@ def run_ours(args):
     achieved = algo_bytes / (dense_ms * 1e-3) / 1e9
     line = {
         "metric": "chunks/s",
-        "value": world * n / (ms * 1e-3),
+        "value": replica_throughput(n, world, ms),
         "unit": "chunks/s",
         "n_gpus": world,
         "steps": args.steps,
