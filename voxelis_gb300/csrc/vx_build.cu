@@ -2709,11 +2709,13 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     cuuint64_t strides[3] = {side * es, side * side * es, side * side * side * es};
     cuuint32_t box[4] = {32, 32, 32, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
-                        const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    CUresult r = CUDA_SUCCESS;
+    if (!VX_QUADS16) {  // the 16^3 kernel encodes its own map below
+        r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                   const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    }
     const bool oct_levels = VX_QUADS16 && VX_Q16_LEVELS;
     uint64_t *q_ids = ids + off[oct_levels ? depth - 4 : depth - 2];
     uint32_t *q_vals = vals + off[oct_levels ? depth - 4 : depth - 2];

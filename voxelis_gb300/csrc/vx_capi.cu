@@ -79,7 +79,9 @@ uint64_t batch_touched_count(const vx_batch *b) {
 // Calls f(g) for every group with a set or clear bit, in ascending group order.
 template <class F>
 void batch_for_each_touched(const vx_batch *b, F f) {
-    if (b->all_touched) {
+    // a dense fill, or a touched list long enough that scanning the group arrays in order beats
+    // sorting it
+    if (b->all_touched || (!b->touched_sorted && b->touched.size() * 16 > b->groups)) {
         for (uint64_t g = 0; g < b->groups; ++g)
             if (b->set[g] | b->clear[g]) f(g);
         return;
@@ -111,7 +113,7 @@ struct DevBuf {
     }
 };
 
-constexpr int kCopyPieces = 4;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
+constexpr int kCopyPieces = 8;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
 
 struct HostBuf {
     void *p = nullptr;
@@ -170,6 +172,8 @@ struct vx_interner {
     // tree table
     uint32_t tree_cap = 0;
     std::vector<uint8_t> tree_depth, tree_used, tree_maybe_nonempty;
+    std::vector<uint32_t> tree_stamp;  // duplicate detection within one call
+    uint32_t stamp_epoch = 0;
     std::vector<uint32_t> free_trees;
     uint32_t tree_count = 0;
     bool all_trees_unknown = false;
@@ -1255,12 +1259,18 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
     } else {
         std::copy(trees, trees + n, htrees.begin());
     }
-    std::unordered_set<vx_tree> seen;
+    // duplicate check with a per-interner stamp per tree slot (no allocation per call)
+    if (it->tree_stamp.size() < it->tree_depth.size()) it->tree_stamp.assign(it->tree_depth.size(), 0);
+    if (++it->stamp_epoch == 0) {
+        std::fill(it->tree_stamp.begin(), it->tree_stamp.end(), 0u);
+        it->stamp_epoch = 1;
+    }
     int d = -1;
     bool fresh = !it->all_trees_unknown;
     for (vx_tree t : htrees) {
         if (!tree_ok(it, t)) return set_err(it, VX_E_INVALID_ARG, "unknown tree handle");
-        if (!seen.insert(t).second) return set_err(it, VX_E_INVALID_ARG, "a tree appears twice in one call");
+        if (it->tree_stamp[t] == it->stamp_epoch) return set_err(it, VX_E_INVALID_ARG, "a tree appears twice in one call");
+        it->tree_stamp[t] = it->stamp_epoch;
         if (d >= 0 && it->tree_depth[t] != d) return set_err(it, VX_E_INVALID_ARG, "trees of one call share a depth");
         d = it->tree_depth[t];
         fresh = fresh && !it->tree_maybe_nonempty[t];
