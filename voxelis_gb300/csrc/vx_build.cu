@@ -54,9 +54,6 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -94,7 +91,7 @@ __device__ __forceinline__ uint64_t leaf_of(const DevInterner &I, uint64_t *leaf
 template <class T>
 __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, DenseArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int B = a.bdepth;
+    const int B = a.depth;
     const int S = 1 << B;
     const uint32_t V = 1u << (3 * B);
     const uint32_t G = V >> 3;
@@ -115,12 +112,8 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
     }
     __syncthreads();
 
-    const uint64_t total_blocks = (uint64_t)a.n_chunks * a.blocks_per_chunk;
-    const int side = 1 << a.depth;
     uint32_t phase = 0;
-    for (uint64_t blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
-        const uint32_t chunk = (uint32_t)(blk / a.blocks_per_chunk);
-        const uint32_t m = (uint32_t)(blk % a.blocks_per_chunk);
+    for (uint32_t chunk = blockIdx.x; chunk < a.n_chunks; chunk += gridDim.x) {
         {
             // tree handles may come from device memory: check them before any write
             const uint32_t tree = a.trees[chunk];
@@ -130,37 +123,24 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
                 continue;
             }
         }
-        const T *grid = reinterpret_cast<const T *>(a.grids) + (size_t)chunk * side * side * side;
+        const T *grid = reinterpret_cast<const T *>(a.grids) + (size_t)chunk * V;
 
-        // ---- stage the block into shared memory ------------------------------------------------
-        if (a.depth == B) {
-            if (tid == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(bar, V * (uint32_t)sizeof(T));
-                bulk_copy_g2s(vox, grid, V * (uint32_t)sizeof(T), bar);
-            }
-            bool ok = false;
-            for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-                if ((ok = mbar_try_wait(bar, phase))) break;
-            if (__syncthreads_or(!ok)) {  // every thread leaves together; the copy is drained first
-                if (tid == 0) set_error(I, ERR_TIMEOUT, 20);
-                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bar, phase); ++spin) {
-                }
-                return;
-            }
-            phase ^= 1u;
-        } else {
-            const uint32_t bx = compact3(m), by = compact3(m >> 1), bz = compact3(m >> 2);
-            const int rows = S * S;
-            const int vec_per_row = S * (int)sizeof(T) / 16;
-            for (int r = tid; r < rows * vec_per_row; r += blockDim.x) {
-                const int row = r / vec_per_row, v = r % vec_per_row;
-                const int y = row / S, z = row % S;
-                const T *src = grid + ((size_t)(by * S + y) * side + (bz * S + z)) * side + bx * S;
-                reinterpret_cast<uint4 *>(vox + (size_t)row * S)[v] = __ldcs(reinterpret_cast<const uint4 *>(src) + v);
-            }
-            __syncthreads();
+        // ---- stage the chunk into shared memory (V * sizeof(T) >= 64 bytes: a multiple of 16) ---
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, V * (uint32_t)sizeof(T));
+            bulk_copy_g2s(vox, grid, V * (uint32_t)sizeof(T), bar);
         }
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bar, phase))) break;
+        if (__syncthreads_or(!ok)) {  // every thread leaves together; the copy is drained first
+            if (tid == 0) set_error(I, ERR_TIMEOUT, 20);
+            for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bar, phase); ++spin) {
+            }
+            return;
+        }
+        phase ^= 1u;
 
         // ---- bottom groups (depth d-1) ------------------------------------------------------
         uint64_t *bottom = lvl + (G - 1) / 7;
@@ -289,42 +269,31 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
             __syncthreads();
         }
 
-        // ---- block result -------------------------------------------------------------------
+        // ---- chunk root ----------------------------------------------------------------------
         if (tid == 0) {
             const uint64_t root = lvl[0];
-            if (a.depth == B) {
-                const uint32_t tree = a.trees[chunk];
-                if (root != EMPTY_ID) {
-                    I.roots[tree] = root;
-                    atomicAdd(I.refcount + id_index(root), 1u);
-                }
-                if (a.changed) a.changed[chunk] = root != EMPTY_ID;
-            } else {
-                a.block_roots[blk] = root;
-                a.block_vals[blk] = lval[0];
+            const uint32_t tree = a.trees[chunk];
+            if (root != EMPTY_ID) {
+                I.roots[tree] = root;
+                atomicAdd(I.refcount + id_index(root), 1u);
             }
+            if (a.changed) a.changed[chunk] = root != EMPTY_ID;
         }
         __syncthreads();
     }
 }
 
-// ---- 32^3 blocks: one warp per 16^3 octant, reduced in registers ------------------------------
+// ---- CTA-wide caches of the dense-build kernels ------------------------------------------------
 //
-// Lane l of warp w owns level-3 parents l and l+32 of octant w (a level-3 parent is 4^3 voxels,
-// 8 bottom groups). It reduces its 8 groups one by one in registers, then the parent; levels 2 and 1
-// of the octant are gathered with warp shuffles. Only the 8 octant roots meet in shared memory, so
-// a block costs one CTA barrier (plus the tile's own) instead of one per level. Bottom-group keys
-// (the 8 packed voxel values) are looked up first in a CTA-wide shared cache of the branches this
-// CTA already interned; only misses go to the global branch table, deduplicated within the warp.
+// Bottom-group keys (the 8 packed voxel values of a 2^3 group) are looked up first in a CTA-wide
+// shared cache of the branches this CTA already interned, with their LOD values; only misses go to
+// the global branch table, deduplicated within the warp.
 
 #ifndef VX_KEY_CACHE
 #define VX_KEY_CACHE 256
 #endif
 #ifndef VX_OCT_TILES
 #define VX_OCT_TILES 1
-#endif
-#ifndef VX_TILE_V2
-#define VX_TILE_V2 3  // 0: per-lane groups; 2: + shared quad cache; 3: + device-wide quad memo
 #endif
 constexpr int kKeyCache = VX_KEY_CACHE;  // entries of the shared bottom-key cache (power of two)
 constexpr int kOctTiles = VX_OCT_TILES;  // tile buffers per warp in the octant kernel (1 or 2)
@@ -371,36 +340,6 @@ __device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64
     }
 }
 
-// 8 voxels of the bottom group whose lowest corner is (x, y, z) in a 32^3 [y][z][x] tile.
-template <class T>
-__device__ __forceinline__ void load_group32(const T *vox, uint32_t x, uint32_t y, uint32_t z, uint32_t v[8],
-                                             uint64_t &lo, uint64_t &hi) {
-    const uint32_t base = (y * 32 + z) * 32 + x;
-    const uint32_t off[4] = {base, base + 1024, base + 32, base + 1056};
-    lo = 0;
-    hi = 0;
-    if (sizeof(T) == 1) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t w = *reinterpret_cast<const uint16_t *>(vox + off[q]);
-            v[2 * q] = w & 0xFF;
-            v[2 * q + 1] = w >> 8;
-            lo |= (uint64_t)w << (16 * q);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t w = *reinterpret_cast<const uint32_t *>(vox + off[q]);
-            v[2 * q] = w & 0xFFFF;
-            v[2 * q + 1] = w >> 16;
-            if (q < 2)
-                lo |= (uint64_t)w << (32 * q);
-            else
-                hi |= (uint64_t)w << (32 * (q - 2));
-        }
-    }
-}
-
 // One parent from 8 children held by the calling lane: EMPTY, a collapsed leaf, or an interned
 // branch (warp-cooperative; every lane of the warp calls it).
 __device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active, const uint64_t c[8],
@@ -430,196 +369,6 @@ __device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active,
     }
 }
 
-template <class T>
-__device__ __forceinline__ void reduce_octant(const DevInterner &I, const T *vox, int w, const KeyCache &C,
-                                              uint64_t *leaf_cache, uint64_t &oct_id, uint32_t &oct_val) {
-    const unsigned lane = threadIdx.x & 31u;
-    const uint32_t ox = (w & 1) << 4, oy = ((w >> 1) & 1) << 4, oz = (w >> 2) << 4;
-    const bool wide = sizeof(T) == 2;
-    uint64_t l3[2];
-    uint32_t l3v[2];
-#pragma unroll 1
-    for (int pass = 0; pass < 2; ++pass) {
-        const uint32_t p = lane + 32 * pass;
-        const uint32_t px = compact3(p), py = compact3(p >> 1), pz = compact3(p >> 2);
-        uint64_t c3[8];
-        uint32_t cv3[8];
-#pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t gx = 2 * px + (k & 1), gy = 2 * py + ((k >> 1) & 1), gz = 2 * pz + (k >> 2);
-            uint32_t v[8];
-            uint64_t lo, hi;
-            load_group32<T>(vox, ox + 2 * gx, oy + 2 * gy, oz + 2 * gz, v, lo, hi);
-            uint32_t set = 0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) set |= (v[j] != 0 ? 1u : 0u) << j;
-            bool uniform = set == 0xFF;
-#pragma unroll
-            for (int j = 1; j < 8; ++j) uniform = uniform && v[j] == v[0];
-            const bool is_branch = set != 0 && !uniform;
-            uint64_t id = is_branch ? kc_lookup(C, lo, hi) : 0ull;
-            const bool need = is_branch && id == 0;
-            const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
-            uint32_t lod = is_branch ? calc_average8(v) : 0;
-            if (bm) {  // warp-uniform
-                unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
-                if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
-                grp &= bm;
-                const int leader = need ? __ffs(grp) - 1 : (int)lane;
-                const bool lead = need && leader == (int)lane;
-                uint64_t c[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
-                bool created;
-                uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
-                nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-                if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid);
-                if (need) id = nid;
-            }
-            if (set == 0) {
-                c3[k] = EMPTY_ID;
-                cv3[k] = 0;
-            } else if (uniform) {
-                c3[k] = leaf_of<T>(I, leaf_cache, v[0]);
-                cv3[k] = v[0];
-            } else {
-                c3[k] = id;
-                cv3[k] = lod;
-            }
-        }
-        reduce_parent(I, true, c3, cv3, l3[pass], l3v[pass]);
-    }
-    // level 2: lane q < 8 takes level-3 parents 8q .. 8q+7 (pass q >> 2)
-    uint64_t c2[8];
-    uint32_t cv2[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int src = (8 * lane + j) & 31;
-        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
-        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
-        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
-        cv2[j] = lane < 4 ? b0 : b1;
-    }
-    uint64_t l2;
-    uint32_t l2v;
-    reduce_parent(I, lane < 8, c2, cv2, l2, l2v);
-    // level 1: the octant root, from lanes 0..7
-    uint64_t c1[8];
-    uint32_t cv1[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
-        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
-    }
-    uint64_t l1;
-    uint32_t l1v;
-    reduce_parent(I, lane == 0, c1, cv1, l1, l1v);
-    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
-    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) dense32_kernel(DevInterner I, DenseArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    constexpr uint32_t V = 32768;
-    T *vox = reinterpret_cast<T *>(smem);
-    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + V * sizeof(T));
-    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache};
-    uint64_t *leaf_cache = kc + 3 * kKeyCache;
-    uint64_t *oct_id = leaf_cache + 256;
-    uint32_t *oct_val = reinterpret_cast<uint32_t *>(oct_id + 8);
-    uint64_t *bar = oct_id + 12;
-
-    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
-    if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
-    const uint64_t total_blocks = (uint64_t)a.n_chunks * a.blocks_per_chunk;
-    const int side = 1 << a.depth;
-    uint32_t phase = 0;
-    for (uint64_t blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
-        const uint32_t chunk = (uint32_t)(blk / a.blocks_per_chunk);
-        const uint32_t m = (uint32_t)(blk % a.blocks_per_chunk);
-        {
-            const uint32_t tree = a.trees[chunk];
-            const bool bad = tree >= I.tree_cap || I.depths[tree] != a.depth;
-            if (__syncthreads_or(bad)) {
-                if (tid == 0) set_error(I, ERR_INVALID, 23);
-                continue;
-            }
-        }
-        const T *grid = reinterpret_cast<const T *>(a.grids) + (size_t)chunk * side * side * side;
-        if (a.depth == 5) {
-            if (tid == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(bar, V * (uint32_t)sizeof(T));
-                bulk_copy_g2s(vox, grid, V * (uint32_t)sizeof(T), bar);
-            }
-            bool ok = false;
-            for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-                if ((ok = mbar_try_wait(bar, phase))) break;
-            if (__syncthreads_or(!ok)) {  // every thread leaves together; the copy is drained first
-                if (tid == 0) set_error(I, ERR_TIMEOUT, 24);
-                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bar, phase); ++spin) {
-                }
-                return;
-            }
-            phase ^= 1u;
-        } else {
-            const uint32_t bx = compact3(m), by = compact3(m >> 1), bz = compact3(m >> 2);
-            const int vec_per_row = 32 * (int)sizeof(T) / 16;
-            for (int r = tid; r < 1024 * vec_per_row; r += blockDim.x) {
-                const int row = r / vec_per_row, v = r % vec_per_row;
-                const int y = row >> 5, z = row & 31;
-                const T *src = grid + ((size_t)(by * 32 + y) * side + (bz * 32 + z)) * side + bx * 32;
-                reinterpret_cast<uint4 *>(vox + (size_t)row * 32)[v] = __ldcs(reinterpret_cast<const uint4 *>(src) + v);
-            }
-            __syncthreads();
-        }
-
-        uint64_t oid;
-        uint32_t oval;
-        reduce_octant<T>(I, vox, (int)warp, C, leaf_cache, oid, oval);
-        if (lane == 0) {
-            oct_id[warp] = oid;
-            oct_val[warp] = oval;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            uint64_t c[8];
-            uint32_t cv[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                c[j] = oct_id[j];
-                cv[j] = oct_val[j];
-            }
-            uint64_t root;
-            uint32_t rval;
-            reduce_parent(I, lane == 0, c, cv, root, rval);
-            if (lane == 0) {
-                if (a.depth == 5) {
-                    const uint32_t tree = a.trees[chunk];
-                    if (root != EMPTY_ID) {
-                        I.roots[tree] = root;
-                        atomicAdd(I.refcount + id_index(root), 1u);
-                    }
-                    if (a.changed) a.changed[chunk] = root != EMPTY_ID;
-                } else {
-                    a.block_roots[blk] = root;
-                    a.block_vals[blk] = rval;
-                }
-            }
-        }
-        __syncthreads();
-    }
-}
-
 // ---- 16^3 octants, one warp each, TMA tensor copies, last-arriver reduction above ------------
 //
 // Each warp streams its own octants: lane 0 issues a 4-D tiled TMA copy (box 16 x 16 x 16 of the
@@ -646,134 +395,20 @@ struct OctArgs {
     unsigned char *memo_recs;        // record r: 16 row words, then id (8 B) and LOD value (4 B)
     uint32_t memo_mask;              // slots - 1
     uint32_t memo_cap;               // records
+    unsigned long long *work;        // octants handed out beyond the first one per warp (nullptr: fixed stride)
 };
 
 constexpr int kOctWarps = 8;
 
-template <class T>
-__device__ __forceinline__ void reduce_tile16(const DevInterner &I, const T *tile, const KeyCache &C,
-                                              uint64_t *leaf_cache, uint64_t &oct_id, uint32_t &oct_val) {
-    const unsigned lane = threadIdx.x & 31u;
-    const bool wide = sizeof(T) == 2;
-    uint64_t l3[2];
-    uint32_t l3v[2];
-#pragma unroll 1
-    for (int pass = 0; pass < 2; ++pass) {
-        const uint32_t p = lane + 32 * pass;
-        const uint32_t px = compact3(p), py = compact3(p >> 1), pz = compact3(p >> 2);
-        uint64_t c3[8];
-        uint32_t cv3[8];
-#pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t x = 4 * px + 2 * (k & 1), y = 4 * py + 2 * ((k >> 1) & 1), z = 4 * pz + 2 * (k >> 2);
-            const uint32_t base = (y * 16 + z) * 16 + x;
-            const uint32_t off[4] = {base, base + 256, base + 16, base + 272};
-            uint32_t v[8];
-            uint64_t lo = 0, hi = 0;
-            if (sizeof(T) == 1) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t w = *reinterpret_cast<const uint16_t *>(tile + off[q]);
-                    v[2 * q] = w & 0xFF;
-                    v[2 * q + 1] = w >> 8;
-                    lo |= (uint64_t)w << (16 * q);
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t w = *reinterpret_cast<const uint32_t *>(tile + off[q]);
-                    v[2 * q] = w & 0xFFFF;
-                    v[2 * q + 1] = w >> 16;
-                    if (q < 2)
-                        lo |= (uint64_t)w << (32 * q);
-                    else
-                        hi |= (uint64_t)w << (32 * (q - 2));
-                }
-            }
-            uint32_t set = 0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) set |= (v[j] != 0 ? 1u : 0u) << j;
-            bool uniform = set == 0xFF;
-#pragma unroll
-            for (int j = 1; j < 8; ++j) uniform = uniform && v[j] == v[0];
-            const bool is_branch = set != 0 && !uniform;
-            uint64_t id = is_branch ? kc_lookup(C, lo, hi) : 0ull;
-            const bool need = is_branch && id == 0;
-            const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
-            const uint32_t lod = is_branch ? calc_average8(v) : 0;
-            if (bm) {
-                unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
-                if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
-                grp &= bm;
-                const int leader = need ? __ffs(grp) - 1 : (int)lane;
-                const bool lead = need && leader == (int)lane;
-                uint64_t c[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
-                bool created;
-                uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
-                nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-                if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid);
-                if (need) id = nid;
-            }
-            if (set == 0) {
-                c3[k] = EMPTY_ID;
-                cv3[k] = 0;
-            } else if (uniform) {
-                c3[k] = leaf_of<T>(I, leaf_cache, v[0]);
-                cv3[k] = v[0];
-            } else {
-                c3[k] = id;
-                cv3[k] = lod;
-            }
-        }
-        reduce_parent(I, true, c3, cv3, l3[pass], l3v[pass]);
-    }
-    uint64_t c2[8];
-    uint32_t cv2[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int src = (8 * lane + j) & 31;
-        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
-        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
-        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
-        cv2[j] = lane < 4 ? b0 : b1;
-    }
-    uint64_t l2;
-    uint32_t l2v;
-    reduce_parent(I, lane < 8, c2, cv2, l2, l2v);
-    uint64_t c1[8];
-    uint32_t cv1[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
-        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
-    }
-    uint64_t l1;
-    uint32_t l1v;
-    reduce_parent(I, lane == 0, c1, cv1, l1, l1v);
-    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
-    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
-}
-
-// ---- octant reduction with whole-quad fast paths ------------------------------------------------
+// ---- CTA-wide cache of parents by their 8 child ids ----------------------------------------------
 //
-// Lane l owns the level-3 parents ("quads", 4^3 voxels) l and l+32 of the warp's 16^3 octant. It
-// loads the quad as 16 row words (4 voxels along x each) and decides with word compares whether the
-// quad is uniform: then the quad is EMPTY or one leaf and none of its 8 bottom groups needs any
-// work, exactly what Phase 1 + Phase 2 produce for it (a uniform full group becomes a leaf; 8 equal
-// leaves collapse; 8 EMPTY children leave EMPTY). For 8-bit voxels a non-uniform quad's 64 raw
-// bytes then key a CTA-wide cache of the quads this CTA already reduced (the quad's node is a pure
-// function of its voxels), so repeated surface patterns skip the group work too. Parents above the
-// quads are looked up in the same cache by their 8 child ids. Every cache entry also holds the
-// node's LOD value, so hits skip calc_average. Only misses reach the bottom-group path of
-// reduce_tile16 and the global branch table.
+// Parents above the quads are looked up in a small shared cache keyed by their 8 child ids before the
+// global branch table; every entry also holds the node's LOD value, so a hit skips calc_average.
 
 #ifndef VX_NODE_CACHE
 #define VX_NODE_CACHE 64
 #endif
 constexpr int kNodeCache = VX_NODE_CACHE;  // entries (power of two)
-constexpr int kNodeCacheAlloc = VX_TILE_V2 ? kNodeCache : 0;  // entries with shared memory behind them
 
 struct NodeCache {
     uint64_t *key;   // [kNodeCache][8]
@@ -876,7 +511,7 @@ __device__ __forceinline__ void reduce_parent_cached(const DevInterner &I, const
     }
 }
 
-// Nonzero-voxel mask of 8 voxels packed as in load_group32 (voxel j in bits [j*w, (j+1)*w)).
+// Nonzero-voxel mask of 8 voxels packed as in quad_groups (voxel j in bits [j*w, (j+1)*w) of lo:hi).
 template <class T>
 __device__ __forceinline__ uint32_t set_mask8(uint64_t lo, uint64_t hi) {
     if (sizeof(T) == 1) {
@@ -903,151 +538,6 @@ __device__ __forceinline__ void unpack8(uint64_t lo, uint64_t hi, uint32_t v[8])
     }
 }
 
-template <class T>
-__device__ __forceinline__ void reduce_tile16_v2(const DevInterner &I, const T *tile, const KeyCache &C,
-                                                 const NodeCache &N, uint64_t *leaf_cache, uint64_t &oct_id,
-                                                 uint32_t &oct_val) {
-    using W = typename std::conditional<sizeof(T) == 1, uint32_t, uint64_t>::type;  // 4 voxels along x
-    const unsigned lane = threadIdx.x & 31u;
-    const bool wide = sizeof(T) == 2;
-    uint64_t l3[2];
-    uint32_t l3v[2];
-#pragma unroll 1
-    for (int pass = 0; pass < 2; ++pass) {
-        const uint32_t p = lane + 32 * pass;
-        const uint32_t qx = compact3(p), qy = compact3(p >> 1), qz = compact3(p >> 2);
-        const T *qbase = tile + ((4 * qy) * 16 + 4 * qz) * 16 + 4 * qx;
-        // the quad's 16 row words, row r = yy * 4 + zz
-        W w[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) w[r] = *reinterpret_cast<const W *>(qbase + ((r >> 2) * 16 + (r & 3)) * 16);
-        const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
-        const W splat = sizeof(T) == 1 ? (W)(v0 * 0x01010101u) : (W)((uint64_t)v0 * 0x0001000100010001ull);
-        bool uniform = true;
-#pragma unroll
-        for (int r = 0; r < 16; ++r) uniform = uniform && w[r] == splat;
-        uint64_t qid = 0;
-        uint32_t qval = 0;
-        bool active = false;
-        uint64_t key[8];
-        if (uniform) {
-            qid = v0 ? leaf_of<T>(I, leaf_cache, v0) : EMPTY_ID;
-            qval = v0;
-        } else if (sizeof(T) == 1) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) key[i] = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
-            qid = nc_lookup(N, key, 0u, qval);
-            active = qid == 0;
-        } else {
-            active = true;
-        }
-        if (__any_sync(0xFFFFFFFFu, active)) {
-            uint64_t c3[8];
-            uint32_t cv3[8];
-#pragma unroll 1
-            for (int k = 0; k < 8; ++k) {
-                // bottom group k of the quad: rows (2gy + dy, 2gz + dz), voxels 2gx, 2gx + 1
-                const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
-                const T *g = qbase + ((2 * gy) * 16 + 2 * gz) * 16 + 2 * gx;
-                uint64_t lo = 0, hi = 0;
-                if (sizeof(T) == 1) {
-                    const uint32_t p0 = *reinterpret_cast<const uint16_t *>(g);
-                    const uint32_t p1 = *reinterpret_cast<const uint16_t *>(g + 256);
-                    const uint32_t p2 = *reinterpret_cast<const uint16_t *>(g + 16);
-                    const uint32_t p3 = *reinterpret_cast<const uint16_t *>(g + 272);
-                    lo = (uint64_t)(p0 | (p1 << 16)) | ((uint64_t)(p2 | (p3 << 16)) << 32);
-                } else {
-                    lo = (uint64_t)*reinterpret_cast<const uint32_t *>(g) |
-                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 256) << 32);
-                    hi = (uint64_t)*reinterpret_cast<const uint32_t *>(g + 16) |
-                         ((uint64_t)*reinterpret_cast<const uint32_t *>(g + 272) << 32);
-                }
-                const uint32_t set = set_mask8<T>(lo, hi);
-                const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
-                const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
-                                                 : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
-                const bool is_branch = active && set != 0 && !(guni && set == 0xFFu);
-                uint32_t lod = 0;
-                uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
-                const bool need = is_branch && id == 0;
-                const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
-                if (bm) {  // warp-uniform
-                    uint32_t v[8];
-                    unpack8<T>(lo, hi, v);
-                    if (need) lod = calc_average8(v);
-                    unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
-                    if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
-                    grp &= bm;
-                    const int leader = need ? __ffs(grp) - 1 : (int)lane;
-                    const bool lead = need && leader == (int)lane;
-                    uint64_t c[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
-                    bool created;
-                    uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
-                    nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-                    if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
-                    if (need) id = nid;
-                }
-                if (set == 0) {
-                    c3[k] = EMPTY_ID;
-                    cv3[k] = 0;
-                } else if (!is_branch) {  // a uniform full group (or an inactive lane)
-                    c3[k] = active ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
-                    cv3[k] = gv0;
-                } else {
-                    c3[k] = id;
-                    cv3[k] = lod;
-                }
-            }
-            uint64_t pid;
-            uint32_t pval;
-            reduce_parent(I, active, c3, cv3, pid, pval);
-            if (active) {
-                qid = pid;
-                qval = pval;
-                if (sizeof(T) == 1 && pid != INVALID_ID) {
-                    // the key again from the tile (cheaper than keeping 16 registers live)
-#pragma unroll
-                    for (int i = 0; i < 8; ++i)
-                        key[i] = (uint64_t)*reinterpret_cast<const W *>(qbase + (((2 * i) >> 2) * 16 + ((2 * i) & 3)) * 16) |
-                                 ((uint64_t)*reinterpret_cast<const W *>(qbase + (((2 * i + 1) >> 2) * 16 + ((2 * i + 1) & 3)) * 16)
-                                  << 32);
-                    nc_insert(N, key, 0u, pid, pval);
-                }
-            }
-        }
-        l3[pass] = qid;
-        l3v[pass] = qval;
-    }
-    // level 2: lane q < 8 takes quads 8q .. 8q+7 (pass q >> 2)
-    uint64_t c2[8];
-    uint32_t cv2[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int src = (8 * lane + j) & 31;
-        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, l3[0], src), a1 = __shfl_sync(0xFFFFFFFFu, l3[1], src);
-        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, l3v[0], src), b1 = __shfl_sync(0xFFFFFFFFu, l3v[1], src);
-        c2[j] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
-        cv2[j] = lane < 4 ? b0 : b1;
-    }
-    uint64_t l2;
-    uint32_t l2v;
-    reduce_parent_cached(I, N, lane < 8, c2, cv2, l2, l2v);
-    uint64_t c1[8];
-    uint32_t cv1[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        c1[j] = __shfl_sync(0xFFFFFFFFu, l2, j);
-        cv1[j] = __shfl_sync(0xFFFFFFFFu, l2v, j);
-    }
-    uint64_t l1;
-    uint32_t l1v;
-    reduce_parent_cached(I, N, lane == 0, c1, cv1, l1, l1v);
-    oct_id = __shfl_sync(0xFFFFFFFFu, l1, 0);
-    oct_val = __shfl_sync(0xFFFFFFFFu, l1v, 0);
-}
-
 // ---- octant reduction with a device-wide quad memo ---------------------------------------------
 //
 // Terrain repeats: the 4096-chunk dune workload has 508k non-uniform quads (4^3 voxels) but only
@@ -1055,8 +545,8 @@ __device__ __forceinline__ void reduce_tile16_v2(const DevInterner &I, const T *
 // memory (open addressing, 64-bit slots tag:32 | record+1, records = the quad's 16 row words, its node
 // id and LOD value, published by a CAS after the record is written and fenced) replaces the 8-group
 // reduction and the level-3 intern of every repeated quad by one slot load and one record load. Each
-// lane keeps its two quads' probes in flight together. Misses take the bottom-group path of
-// reduce_tile16_v2 and insert the result; the memo only ever holds nodes created or found in this
+// lane keeps its two quads' probes in flight together. Misses take the bottom-group path
+// (quad_groups) and insert the result; the memo only ever holds nodes created or found in this
 // call (no release runs during a build), and inserts stop when its records run out.
 
 template <class T>
@@ -1076,24 +566,15 @@ __device__ __forceinline__ void quad_rows(const T *qbase, typename QuadWord<T>::
     for (int r = 0; r < 16; ++r) w[r] = *quad_row<T, S>(qbase, r);
 }
 
-#ifndef VX_MEMO_L1
-#define VX_MEMO_L1 0
-#endif
 // Bytes of one memo record: 16 row words of 4 voxels, then id (8 B) and LOD value, padded to whole
 // 128-byte lines, so a record never shares a cache line with another.
 __host__ __device__ constexpr size_t memo_stride(size_t voxel_bytes) {
     return ((16 * 4 * voxel_bytes + 16) + 127) & ~(size_t)127;
 }
 
-// A memo slot goes from 0 to its final value once and never changes again. With VX_MEMO_L1 a probe
-// first reads the slot through L1 (a nonzero value there is final) and only re-reads zero from L2.
+// A memo slot goes from 0 to its final value once and never changes again.
 __device__ __forceinline__ uint64_t memo_slot_load(const unsigned long long *slots, uint32_t slot) {
-    const uint64_t *p = reinterpret_cast<const uint64_t *>(slots) + slot;
-    if (VX_MEMO_L1) {
-        const uint64_t v = *p;
-        if (v) return v;
-    }
-    return ld_probe(p);
+    return ld_probe(reinterpret_cast<const uint64_t *>(slots) + slot);
 }
 
 // Record r's address; the record's content is 16 row words of 4 voxels.
@@ -1110,7 +591,7 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
     bool eq = true;
 #pragma unroll
     for (int k = 0; k < 4 * (int)sizeof(T); ++k) {
-        const uint4 x = VX_MEMO_L1 ? rv[k] : __ldcg(rv + k);  // a published record never changes
+        const uint4 x = __ldcg(rv + k);  // a published record never changes
         if (sizeof(T) == 1) {
             eq = eq && x.x == (uint32_t)*quad_row<T, S>(qbase, 4 * k) && x.y == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 1) &&
                  x.z == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 2) && x.w == (uint32_t)*quad_row<T, S>(qbase, 4 * k + 3);
@@ -1121,8 +602,7 @@ __device__ __forceinline__ bool memo_match(const OctArgs &a, uint32_t r, const T
         }
     }
     if (!eq) return false;
-    const uint4 tail = VX_MEMO_L1 ? *reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T))
-                                  : __ldcg(reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T)));
+    const uint4 tail = __ldcg(reinterpret_cast<const uint4 *>(rec + 16 * 4 * sizeof(T)));
     id = (uint64_t)tail.x | ((uint64_t)tail.y << 32);
     lod = tail.z;
     return true;
@@ -1218,7 +698,7 @@ __device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache
 }
 
 template <class T>
-__device__ __forceinline__ void reduce_tile16_v3(const DevInterner &I, const OctArgs &a, const T *tile,
+__device__ __forceinline__ void reduce_tile16(const DevInterner &I, const OctArgs &a, const T *tile,
                                                  const KeyCache &C, const NodeCache &N, uint64_t *leaf_cache,
                                                  uint64_t &oct_id, uint32_t &oct_val) {
     using W = typename QuadWord<T>::type;
@@ -1360,12 +840,12 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
     uint64_t *leaf_cache = kc + 3 * kKeyCache;
     uint64_t *bars = leaf_cache + 256 + warp * 2;
     uint64_t *nc = leaf_cache + 256 + 2 * kOctWarps;
-    uint32_t *u32s = reinterpret_cast<uint32_t *>(nc + 9 * kNodeCacheAlloc);
+    uint32_t *u32s = reinterpret_cast<uint32_t *>(nc + 9 * kNodeCache);
     KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, u32s};
     NodeCache N{nc, nc + 8 * kNodeCache, u32s + kKeyCache};
 
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
-    for (unsigned k = tid; k < kNodeCacheAlloc; k += blockDim.x) N.id[k] = 0;
+    for (unsigned k = tid; k < kNodeCache; k += blockDim.x) N.id[k] = 0;
     if (sizeof(T) == 1)
         for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
     if (lane == 0) {
@@ -1418,13 +898,7 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
         }
         uint64_t node;
         uint32_t val;
-#if VX_TILE_V2 == 3
-        reduce_tile16_v3<T>(I, a, tiles + buf * 4096, C, N, leaf_cache, node, val);
-#elif VX_TILE_V2
-        reduce_tile16_v2<T>(I, tiles + buf * 4096, C, N, leaf_cache, node, val);
-#else
-        reduce_tile16<T>(I, tiles + buf * 4096, C, leaf_cache, node, val);
-#endif
+        reduce_tile16<T>(I, a, tiles + buf * 4096, C, N, leaf_cache, node, val);
         __syncwarp();
         if (kOctTiles == 1 && nx < n_oct && lane == 0) issue(nx, 0);  // single buffer: load after use
         // climb while this warp brings the last child of a parent
@@ -1461,11 +935,7 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
                 ch[j] = __shfl_sync(0xFFFFFFFFu, sid, j);
                 cv[j] = __shfl_sync(0xFFFFFFFFu, sval, j);
             }
-#if VX_TILE_V2
             reduce_parent_cached(I, N, lane == 0, ch, cv, node, val);
-#else
-            reduce_parent(I, lane == 0, ch, cv, node, val);
-#endif
             node = __shfl_sync(0xFFFFFFFFu, node, 0);
             val = __shfl_sync(0xFFFFFFFFu, val, 0);
             q >>= 3;
@@ -1749,66 +1219,20 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
     }
 }
 
-// ---- quads of 32^3 blocks, then one pass per level above them -------------------------------------
+// ---- quads of 16^3 octants, then one pass per level above them ------------------------------------
 //
-// The upper levels of a block are a chain of dependent probes (8^3 nodes, then 16^3, then the block
-// root), which leaves most of a CTA idle when one CTA walks it per block. Here the quad kernel only
-// reduces quads (phase 1 of dense_cta32_kernel: uniformity on row words, the device-wide quad memo,
-// the bottom-group path on misses) and writes them to global memory in per-chunk Morton order; every
-// level above is then one fresh_level_kernel pass over all chunks, one parent per thread, so the
-// probes of a whole level are in flight together. Tiles are double-buffered for 8-bit voxels: the
-// copy of block i+2 is issued when block i is done.
-#ifndef VX_QUAD_BULK1D
-#define VX_QUAD_BULK1D 0
-#endif
-#ifndef VX_QUAD_CACHE
-#define VX_QUAD_CACHE 0
-#endif
+// The upper levels of a chunk are a chain of dependent probes (8^3 nodes, then 16^3, then the root),
+// which leaves most of a CTA idle when one CTA walks it per block. Here the quad kernel only reduces
+// quads (uniformity on row words, the device-wide quad memo, the bottom-group path on misses) and
+// writes them to global memory in per-chunk Morton order; every level above is then one
+// fresh_level_kernel pass over all chunks, one parent per thread, so the probes of a whole level are
+// in flight together.
 #ifndef VX_QUAD_DEDUP
 #define VX_QUAD_DEDUP 1  // identical quads of a warp are looked up once
 #endif
 #ifndef VX_LEVEL_DEDUP
 #define VX_LEVEL_DEDUP 1  // identical parents of a warp probe the table once
 #endif
-constexpr int kQuadCache = VX_QUAD_CACHE;  // entries of the CTA's quad cache (8-bit voxels; power of two)
-
-constexpr int kQuadConsumers = 8;                         // warps reducing quads
-constexpr int kQuadThreads = (kQuadConsumers + 1) * 32;   // plus one warp issuing the copies
-
-#ifndef VX_QUAD_PRIVATE
-#define VX_QUAD_PRIVATE 0  // 1: 8-bit voxels are copied out of the tile per warp and the tile released at once
-#endif
-#ifndef VX_QUAD_TILES
-#define VX_QUAD_TILES 1
-#endif
-
-template <class T>
-struct QuadSmem {
-    static constexpr bool priv = VX_QUAD_PRIVATE && sizeof(T) == 1;
-    static constexpr int tiles = priv ? VX_QUAD_TILES : (sizeof(T) == 1 ? 2 : 1);
-    static constexpr size_t slab = 4 * 32 * 32 * sizeof(T);  // one warp's 4 x 32 x 32 voxels
-    static constexpr int qcache = sizeof(T) == 1 ? kQuadCache : 0;
-    static constexpr size_t tile = 32768 * sizeof(T);
-    static constexpr size_t privs = tiles * tile;                    // kQuadConsumers private slabs
-    static constexpr size_t kc = privs + (priv ? kQuadConsumers * slab : 0);  // 3 * kKeyCache u64
-    static constexpr size_t leaf = kc + 3 * (size_t)kKeyCache * 8;    // 256 u64
-    static constexpr size_t full = leaf + 256 * 8;                   // tiles u64: copy landed
-    static constexpr size_t empty = full + 16;                       // tiles u64: consumers done
-    static constexpr size_t qid = empty + 16;                        // qcache u64: node id (0 free, 1 busy)
-    static constexpr size_t qwords = qid + (size_t)qcache * 8;       // qcache x 16 u32: the quad's rows
-    static constexpr size_t kcval = qwords + (size_t)qcache * 64;    // kKeyCache u32
-    static constexpr size_t qtag = kcval + (size_t)kKeyCache * 4;    // qcache u32: second hash
-    static constexpr size_t qlod = qtag + (size_t)qcache * 4;        // qcache u32: LOD value
-    static constexpr size_t total = qlod + (size_t)qcache * 4;
-};
-
-// CTA-wide cache of quads (8-bit voxels) in front of the device-wide memo: popular quads hit here
-// instead of sending every warp of the GPU to the same L2 lines.
-struct QuadCache {
-    uint64_t *id;
-    uint32_t *words, *tag, *lod;
-    int n;  // entries (0: none)
-};
 
 template <class T, int S>
 __device__ __forceinline__ bool rows_equal(const T *a, const T *b) {
@@ -1818,59 +1242,13 @@ __device__ __forceinline__ bool rows_equal(const T *a, const T *b) {
     return eq;
 }
 
-template <class T, int S>
-__device__ __forceinline__ uint64_t qc_lookup(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase,
-                                              uint32_t &lod) {
-    if (sizeof(T) != 1 || Q.n == 0) return 0;
-    uint32_t h = (h1 >> 7) & (Q.n - 1);
-#pragma unroll 1
-    for (int p = 0; p < 4; ++p) {
-        const uint64_t id = *(volatile uint64_t *)(Q.id + h);
-        if (id == 0) return 0;
-        if (id > 1 && *(volatile uint32_t *)(Q.tag + h) == h2) {
-            bool eq = true;
-            const volatile uint32_t *w = Q.words + 16 * h;
-#pragma unroll
-            for (int r = 0; r < 16; ++r) eq = eq && w[r] == (uint32_t)*quad_row<T, S>(qbase, r);
-            if (eq) {
-                lod = *(volatile uint32_t *)(Q.lod + h);
-                return id;
-            }
-        }
-        h = (h + 1) & (Q.n - 1);
-    }
-    return 0;
-}
-
-template <class T, int S>
-__device__ __forceinline__ void qc_insert(const QuadCache &Q, uint32_t h1, uint32_t h2, const T *qbase, uint64_t id,
-                                          uint32_t lod) {
-    if (sizeof(T) != 1 || Q.n == 0) return;
-    uint32_t h = (h1 >> 7) & (Q.n - 1);
-#pragma unroll 1
-    for (int p = 0; p < 4; ++p) {
-        if (atomicCAS((unsigned long long *)(Q.id + h), 0ull, 1ull) == 0ull) {
-#pragma unroll
-            for (int r = 0; r < 16; ++r) Q.words[16 * h + r] = (uint32_t)*quad_row<T, S>(qbase, r);
-            Q.tag[h] = h2;
-            Q.lod[h] = lod;
-            __threadfence_block();
-            *(volatile uint64_t *)(Q.id + h) = id;
-            return;
-        }
-        h = (h + 1) & (Q.n - 1);
-    }
-}
-
-// 64 quads reduced by one warp, two per lane: uniformity on row words, the quad memo, the bottom-group
-// path on misses; results to oid/oval in Morton order (when given) and to lane_out/lane_val[p] for
-// the lane's quad p (when given). S = 32: the quads of slab `qy` (4 voxels thick
-// in y, [4][32][32] voxels at `tile`) of a 32^3 block; S = 16: all quads of the 16^3 octant at `tile`.
-template <class T, int S>
-__device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArgs &a, const T *tile, uint32_t qy,
-                                              const KeyCache &C, const QuadCache &Q, uint64_t *leaf_cache,
-                                              uint64_t *oid, uint32_t *oval, uint64_t *lane_out = nullptr,
-                                              uint32_t *lane_val = nullptr) {
+// The 64 quads of the 16^3 octant at `tile` ([y][z][x]) reduced by one warp, two per lane: uniformity
+// on row words, the quad memo, the bottom-group path on misses; results to oid/oval in Morton order.
+template <class T>
+__device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArgs &a, const T *tile,
+                                              const KeyCache &C, uint64_t *leaf_cache, uint64_t *oid,
+                                              uint32_t *oval) {
+    constexpr int S = 16;
     using W = typename QuadWord<T>::type;
     const unsigned lane = threadIdx.x & 31u;
     const bool memo = a.memo_slots != nullptr;
@@ -1881,15 +1259,9 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
     uint32_t qvalv[2];
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
-        if (S == 32) {
-            const uint32_t qx = lane & 7u, qz = (lane >> 3) + 4u * p;
-            qm[p] = spread3b(qx) | (spread3b(qy) << 1) | (spread3b(qz) << 2);
-            qb[p] = tile + (4 * qz) * 32 + 4 * qx;
-        } else {
-            const uint32_t q = lane + 32u * p, qx = compact3(q), qyy = compact3(q >> 1), qz = compact3(q >> 2);
-            qm[p] = q;
-            qb[p] = tile + ((4 * qyy) * 16 + 4 * qz) * 16 + 4 * qx;
-        }
+        const uint32_t q = lane + 32u * p, qx = compact3(q), qy = compact3(q >> 1), qz = compact3(q >> 2);
+        qm[p] = q;
+        qb[p] = tile + ((4 * qy) * 16 + 4 * qz) * 16 + 4 * qx;
         W w[16];
         quad_rows<T, S>(qb[p], w);
         const uint32_t v0 = (uint32_t)(w[0] & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu));
@@ -1928,7 +1300,6 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
         const T *lq = reinterpret_cast<const T *>(
             __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(qb[p]), leader[p]));
         follow[p] = !uni[p] && leader[p] != (int)lane && rows_equal<T, S>(qb[p], lq);
-        if (!uni[p] && !follow[p]) qidv[p] = qc_lookup<T, S>(Q, h1[p], h2[p], qb[p], qvalv[p]);
     }
     {  // memo probes, both quads in flight
         bool look[2];
@@ -1950,7 +1321,6 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
                 } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
                            memo_match<T, S>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
                     look[p] = false;
-                    qc_insert<T, S>(Q, h1[p], h2[p], qb[p], qidv[p], qvalv[p]);
                 } else if (step == 3) {
                     look[p] = false;
                 } else {
@@ -1970,10 +1340,7 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             if (active) {
                 qidv[p] = pid;
                 qvalv[p] = pval;
-                if (pid != INVALID_ID) {
-                    if (memo) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
-                    qc_insert<T, S>(Q, h1[p], h2[p], qb[p], pid, pval);
-                }
+                if (memo && pid != INVALID_ID) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
             }
         }
         const uint64_t lid = __shfl_sync(0xFFFFFFFFu, qidv[p], leader[p]);
@@ -1982,31 +1349,20 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             qidv[p] = lid;
             qvalv[p] = lval;
         }
-        if (oid) {
-            oid[qm[p]] = qidv[p];
-            oval[qm[p]] = qvalv[p];
-        }
-        if (lane_out) {
-            lane_out[p] = qidv[p];
-            lane_val[p] = qvalv[p];
-        }
+        oid[qm[p]] = qidv[p];
+        oval[qm[p]] = qvalv[p];
     }
 }
 
-__device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool in, const uint64_t c[8],
-                                                    const uint32_t cv[8], uint64_t &out, uint32_t &val);
-
 // ---- quads of 16^3 octants, one warp each, with no coupling between warps ----------------------------
-// Each warp streams its own octants through its own two tiles (4-D TMA box of 16^3, the copy of octant
-// i+2 issued as soon as octant i has been reduced), so a warp slowed by memo misses holds back nobody.
-#ifndef VX_QUADS16
-#define VX_QUADS16 1
-#endif
+// Each warp streams its own octants through its own tile (4-D TMA box of 16^3; the copy of the next
+// octant is issued as soon as the current one has been reduced), so a warp slowed by memo misses
+// holds back nobody.
 #ifndef VX_Q16_TILES
 #define VX_Q16_TILES 1  // 1: more resident warps beat prefetching within a warp (measured)
 #endif
-#ifndef VX_Q16_LEVELS
-#define VX_Q16_LEVELS 0  // 1: the warp also reduces its octant's 8^3 nodes and the octant node
+#ifndef VX_Q16_DYNAMIC
+#define VX_Q16_DYNAMIC 1  // octants after each warp's first one come from a device-wide counter
 #endif
 #ifndef VX_Q16_MINB
 #define VX_Q16_MINB 4  // resident CTAs per SM the register allocation must allow
@@ -2036,7 +1392,6 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bars) + warp * NT;
     T *tiles = reinterpret_cast<T *>(smem + (size_t)warp * NT * L::tile);
     KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
-    QuadCache Q{nullptr, nullptr, nullptr, nullptr, 0};
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     if (sizeof(T) == 1)
         for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
@@ -2063,8 +1418,12 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
     if (lane == 0)
         for (int b = 0; b < NT; ++b)
             if (gw + b * total < n_oct) issue(gw + b * total, b);
+    // With one tile per warp the octants after the first are handed out by a device-wide counter:
+    // octant cost varies by an order of magnitude (uniform air or rock against dune surface), and a
+    // fixed stride gives every warp the same octant position in each of its chunks.
+    const bool dyn = VX_Q16_DYNAMIC && NT == 1 && a.work != nullptr;
     uint32_t j = 0;
-    for (uint64_t o = gw; o < n_oct; o += total, ++j) {
+    for (uint64_t o = gw, next = 0; o < n_oct; o = next, ++j) {
         const int b = (int)(j % NT);
         const uint32_t use = j / NT;
         bool ok = false;
@@ -2077,51 +1436,20 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
                 }
             return;
         }
+        if (dyn) {  // claimed now, so the atomic's round trip overlaps this octant's work
+            unsigned long long nx = 0;
+            if (lane == 0) nx = atomicAdd(a.work, 1ull);
+            next = total + __shfl_sync(0xFFFFFFFFu, nx, 0);
+        } else {
+            next = o + total;
+        }
         const uint32_t c = (uint32_t)(o >> ob);
         const uint64_t q = o & ((1ull << ob) - 1);
         const uint32_t tree = a.trees[c];
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 6);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 6);
-        if (VX_Q16_LEVELS) {  // q_ids / q_vals hold octant nodes: n_chunks x 8^(d-4)
-            uint64_t qid2[2];
-            uint32_t qval2[2];
-            const bool ok_tree = tree < I.tree_cap && I.depths[tree] == d;
-            if (ok_tree) {
-                quads_of_tile<T, 16>(I, a, tiles + (size_t)b * 4096, 0, C, Q, leaf_cache, nullptr, nullptr, qid2,
-                                     qval2);
-            } else {
-                if (lane == 0) set_error(I, ERR_INVALID, 34);
-                qid2[0] = qid2[1] = EMPTY_ID;
-                qval2[0] = qval2[1] = 0;
-            }
-            // 8^3 nodes: lane j < 8 takes quads 8j .. 8j+7 (pass j >> 2)
-            uint64_t ch[8];
-            uint32_t cv[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const int src = (8 * lane + k) & 31;
-                const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, qid2[0], src), a1 = __shfl_sync(0xFFFFFFFFu, qid2[1], src);
-                const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, qval2[0], src), b1 = __shfl_sync(0xFFFFFFFFu, qval2[1], src);
-                ch[k] = lane < 8 ? (lane < 4 ? a0 : a1) : 0ull;
-                cv[k] = lane < 4 ? b0 : b1;
-            }
-            uint64_t o2;
-            uint32_t v2;
-            reduce_parent_dedup(I, lane < 8, ch, cv, o2, v2);
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                ch[k] = __shfl_sync(0xFFFFFFFFu, o2, k);
-                cv[k] = __shfl_sync(0xFFFFFFFFu, v2, k);
-            }
-            uint64_t o1;
-            uint32_t v1;
-            reduce_parent_dedup(I, lane == 0, ch, cv, o1, v1);
-            if (lane == 0) {
-                q_ids[((uint64_t)c << ob) + q] = o1;
-                q_vals[((uint64_t)c << ob) + q] = v1;
-            }
-        } else if (tree < I.tree_cap && I.depths[tree] == d) {
-            quads_of_tile<T, 16>(I, a, tiles + (size_t)b * 4096, 0, C, Q, leaf_cache, oid, oval);
+        if (tree < I.tree_cap && I.depths[tree] == d) {
+            quads_of_tile<T>(I, a, tiles + (size_t)b * 4096, C, leaf_cache, oid, oval);
         } else {
             if (lane == 0) set_error(I, ERR_INVALID, 34);
             for (unsigned k = lane; k < 64; k += 32) {
@@ -2130,117 +1458,8 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
             }
         }
         __syncwarp();
-        const uint64_t ahead = o + (uint64_t)NT * total;
+        const uint64_t ahead = NT == 1 ? next : o + (uint64_t)NT * total;
         if (lane == 0 && ahead < n_oct) issue(ahead, b);
-    }
-}
-
-// One CTA streams 32^3 blocks through its tiles: warp kQuadConsumers (the producer) issues the copy of
-// each block as soon as the tile it goes to has been released; every consumer warp waits for the copy,
-// reduces its slab and releases the tile (an mbarrier arrival), so consumer warps never wait on one
-// another and a warp slowed by memo misses only holds back the copy two blocks ahead.
-template <class T>
-__global__ void __launch_bounds__(kQuadThreads) dense_quads_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
-                                                                  uint32_t *q_vals,
-                                                                  const __grid_constant__ CUtensorMap tmap) {
-    using L = QuadSmem<T>;
-    extern __shared__ __align__(128) unsigned char smem[];
-    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    uint64_t *kc = reinterpret_cast<uint64_t *>(smem + L::kc);
-    uint64_t *leaf_cache = reinterpret_cast<uint64_t *>(smem + L::leaf);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + L::full);
-    uint64_t *empty = reinterpret_cast<uint64_t *>(smem + L::empty);
-    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
-    QuadCache Q{reinterpret_cast<uint64_t *>(smem + L::qid), reinterpret_cast<uint32_t *>(smem + L::qwords),
-                reinterpret_cast<uint32_t *>(smem + L::qtag), reinterpret_cast<uint32_t *>(smem + L::qlod), L::qcache};
-    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
-    if (L::qcache)
-        for (unsigned k = tid; k < (unsigned)L::qcache; k += blockDim.x) Q.id[k] = 0;
-    if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
-    if (tid == 0) {
-        for (int b = 0; b < L::tiles; ++b) {
-            mbar_init(full + b, 1);
-            mbar_init(empty + b, kQuadConsumers);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
-    const int d = a.depth;
-    const int bb = 3 * (d - 5);
-    const uint64_t n_blk = (uint64_t)a.n_chunks << bb;
-    const uint64_t per_chunk = 1ull << (3 * (d - 2));  // quads per chunk
-    if (warp == kQuadConsumers) {  // producer
-        if (lane != 0) return;
-        uint32_t j = 0;
-        for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x, ++j) {
-            const int b = (int)(j % L::tiles);
-            const uint32_t use = j / L::tiles;
-            if (use > 0) {  // wait until every consumer released this tile's previous block
-                bool ok = false;
-                for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-                    if ((ok = mbar_try_wait(empty + b, (use - 1) & 1u))) break;
-                if (!ok) {
-                    set_error(I, ERR_TIMEOUT, 32);
-                    return;  // no copy of this CTA is in flight: every issued one was consumed or waited
-                }
-            }
-            const uint32_t c = (uint32_t)(blk >> bb);
-            const uint32_t q = (uint32_t)(blk & ((1ull << bb) - 1));
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(full + b, (uint32_t)L::tile);
-            if (VX_QUAD_BULK1D && bb == 0)  // a MaxDepth-5 chunk is one contiguous 32^3 block
-                bulk_copy_g2s(smem + b * L::tile, static_cast<const unsigned char *>(a.grids) + (size_t)c * L::tile,
-                              (uint32_t)L::tile, full + b);
-            else
-                tma_load_block32(smem + b * L::tile, &tmap, (int)(compact3(q) * 32), (int)(compact3(q >> 2) * 32),
-                                 (int)(compact3(q >> 1) * 32), (int)c, full + b);
-        }
-        return;
-    }
-    uint32_t j = 0;
-    for (uint64_t blk = blockIdx.x; blk < n_blk; blk += gridDim.x, ++j) {
-        const int b = (int)(j % L::tiles);
-        const uint32_t use = j / L::tiles;
-        bool ok = false;
-        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-            if ((ok = mbar_try_wait(full + b, use & 1u))) break;
-        if (!__all_sync(0xFFFFFFFFu, ok)) {
-            // give up: the copy may still land, so keep waiting for it (bounded) before leaving
-            if (lane == 0) set_error(I, ERR_TIMEOUT, 29);
-            for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(full + b, use & 1u); ++spin) {
-            }
-            return;
-        }
-        const uint32_t c = (uint32_t)(blk >> bb);
-        const uint64_t q = blk & ((1ull << bb) - 1);
-        const uint32_t tree = a.trees[c];
-        const bool bad = tree >= I.tree_cap || I.depths[tree] != d;  // the same answer in every thread
-        uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 9);
-        uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 9);
-        const T *slab = reinterpret_cast<const T *>(smem + b * L::tile + warp * L::slab);
-        if (L::priv) {  // copy the slab out (4 KiB, 128 B a lane) and hand the tile back at once
-            const uint4 *src = reinterpret_cast<const uint4 *>(slab);
-            uint4 *dst = reinterpret_cast<uint4 *>(smem + L::privs + warp * L::slab);
-#pragma unroll
-            for (int k = 0; k < (int)(L::slab / 16 / 32); ++k) dst[k * 32 + lane] = src[k * 32 + lane];
-            __syncwarp();
-            if (lane == 0) mbar_arrive(empty + b);
-            slab = reinterpret_cast<const T *>(dst);
-        }
-        if (!bad) {
-            quads_of_tile<T, 32>(I, a, slab, warp, C, Q, leaf_cache, oid, oval);
-        } else {
-            if (tid == 0) set_error(I, ERR_INVALID, 31);
-            for (unsigned k = lane; k < 64; k += 32) {
-                const uint32_t qm = spread3b(k & 7u) | (spread3b(warp) << 1) | (spread3b(k >> 3) << 2);
-                oid[qm] = EMPTY_ID;
-                oval[qm] = 0;
-            }
-        }
-        __syncwarp();
-        if (!L::priv && lane == 0) mbar_arrive(empty + b);
     }
 }
 
@@ -2494,10 +1713,8 @@ static int prepare_kernel(const void *kernel, int threads, size_t smem, cudaErro
     return per_sm;
 }
 
-size_t dense32_smem_bytes(int vbytes) { return (size_t)32768 * vbytes + (3 * kKeyCache + 256 + 8) * 8 + 8 * 4 + 64; }
-
-size_t dense_smem_bytes(int bdepth, int vbytes) {
-    const size_t V = (size_t)1 << (3 * bdepth);
+size_t dense_smem_bytes(int depth, int vbytes) {
+    const size_t V = (size_t)1 << (3 * depth);
     const size_t n_nodes = (V - 1) / 7;
     const size_t vox = (V * vbytes + 127) & ~(size_t)127;
     return vox + n_nodes * 8 + ((n_nodes + 1) & ~(size_t)1) * 4 + 256 * 8 + 16;
@@ -2506,7 +1723,7 @@ size_t dense_smem_bytes(int bdepth, int vbytes) {
 template <class K>
 static cudaError_t launch_persistent(K kernel, const DevInterner &I, const DenseArgs &a, size_t smem, int num_sms,
                                     cudaStream_t s) {
-    const uint64_t total = (uint64_t)a.n_chunks * a.blocks_per_chunk;
+    const uint64_t total = a.n_chunks;
     cudaError_t e = cudaSuccess;
     const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kThreads, smem, &e);
     if (e != cudaSuccess) return e;
@@ -2519,13 +1736,9 @@ static cudaError_t launch_persistent(K kernel, const DevInterner &I, const Dense
 
 
 cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s) {
-    if ((uint64_t)a.n_chunks * a.blocks_per_chunk == 0) return cudaSuccess;
-    if (a.bdepth == 5) {
-        const size_t smem = dense32_smem_bytes(I.vbits / 8);
-        if (I.vbits == 8) return launch_persistent(dense32_kernel<uint8_t>, I, a, smem, num_sms, s);
-        return launch_persistent(dense32_kernel<uint16_t>, I, a, smem, num_sms, s);
-    }
-    const size_t smem = dense_smem_bytes(a.bdepth, I.vbits / 8);
+    if (a.n_chunks == 0) return cudaSuccess;
+    if (a.depth < 2 || a.depth > 3) return cudaErrorInvalidValue;
+    const size_t smem = dense_smem_bytes(a.depth, I.vbits / 8);
     if (I.vbits == 8) return launch_persistent(dense_blocks_kernel<uint8_t>, I, a, smem, num_sms, s);
     return launch_persistent(dense_blocks_kernel<uint16_t>, I, a, smem, num_sms, s);
 }
@@ -2627,7 +1840,7 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     const size_t smem = (size_t)kOctWarps * kOctTiles * 4096 * es +
-                        (3 * kKeyCache + 256 + 2 * kOctWarps + 9 * kNodeCacheAlloc) * 8 + (kKeyCache + kNodeCacheAlloc) * 4 + 64;
+                        (3 * kKeyCache + 256 + 2 * kOctWarps + 9 * kNodeCache) * 8 + (kKeyCache + kNodeCache) * 4 + 64;
     const uint64_t n_oct = (uint64_t)n_chunks << (3 * (depth - 4));
     auto launch = [&](auto kernel) -> cudaError_t {
         cudaError_t e = cudaSuccess;
@@ -2687,10 +1900,9 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
         a.memo_recs = reinterpret_cast<unsigned char *>(m + sl * 8 + 256);
         a.memo_mask = (uint32_t)(sl - 1);
         a.memo_cap = (uint32_t)rc;
-        if (clear_memo) {
-            cudaError_t e = cudaMemsetAsync(m, 0, sl * 8 + 256, s);
-            if (e != cudaSuccess) return e;
-        }
+        a.work = reinterpret_cast<unsigned long long *>(m + sl * 8 + 128);  // in the header the clear zeroes
+        cudaError_t e = clear_memo ? cudaMemsetAsync(m, 0, sl * 8 + 256, s) : cudaMemsetAsync(a.work, 0, 8, s);
+        if (e != cudaSuccess) return e;
     }
     // level k (k = 1 .. depth-2, quads at k = depth-2) holds n_chunks * 8^k nodes
     size_t off[12] = {0}, total = 0;
@@ -2707,65 +1919,30 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     CUtensorMap tmap;
     cuuint64_t dims[4] = {side, side, side, n_chunks};
     cuuint64_t strides[3] = {side * es, side * side * es, side * side * side * es};
-    cuuint32_t box[4] = {32, 32, 32, 1};
+    cuuint32_t box[4] = {16, 16, 16, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = CUDA_SUCCESS;
-    if (!VX_QUADS16) {  // the 16^3 kernel encodes its own map below
-        r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
-                   const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-    }
-    const bool oct_levels = VX_QUADS16 && VX_Q16_LEVELS;
-    uint64_t *q_ids = ids + off[oct_levels ? depth - 4 : depth - 2];
-    uint32_t *q_vals = vals + off[oct_levels ? depth - 4 : depth - 2];
-    auto launchq = [&](auto kernel, size_t smem) -> cudaError_t {
-        cudaError_t e = cudaSuccess;
-        const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQuadThreads, smem, &e);
-        if (e != cudaSuccess) return e;
+    CUresult r = encode(&tmap, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                        const_cast<void *>(grids), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    uint64_t *q_ids = ids + off[depth - 2];
+    uint32_t *q_vals = vals + off[depth - 2];
+    auto launch16 = [&](auto kernel, size_t smem) -> cudaError_t {
+        cudaError_t e2 = cudaSuccess;
+        const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQ16Warps * 32, smem, &e2);
+        if (e2 != cudaSuccess) return e2;
         uint64_t grid = (uint64_t)num_sms * per_sm;
-        const uint64_t need = (uint64_t)n_chunks << (3 * (depth - 5));
+        const uint64_t need = (((uint64_t)n_chunks << (3 * (depth - 4))) + kQ16Warps - 1) / kQ16Warps;
         if (grid > need) grid = need;
         count_launches(1);
-        kernel<<<(unsigned)grid, kQuadThreads, smem, s>>>(I, a, q_ids, q_vals, tmap);
+        kernel<<<(unsigned)grid, kQ16Warps * 32, smem, s>>>(I, a, q_ids, q_vals, tmap);
         return cudaGetLastError();
     };
-    cudaError_t e = cudaSuccess;
-    if (VX_QUADS16) {
-        CUtensorMap tmap16;
-        cuuint32_t box16[4] = {16, 16, 16, 1};
-        r = encode(&tmap16, es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
-                   const_cast<void *>(grids), dims, strides, box16, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-        auto launch16 = [&](auto kernel, size_t smem) -> cudaError_t {
-            cudaError_t e2 = cudaSuccess;
-            const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQ16Warps * 32, smem, &e2);
-            if (e2 != cudaSuccess) return e2;
-            uint64_t grid = (uint64_t)num_sms * per_sm;
-            const uint64_t need = (((uint64_t)n_chunks << (3 * (depth - 4))) + kQ16Warps - 1) / kQ16Warps;
-            if (grid > need) grid = need;
-            count_launches(1);
-            kernel<<<(unsigned)grid, kQ16Warps * 32, smem, s>>>(I, a, q_ids, q_vals, tmap16);
-            return cudaGetLastError();
-        };
-        e = es == 1 ? launch16(dense_quads16_kernel<uint8_t>, Q16Smem<uint8_t>::total)
-                    : launch16(dense_quads16_kernel<uint16_t>, Q16Smem<uint16_t>::total);
-    } else {
-        e = es == 1 ? launchq(dense_quads_kernel<uint8_t>, QuadSmem<uint8_t>::total)
-                    : launchq(dense_quads_kernel<uint16_t>, QuadSmem<uint16_t>::total);
-    }
+    cudaError_t e = es == 1 ? launch16(dense_quads16_kernel<uint8_t>, Q16Smem<uint8_t>::total)
+                            : launch16(dense_quads16_kernel<uint16_t>, Q16Smem<uint16_t>::total);
     if (e != cudaSuccess) return e;
     if (levels_begin) (*levels_begin)(levels_ctx);
-    if (oct_levels) {  // passes above the octant nodes, the last one commits the roots
-        for (int k = depth - 5; k >= 0; --k) {
-            const uint64_t np = (uint64_t)n_chunks << (3 * k);
-            e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], k > 0 ? ids + off[k] : nullptr,
-                                   k > 0 ? vals + off[k] : nullptr, np, k == 0, trees, changed, s);
-            if (e != cudaSuccess) return e;
-        }
-        return cudaSuccess;
-    }
     for (int k = depth - 3; k >= 3; --k) {
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
         e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], ids + off[k], vals + off[k], np, false, trees,

@@ -20,7 +20,6 @@
 using namespace vxg;
 
 namespace vxg {
-size_t dense_smem_bytes(int bdepth, int vbytes);
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 }
@@ -606,71 +605,27 @@ void batch_from_dense(vx_batch *b, const void *grid) {
 }
 
 // Fused dense construction on EMPTY trees (vx_build.cu). All arguments in device memory.
-#ifndef VX_DENSE_OCTANTS
-#define VX_DENSE_OCTANTS 1
-#endif
-#ifndef VX_DENSE_SPLIT
-#define VX_DENSE_SPLIT 1  // depth >= 5: quad kernel + one pass per level (else the fused per-block kernel)
-#endif
-
 int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void *d_grids, uint8_t *d_changed,
                int depth) {
     cudaStream_t s = it->stream;
-    if (VX_DENSE_SPLIT && depth >= 5) {
+    if (depth >= 5) {  // quad kernel, then one pass per level
         const size_t sb = (dense_split_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
         PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
         VX_CUDA(launch_dense_split(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
                                    static_cast<char *>(it->ws.p) + sb, true, 0, &PhaseSwitch::next, &ps));
-    } else if (VX_DENSE_OCTANTS && depth >= 4) {
+    } else if (depth == 4) {  // one warp per chunk
         const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
         Phase ph(it, VX_PROF_DENSE);
         VX_CUDA(launch_dense_octants(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
                                      static_cast<char *>(it->ws.p) + sb));
-    } else if (depth > 5) {
-        // 32^3 blocks, then one launch per level above them
-        DenseArgs a{};
-        a.grids = d_grids;
-        a.trees = d_trees;
-        a.n_chunks = n;
-        a.depth = depth;
-        a.bdepth = 5;
-        a.blocks_per_chunk = 1u << (3 * (depth - 5));
-        a.changed = d_changed;
-        size_t total = 0;
-        for (int k = depth - 5; k >= 1; --k) total += (size_t)n << (3 * k);
-        VX_CUDA(it->ws.reserve(Carve::need({total * 8, total * 4}) + 1024));
-        Carve c(it->ws.p);
-        uint64_t *ids = c.take<uint64_t>(total);
-        uint32_t *vals = c.take<uint32_t>(total);
-        a.block_roots = ids;
-        a.block_vals = vals;
-        {
-            Phase ph(it, VX_PROF_DENSE);
-            VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
-        }
-        Phase ph(it, VX_PROF_LEVELS);
-        uint64_t *in_ids = ids;
-        uint32_t *in_vals = vals;
-        size_t off = (size_t)n << (3 * (depth - 5));
-        for (int k = depth - 6; k >= 0; --k) {
-            const uint64_t np = (uint64_t)n << (3 * k);
-            uint64_t *out_ids = k > 0 ? ids + off : nullptr;
-            uint32_t *out_vals = k > 0 ? vals + off : nullptr;
-            VX_CUDA(launch_fresh_level(it->dev, in_ids, in_vals, out_ids, out_vals, np, k == 0, d_trees, d_changed, s));
-            in_ids = out_ids;
-            in_vals = out_vals;
-            off += np;
-        }
     } else {
         DenseArgs a{};
         a.grids = d_grids;
         a.trees = d_trees;
         a.n_chunks = n;
         a.depth = depth;
-        a.bdepth = depth;
-        a.blocks_per_chunk = 1;
         a.changed = d_changed;
         Phase ph(it, VX_PROF_DENSE);
         VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
@@ -1304,7 +1259,7 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
         }
         return st;
     }
-    if (mem == VX_MEM_HOST && VX_DENSE_OCTANTS && d >= 4 && n >= 2 * kCopyPieces) {
+    if (mem == VX_MEM_HOST && d >= 4 && n >= 2 * kCopyPieces) {
         // pipelined: the grids go over in kCopyPieces pieces on a copy stream; piece k is built on
         // the interner's stream as soon as its copy lands, while piece k+1 is still in flight
         if (!it->copy_stream) {
@@ -1316,7 +1271,7 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
         uint32_t *dt = c.take<uint32_t>(n);
         uint8_t *dg = c.take<uint8_t>(per * n);
         uint8_t *dc = c.take<uint8_t>(n);
-        const bool split = VX_DENSE_SPLIT && d >= 5;
+        const bool split = d >= 5;
         const size_t sb = ((split ? dense_split_scratch_bytes(n, d) : dense_octant_scratch_bytes(n, d)) + 255) &
                           ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, d, it->vbits)));

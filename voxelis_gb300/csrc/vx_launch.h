@@ -16,14 +16,10 @@ struct DenseArgs {
     const void *grids;           // n_chunks * side^3 voxels, [y][z][x] per chunk
     const uint32_t *trees;       // tree handle per chunk
     uint32_t n_chunks;
-    int depth;                   // chunk depth d (2..10)
-    int bdepth;                  // depth of one shared-memory block, min(d, 5)
-    uint32_t blocks_per_chunk;   // 8^(d - bdepth)
-    uint64_t *block_roots;       // [n_chunks * blocks_per_chunk] when d > bdepth
-    uint32_t *block_vals;        // LOD values of block roots
+    int depth;                   // chunk depth d (2..3)
     uint8_t *changed;            // [n_chunks] or null
 };
-// Builds the level-(d - bdepth) subtrees of every chunk (or the whole tree when d <= 5).
+// Builds whole chunks of depth 2 or 3, one CTA per chunk (staged in shared memory by one bulk copy).
 cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s);
 
 // Fused dense construction for chunk depths 4..10: warps take 16^3 octants (TMA tensor copies),

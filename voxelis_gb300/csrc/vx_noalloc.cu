@@ -103,8 +103,6 @@ extern "C" int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree
         a.trees = trees_dev;
         a.n_chunks = n;
         a.depth = max_depth;
-        a.bdepth = max_depth;
-        a.blocks_per_chunk = 1;
         a.changed = changed_dev;
         e = launch_dense_blocks(D, a, num_sms, s);
     }
