@@ -1355,9 +1355,9 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
 }
 
 // ---- quads of 16^3 octants, one warp each, with no coupling between warps ----------------------------
-// Each warp streams its own octants through its own tile (4-D TMA box of 16^3; the copy of the next
-// octant is issued as soon as the current one has been reduced), so a warp slowed by memo misses
-// holds back nobody.
+// Each warp streams its own octants through its own tile(s) (4-D TMA box of 16^3; the copy of the next
+// octant is issued as soon as a tile has been reduced), so a warp slowed by memo misses holds back
+// nobody.
 #ifndef VX_Q16_TILES
 #define VX_Q16_TILES 1  // 1: more resident warps beat prefetching within a warp (measured)
 #endif
@@ -1415,40 +1415,50 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
         tma_load_octant(tiles + (size_t)b * 4096, &tmap, (int)(compact3(q) * 16), (int)(compact3(q >> 2) * 16),
                         (int)(compact3(q >> 1) * 16), (int)c, bars + b);
     };
-    if (lane == 0)
-        for (int b = 0; b < NT; ++b)
-            if (gw + b * total < n_oct) issue(gw + b * total, b);
-    // With one tile per warp the octants after the first are handed out by a device-wide counter:
-    // octant cost varies by an order of magnitude (uniform air or rock against dune surface), and a
-    // fixed stride gives every warp the same octant position in each of its chunks.
-    const bool dyn = VX_Q16_DYNAMIC && NT == 1 && a.work != nullptr;
-    uint32_t j = 0;
-    for (uint64_t o = gw, next = 0; o < n_oct; o = next, ++j) {
+    // Octants in the order this warp claimed them; fifo[0] is in tile j % NT. The first NT are fixed
+    // (gw + b * total); later ones come from a device-wide counter: octant cost varies by an order of
+    // magnitude (uniform air or rock against dune surface), and a fixed stride would give a warp the
+    // same octant position in each of its chunks. Claims only grow, so once fifo[0] is past the end
+    // every later one is too and no copy is left in flight.
+    const bool dyn = VX_Q16_DYNAMIC && a.work != nullptr;
+    uint64_t fifo[NT];
+#pragma unroll
+    for (int b = 0; b < NT; ++b) {
+        fifo[b] = gw + b * total;
+        if (lane == 0 && fifo[b] < n_oct) issue(fifo[b], b);
+    }
+    for (uint32_t j = 0; fifo[0] < n_oct; ++j) {
+        const uint64_t o = fifo[0];
         const int b = (int)(j % NT);
-        const uint32_t use = j / NT;
-        bool ok = false;
-        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
-            if ((ok = mbar_try_wait(bars + b, use & 1u))) break;
-        if (!__all_sync(0xFFFFFFFFu, ok)) {  // give up: wait (bounded) for this warp's copies, then leave
-            if (lane == 0) set_error(I, ERR_TIMEOUT, 33);
-            for (int bb = 0; bb < NT; ++bb)
-                for (uint32_t spin = 0; spin < SPIN_LIMIT && !mbar_try_wait(bars + bb, ((j + bb) / NT) & 1u); ++spin) {
-                }
-            return;
-        }
-        if (dyn) {  // claimed now, so the atomic's round trip overlaps this octant's work
-            unsigned long long nx = 0;
-            if (lane == 0) nx = atomicAdd(a.work, 1ull);
-            next = total + __shfl_sync(0xFFFFFFFFu, nx, 0);
-        } else {
-            next = o + total;
-        }
         const uint32_t c = (uint32_t)(o >> ob);
         const uint64_t q = o & ((1ull << ob) - 1);
+        // the tree check's two dependent loads go out before the wait, beside the tile's copy
         const uint32_t tree = a.trees[c];
+        const bool tree_ok = tree < I.tree_cap && I.depths[tree] == d;
+        bool ok = false;
+        for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
+            if ((ok = mbar_try_wait(bars + b, (j / NT) & 1u))) break;
+        if (!__all_sync(0xFFFFFFFFu, ok)) {  // give up: wait (bounded) for this warp's copies, then leave
+            if (lane == 0) set_error(I, ERR_TIMEOUT, 33);
+#pragma unroll
+            for (int k = 0; k < NT; ++k)
+                if (fifo[k] < n_oct)
+                    for (uint32_t spin = 0;
+                         spin < SPIN_LIMIT && !mbar_try_wait(bars + (j + k) % NT, ((j + k) / NT) & 1u); ++spin) {
+                    }
+            return;
+        }
+        uint64_t nx;
+        if (dyn) {  // claimed now, so the atomic's round trip overlaps this octant's work
+            unsigned long long t = 0;
+            if (lane == 0) t = atomicAdd(a.work, 1ull);
+            nx = (uint64_t)NT * total + __shfl_sync(0xFFFFFFFFu, t, 0);
+        } else {
+            nx = o + (uint64_t)NT * total;
+        }
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 6);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 6);
-        if (tree < I.tree_cap && I.depths[tree] == d) {
+        if (tree_ok) {
             quads_of_tile<T>(I, a, tiles + (size_t)b * 4096, C, leaf_cache, oid, oval);
         } else {
             if (lane == 0) set_error(I, ERR_INVALID, 34);
@@ -1458,8 +1468,10 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
             }
         }
         __syncwarp();
-        const uint64_t ahead = NT == 1 ? next : o + (uint64_t)NT * total;
-        if (lane == 0 && ahead < n_oct) issue(ahead, b);
+#pragma unroll
+        for (int k = 0; k + 1 < NT; ++k) fifo[k] = fifo[k + 1];
+        fifo[NT - 1] = nx;
+        if (lane == 0 && nx < n_oct) issue(nx, b);
     }
 }
 
@@ -1484,7 +1496,10 @@ __device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool i
     const int leader = __ffs(peers) - 1;
     bool same_key = true;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) same_key = same_key && __shfl_sync(0xFFFFFFFFu, c[k], leader) == c[k];
+    for (int k = 0; k < 8; ++k) {  // every lane takes part in each shuffle
+        const uint64_t lk = __shfl_sync(0xFFFFFFFFu, c[k], leader);
+        same_key = same_key && lk == c[k];
+    }
     const bool follow = is_branch && leader != (int)(threadIdx.x & 31u) && same_key;
     const bool probe = is_branch && !follow;
     const uint32_t lod = probe ? calc_average8(cv) : 0;
@@ -1543,8 +1558,11 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
 // from their depth-3 nodes, level by level in shared memory: one launch instead of three, whose
 // latency chains overlap across the CTAs.
 constexpr int kTopChunks = 4;
+#ifndef VX_TOP_MINB
+#define VX_TOP_MINB 5  // resident CTAs per SM the register allocation must allow (48 registers, no spills)
+#endif
 
-__global__ void __launch_bounds__(kThreads) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
+__global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
                                                              const uint32_t *in_vals, uint32_t n_chunks,
                                                              const uint32_t *trees, uint8_t *changed) {
     __shared__ uint64_t s2[64 * kTopChunks], s1[8 * kTopChunks];
@@ -1616,8 +1634,11 @@ __device__ __forceinline__ void leaf_tab_add(uint32_t *tab_key, uint32_t *tab_cn
 }
 
 __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I) {
-    __shared__ uint32_t leaf_cnt[256];
-    __shared__ uint32_t tab_key[kLeafTab], tab_cnt[kLeafTab];
+    // 8-bit leaves: 256 counters; wider leaves: the kLeafTab-entry table (dynamic shared memory, so
+    // the 8-bit case keeps its occupancy)
+    extern __shared__ uint32_t ref_smem[];
+    uint32_t *leaf_cnt = ref_smem;
+    uint32_t *tab_key = ref_smem, *tab_cnt = ref_smem + kLeafTab;
     const bool small = I.vbits == 8;
     if (small)
         for (unsigned k = threadIdx.x; k < 256; k += blockDim.x) leaf_cnt[k] = 0;
@@ -1969,8 +1990,9 @@ cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, con
 }
 
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s) {
+    const size_t smem = I.vbits == 8 ? 256 * 4 : (size_t)2 * kLeafTab * 4;
     count_launches(1);
-    epoch_refcount_kernel<<<num_sms * 16, kThreads, 0, s>>>(I);
+    epoch_refcount_kernel<<<num_sms * 16, kThreads, smem, s>>>(I);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_epoch_finalize(I, s);

@@ -112,7 +112,10 @@ struct DevBuf {
     }
 };
 
-constexpr int kCopyPieces = 8;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
+#ifndef VX_COPY_PIECES
+#define VX_COPY_PIECES 4  // 8 and 16 measured slower: small pieces build below the copy rate
+#endif
+constexpr int kCopyPieces = VX_COPY_PIECES;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
 
 struct HostBuf {
     void *p = nullptr;
