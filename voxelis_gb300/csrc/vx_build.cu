@@ -629,6 +629,57 @@ __device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint3
     }
 }
 
+#ifndef VX_QUAD_DEFER
+#define VX_QUAD_DEFER 1  // memo misses claim a pending record computed by a later kernel (else inline)
+#endif
+// q_vals marker of a quad whose node is still being computed: its q_ids entry is the memo record.
+constexpr uint32_t kQuadPending = 0xFFFFFFFFu;
+// Record tail id of a claimed record that lost its slot to an identical quad (never computed).
+constexpr uint64_t kRecordDead = 1ull;
+
+// Claims record r for a quad that missed the memo: the record gets the quad's rows and a pending
+// tail (id 0), is fenced, then published by a CAS into the first free slot from h1. A CAS that meets
+// an identical quad published meanwhile follows that record instead (r is marked dead). Without a
+// free slot within 4 steps r stays pending and reachable only from this quad. id / val receive the
+// record to resolve (val = kQuadPending) or, for a record already computed, its node.
+template <class T, int S>
+__device__ __forceinline__ void memo_claim(const OctArgs &a, uint32_t h1, uint32_t h2, const T *qbase, uint32_t r,
+                                           uint64_t &id, uint32_t &val) {
+    using W = typename QuadWord<T>::type;
+    unsigned char *rec = memo_rec<T>(a, r);
+    W *dst = reinterpret_cast<W *>(rec);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) dst[k] = *quad_row<T, S>(qbase, k);
+    uint4 *tail = reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T));
+    *tail = make_uint4(0u, 0u, 0u, 0u);
+    __threadfence();
+    id = r;
+    val = kQuadPending;
+    uint32_t slot = h1 & a.memo_mask;
+    const unsigned long long v = ((unsigned long long)h2 << 32) | (r + 1u);
+#pragma unroll 1
+    for (int p = 0; p < 4; ++p) {
+        const unsigned long long prev = atomicCAS(a.memo_slots + slot, 0ull, v);
+        if (prev == 0ull) return;
+        if ((uint32_t)(prev >> 32) == h2) {
+            __threadfence();  // the other record was fenced before its CAS: read it after ours
+            uint64_t oid;
+            uint32_t olod;
+            if (memo_match<T, S>(a, (uint32_t)prev - 1u, qbase, oid, olod)) {
+                tail->x = (uint32_t)kRecordDead;
+                if (oid == 0) {
+                    id = (uint32_t)prev - 1u;
+                } else {
+                    id = oid;
+                    val = olod;
+                }
+                return;
+            }
+        }
+        slot = (slot + 1) & a.memo_mask;
+    }
+}
+
 // The 8 bottom groups of one quad (4^3 voxels at qbase in a tile of side S) reduced as Phase 1 and
 // Phase 2 do, then the quad's own node, which a non-uniform quad always is a branch. Warp-collective:
 // every lane calls it; lanes with active == false only take part in the ballots.
@@ -1301,13 +1352,15 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(qb[p]), leader[p]));
         follow[p] = !uni[p] && leader[p] != (int)lane && rows_equal<T, S>(qb[p], lq);
     }
+    // have[p]: the quad's result is known (uniform, a memo hit, or a pending record of this build)
+    bool have[2] = {uni[0], uni[1]};
     {  // memo probes, both quads in flight
         bool look[2];
         uint32_t slot[2];
         unsigned long long sv[2];
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-            look[p] = memo && !uni[p] && !follow[p] && qidv[p] == 0;
+            look[p] = memo && !uni[p] && !follow[p];
             slot[p] = h1[p] & a.memo_mask;
             sv[p] = look[p] ? memo_slot_load(a.memo_slots, slot[p]) : 0ull;
         }
@@ -1321,6 +1374,11 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
                 } else if ((uint32_t)(sv[p] >> 32) == h2[p] &&
                            memo_match<T, S>(a, (uint32_t)sv[p] - 1u, qb[p], qidv[p], qvalv[p])) {
                     look[p] = false;
+                    have[p] = true;
+                    if (qidv[p] == 0) {  // pending: computed after this kernel by dense_memo_compute_kernel
+                        qidv[p] = (uint32_t)sv[p] - 1u;
+                        qvalv[p] = kQuadPending;
+                    }
                 } else if (step == 3) {
                     look[p] = false;
                 } else {
@@ -1330,9 +1388,30 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             }
         }
     }
+    if (memo && VX_QUAD_DEFER) {  // misses claim a pending record: one record range per warp
+        const bool cl0 = !uni[0] && !follow[0] && !have[0], cl1 = !uni[1] && !follow[1] && !have[1];
+        const unsigned b0 = __ballot_sync(0xFFFFFFFFu, cl0), b1 = __ballot_sync(0xFFFFFFFFu, cl1);
+        if (b0 | b1) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.memo_count, (unsigned)(__popc(b0) + __popc(b1)));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            const unsigned lt = (1u << lane) - 1u;
+            const uint32_t r0 = base + __popc(b0 & lt), r1 = base + __popc(b0) + __popc(b1 & lt);
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const bool cl = p ? cl1 : cl0;
+                const uint32_t r = p ? r1 : r0;
+                if (cl && r < a.memo_cap) {
+                    memo_claim<T, S>(a, h1[p], h2[p], qb[p], r, qidv[p], qvalv[p]);
+                    have[p] = true;
+                }
+            }
+        }
+    }
 #pragma unroll 1
     for (int p = 0; p < 2; ++p) {
-        const bool active = !uni[p] && !follow[p] && qidv[p] == 0;
+        // computed here only without a memo, with deferral off, or once the memo's records run out
+        const bool active = !uni[p] && !follow[p] && !have[p];
         if (__any_sync(0xFFFFFFFFu, active)) {
             uint64_t pid;
             uint32_t pval;
@@ -1340,7 +1419,7 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             if (active) {
                 qidv[p] = pid;
                 qvalv[p] = pval;
-                if (memo && pid != INVALID_ID) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
+                if (memo && !VX_QUAD_DEFER && pid != INVALID_ID) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
             }
         }
         const uint64_t lid = __shfl_sync(0xFFFFFFFFu, qidv[p], leader[p]);
@@ -1448,14 +1527,10 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
                     }
             return;
         }
-        uint64_t nx;
-        if (dyn) {  // claimed now, so the atomic's round trip overlaps this octant's work
-            unsigned long long t = 0;
-            if (lane == 0) t = atomicAdd(a.work, 1ull);
-            nx = (uint64_t)NT * total + __shfl_sync(0xFFFFFFFFu, t, 0);
-        } else {
-            nx = o + (uint64_t)NT * total;
-        }
+        // the next octant is claimed now and its number read after this one is done, so the
+        // atomic's round trip overlaps this octant's work
+        unsigned long long claim = 0;
+        if (dyn && lane == 0) claim = atomicAdd(a.work, 1ull);
         uint64_t *oid = q_ids + (uint64_t)c * per_chunk + (q << 6);
         uint32_t *oval = q_vals + (uint64_t)c * per_chunk + (q << 6);
         if (tree_ok) {
@@ -1468,10 +1543,110 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
             }
         }
         __syncwarp();
+        const uint64_t nx = dyn ? (uint64_t)NT * total + __shfl_sync(0xFFFFFFFFu, claim, 0) : o + (uint64_t)NT * total;
 #pragma unroll
         for (int k = 0; k + 1 < NT; ++k) fifo[k] = fifo[k + 1];
         fifo[NT - 1] = nx;
         if (lane == 0 && nx < n_oct) issue(nx, b);
+    }
+}
+
+// ---- pending memo records, computed once each ------------------------------------------------------
+//
+// Every record still pending after dense_quads16_kernel (tail id 0) is a distinct quad of this build.
+// A warp takes 4 records at a time, 8 lanes each: lane 8m + k reduces bottom group k of the m-th
+// record from the record's row words (the groups, keys and interning of quad_groups), then lane 8m
+// reduces the quad node and writes the record's tail. Group keys go through the CTA's key cache.
+template <class T>
+__global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevInterner I, OctArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint64_t *kc = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *leaf_cache = kc + 3 * kKeyCache;
+    KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(leaf_cache + 256)};
+    for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+    __syncthreads();
+    using W = typename QuadWord<T>::type;
+    const bool wide = sizeof(T) == 2;
+    const uint32_t cnt = *(volatile unsigned int *)a.memo_count;
+    const uint32_t n = cnt < a.memo_cap ? cnt : a.memo_cap;
+    const uint32_t m = lane >> 3;
+    const int k = (int)(lane & 7u);
+    const uint32_t gx = k & 1, gy = (k >> 1) & 1, gz = k >> 2;
+    const uint64_t stride = (uint64_t)gridDim.x * kQ16Warps * 4;
+    for (uint64_t base = ((uint64_t)blockIdx.x * kQ16Warps + warp) * 4; base < n; base += stride) {
+        const uint64_t r = base + m;
+        unsigned char *rec = r < n ? memo_rec<T>(a, (uint32_t)r) : nullptr;
+        uint4 *tail = rec ? reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T)) : nullptr;
+        const bool act = rec && tail->x == 0u && tail->y == 0u;
+        uint64_t lo = 0, hi = 0;
+        if (act) {  // bottom group k: rows y*4 + z of 4 voxels along x
+            const W *w = reinterpret_cast<const W *>(rec);
+            const W r00 = w[(2 * gy) * 4 + 2 * gz], r10 = w[(2 * gy + 1) * 4 + 2 * gz];
+            const W r01 = w[(2 * gy) * 4 + 2 * gz + 1], r11 = w[(2 * gy + 1) * 4 + 2 * gz + 1];
+            if (sizeof(T) == 1) {
+                const uint32_t sh = 16 * gx;
+                const uint64_t p0 = ((uint32_t)r00 >> sh) & 0xFFFFu, p1 = ((uint32_t)r10 >> sh) & 0xFFFFu;
+                const uint64_t p2 = ((uint32_t)r01 >> sh) & 0xFFFFu, p3 = ((uint32_t)r11 >> sh) & 0xFFFFu;
+                lo = p0 | (p1 << 16) | (p2 << 32) | (p3 << 48);
+            } else {
+                const uint32_t sh = 32 * gx;
+                lo = (((uint64_t)r00 >> sh) & 0xFFFFFFFFull) | ((((uint64_t)r10 >> sh) & 0xFFFFFFFFull) << 32);
+                hi = (((uint64_t)r01 >> sh) & 0xFFFFFFFFull) | ((((uint64_t)r11 >> sh) & 0xFFFFFFFFull) << 32);
+            }
+        }
+        const uint32_t set = set_mask8<T>(lo, hi);
+        const uint32_t gv0 = (uint32_t)lo & (sizeof(T) == 1 ? 0xFFu : 0xFFFFu);
+        const bool guni = sizeof(T) == 1 ? lo == (uint64_t)gv0 * 0x0101010101010101ull
+                                         : (lo == hi && lo == (uint64_t)gv0 * 0x0001000100010001ull);
+        const bool is_branch = act && set != 0 && !(guni && set == 0xFFu);
+        uint32_t lod = 0;
+        uint64_t id = is_branch ? kc_lookup(C, lo, hi, &lod) : 0ull;
+        const bool need = is_branch && id == 0;
+        const unsigned bm = __ballot_sync(0xFFFFFFFFu, need);
+        if (bm) {
+            uint32_t v[8];
+            unpack8<T>(lo, hi, v);
+            if (need) lod = calc_average8(v);
+            unsigned grp = __match_any_sync(0xFFFFFFFFu, need ? lo : ~(uint64_t)lane);
+            if (wide) grp &= __match_any_sync(0xFFFFFFFFu, need ? hi : ~(uint64_t)lane);
+            grp &= bm;
+            const int leader = need ? __ffs(grp) - 1 : (int)lane;
+            const bool lead = need && leader == (int)lane;
+            uint64_t c[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+            bool created;
+            uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+            nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
+            if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+            if (need) id = nid;
+        }
+        uint64_t gid;
+        uint32_t gval;
+        if (set == 0) {
+            gid = EMPTY_ID;
+            gval = 0;
+        } else if (!is_branch) {
+            gid = act ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
+            gval = gv0;
+        } else {
+            gid = id;
+            gval = lod;
+        }
+        uint64_t c3[8];
+        uint32_t cv3[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            c3[j] = __shfl_sync(0xFFFFFFFFu, gid, (lane & ~7u) + j);
+            cv3[j] = __shfl_sync(0xFFFFFFFFu, gval, (lane & ~7u) + j);
+        }
+        uint64_t qid;
+        uint32_t qval;
+        reduce_parent(I, act && k == 0, c3, cv3, qid, qval);
+        if (act && k == 0) *tail = make_uint4((uint32_t)qid, (uint32_t)(qid >> 32), qval, 0u);
     }
 }
 
@@ -1526,10 +1701,26 @@ __device__ __forceinline__ void commit_root(const DevInterner &I, const uint32_t
     if (changed) changed[p] = out != EMPTY_ID;
 }
 
+// Memo records that quads still pending in q_ids / q_vals name (recs == nullptr: nothing pending).
+struct PendingView {
+    const unsigned char *recs;
+    uint32_t stride;    // bytes per record
+    uint32_t tail_off;  // offset of the (id, LOD value) tail in a record
+};
+
+__device__ __forceinline__ void resolve_pending(const PendingView &P, uint64_t &id, uint32_t &val) {
+    if (P.recs && val == kQuadPending) {
+        const uint4 t = __ldcg(reinterpret_cast<const uint4 *>(P.recs + (size_t)id * P.stride + P.tail_off));
+        id = (uint64_t)t.x | ((uint64_t)t.y << 32);
+        val = t.z;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
-                                                               const uint32_t *trees, uint8_t *changed) {
+                                                               const uint32_t *trees, uint8_t *changed,
+                                                               PendingView P) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_parents; base += stride) {
         const uint64_t p = base + threadIdx.x;
@@ -1540,6 +1731,7 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
         for (int k = 0; k < 8; ++k) {
             c[k] = in ? in_ids[8 * p + k] : 0;
             cv[k] = in ? in_vals[8 * p + k] : 0;
+            resolve_pending(P, c[k], cv[k]);
         }
         uint64_t out;
         uint32_t val;
@@ -1564,7 +1756,8 @@ constexpr int kTopChunks = 4;
 
 __global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
                                                              const uint32_t *in_vals, uint32_t n_chunks,
-                                                             const uint32_t *trees, uint8_t *changed) {
+                                                             const uint32_t *trees, uint8_t *changed,
+                                                             PendingView P) {
     __shared__ uint64_t s2[64 * kTopChunks], s1[8 * kTopChunks];
     __shared__ uint32_t v2[64 * kTopChunks], v1[8 * kTopChunks];
     const unsigned t = threadIdx.x, warp = t >> 5, lane = t & 31u;
@@ -1578,6 +1771,7 @@ __global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInt
             for (int k = 0; k < 8; ++k) {
                 c[k] = in ? in_ids[8 * p + k] : 0;
                 cv[k] = in ? in_vals[8 * p + k] : 0;
+                resolve_pending(P, c[k], cv[k]);
             }
             reduce_parent_dedup(I, in, c, cv, s2[t], v2[t]);
         }
@@ -1900,6 +2094,10 @@ size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth) {
     return nodes * 12 + 512;
 }
 
+static cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
+                                      uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
+                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P);
+
 cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
                                bool clear_memo, uint64_t memo_chunks, void (*levels_begin)(void *),
@@ -1963,29 +2161,46 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     cudaError_t e = es == 1 ? launch16(dense_quads16_kernel<uint8_t>, Q16Smem<uint8_t>::total)
                             : launch16(dense_quads16_kernel<uint16_t>, Q16Smem<uint16_t>::total);
     if (e != cudaSuccess) return e;
+    PendingView P{nullptr, 0, 0};
+    if (memo && VX_QUAD_DEFER) {  // the quads that claimed records, one computation per distinct quad
+        const size_t smemc = (3 * (size_t)kKeyCache + 256) * 8 + (size_t)kKeyCache * 4;
+        auto launchc = [&](auto kernel) -> cudaError_t {
+            cudaError_t e2 = cudaSuccess;
+            const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQ16Warps * 32, smemc, &e2);
+            if (e2 != cudaSuccess) return e2;
+            count_launches(1);
+            kernel<<<(unsigned)(num_sms * per_sm), kQ16Warps * 32, smemc, s>>>(I, a);
+            return cudaGetLastError();
+        };
+        e = es == 1 ? launchc(dense_memo_compute_kernel<uint8_t>) : launchc(dense_memo_compute_kernel<uint16_t>);
+        if (e != cudaSuccess) return e;
+        P = PendingView{a.memo_recs, (uint32_t)memo_stride(es), (uint32_t)(16 * 4 * es)};
+    }
     if (levels_begin) (*levels_begin)(levels_ctx);
-    for (int k = depth - 3; k >= 3; --k) {
+    for (int k = depth - 3; k >= 3; --k) {  // the first pass reads the quads
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
         e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], ids + off[k], vals + off[k], np, false, trees,
-                               changed, s);
+                               changed, s, k == depth - 3 ? P : PendingView{nullptr, 0, 0});
         if (e != cudaSuccess) return e;
     }
     // depths 2, 1 and 0 in one launch
     const unsigned top_blocks = (unsigned)((n_chunks + kTopChunks - 1) / kTopChunks);
     count_launches(1);
-    fresh_top_kernel<<<top_blocks, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed);
+    fresh_top_kernel<<<top_blocks, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed,
+                                                     depth == 5 ? P : PendingView{nullptr, 0, 0});
     return cudaGetLastError();
 }
 
-cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
-                               uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
-                               const uint32_t *trees, uint8_t *changed, cudaStream_t s) {
+// One level of fresh parents: n_parents = n_chunks * 8^k; children pending in P are resolved first.
+static cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
+                                      uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
+                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P) {
     if (n_parents == 0) return cudaSuccess;
     uint64_t blocks = (n_parents + kThreads - 1) / kThreads;
     if (blocks > 65535) blocks = 65535;
     count_launches(1);
     fresh_level_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(I, in_ids, in_vals, out_ids, out_vals, n_parents,
-                                                             is_root ? 1 : 0, trees, changed);
+                                                             is_root ? 1 : 0, trees, changed, P);
     return cudaGetLastError();
 }
 

@@ -43,10 +43,6 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
                                bool clear_memo = true, uint64_t memo_chunks = 0,
                                void (*levels_begin)(void *) = nullptr, void *levels_ctx = nullptr);
-// One level of fresh parents above the blocks: n_parents = n_chunks * 8^k.
-cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
-                               uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
-                               const uint32_t *trees, uint8_t *changed, cudaStream_t s);
 // In-degree refcounts of the nodes created in the current epoch, then closes the epoch.
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s);
 cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
