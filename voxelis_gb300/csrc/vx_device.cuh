@@ -199,10 +199,13 @@ __device__ __forceinline__ uint32_t calc_average8(const uint32_t v[8]) {
 // ---- allocation --------------------------------------------------------------------------------
 // The t-th allocation of an epoch takes free_list[free_count-1-t] while the free list lasts, then
 // next_index + (t - free_count). free_count and next_index only change between epochs.
-__device__ __forceinline__ uint32_t node_for_ticket(const DevInterner &I, unsigned long long t) {
-    unsigned long long fc = I.ctr->free_count;
-    unsigned long long idx = (t < fc) ? (unsigned long long)I.free_list[fc - 1 - t] : I.ctr->next_index + (t - fc);
+__device__ __forceinline__ uint32_t node_for_ticket(const DevInterner &I, unsigned long long t,
+                                                    unsigned long long fc, unsigned long long ni) {
+    unsigned long long idx = (t < fc) ? (unsigned long long)I.free_list[fc - 1 - t] : ni + (t - fc);
     return idx < I.capacity ? (uint32_t)idx : NO_NODE;
+}
+__device__ __forceinline__ uint32_t node_for_ticket(const DevInterner &I, unsigned long long t) {
+    return node_for_ticket(I, t, I.ctr->free_count, I.ctr->next_index);
 }
 
 // Writes a new branch record (children, LOD value, fingerprint, live id); rc starts at 0.
@@ -222,16 +225,19 @@ __device__ __forceinline__ uint64_t write_branch(const DevInterner &I, uint32_t 
     return id;
 }
 
+// The id and the children of node idx are loaded together (one round trip); *id_out gets the id.
 __device__ __forceinline__ bool key_equal(const DevInterner &I, uint32_t idx, const uint64_t c[8], uint32_t types,
-                                          uint32_t mask) {
-    uint64_t id = ld_cg(I.ids + idx);
-    if (id == 0 || id_is_leaf(id) || id_types(id) != types || id_mask(id) != mask) return false;
+                                          uint32_t mask, uint64_t *id_out = nullptr) {
     const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(I.children + 8ull * idx);
+    const uint64_t id = ld_cg(I.ids + idx);
+    ulonglong2 w[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        ulonglong2 w = __ldcg(src + k);
-        if (w.x != c[2 * k] || w.y != c[2 * k + 1]) return false;
-    }
+    for (int k = 0; k < 4; ++k) w[k] = __ldcg(src + k);
+    if (id == 0 || id_is_leaf(id) || id_types(id) != types || id_mask(id) != mask) return false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (w[k].x != c[2 * k] || w[k].y != c[2 * k + 1]) return false;
+    if (id_out) *id_out = id;
     return true;
 }
 
@@ -256,6 +262,8 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
     bool done = !active;
     uint64_t result = INVALID_ID;
     *created = false;
+    // constant during an epoch: loaded beside the first probe instead of after a ticket is taken
+    const unsigned long long fc = I.ctr->free_count, ni = I.ctr->next_index;
     if (active) {
         h = h_in ? h_in : branch_fingerprint(c, tm);
         tag = slot_tag(h);
@@ -279,8 +287,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
                     if (idx == IDX_BUSY) {
                         waiting = true;  // retry the same slot next round
                     } else {
-                        if (key_equal(I, idx, c, types, mask)) {
-                            result = ld_cg(I.ids + idx);
+                        if (key_equal(I, idx, c, types, mask, &result)) {
                             done = true;
                         } else {
                             pos = (pos + 1) & I.table_mask;
@@ -305,7 +312,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
             base = __shfl_sync(0xFFFFFFFFu, base, leader);
             if (claimed) {
                 const unsigned rank = __popc(cm & ((1u << lane) - 1u));
-                const uint32_t idx = node_for_ticket(I, base + rank);
+                const uint32_t idx = node_for_ticket(I, base + rank, fc, ni);
                 if (idx == NO_NODE) {
                     set_error(I, ERR_OOM, 1);
                     atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
