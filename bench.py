@@ -11,9 +11,10 @@ Also measured in the same run:
   per_chunk   the plain per-chunk GPU path: one build call per chunk, same DAG (checked)
   e2e         the same build through the public C ABI with HOST buffers (vx_build_dense,
               VX_MEM_HOST): H2D of the grids from pinned memory, build, D2H of the changed flags
-  roofline    the dominant kernel (dense_quads16_kernel): algorithmic bytes of the build (input grids
-              + new nodes x node_size + roots x 8) / its CUDA-event duration (the "dense" phase; the
-              level passes are the "levels" phase), against the measured HBM copy bandwidth
+  roofline    the dense phase (dense_quads16_kernel streaming the grids, then dense_memo_compute_kernel
+              for the distinct quads): algorithmic bytes of the build (input grids + new nodes x
+              node_size + roots x 8) / the phase's CUDA-event duration (the level passes are the
+              "levels" phase), against the measured HBM copy bandwidth
   cpu_baseline the CPU restatement of the reference (oracle), one thread, whole 4096-chunk workload
 
 --impl reference times the reference's CPU algorithm (the oracle port; the Rust reference cannot be
@@ -436,8 +437,8 @@ def run_ours(args):
         "batched_over_per_chunk": pc_ms / ms,
         "dag": {"nodes": int(new_nodes), "canonical_nodes": int(len(canon["kind"])), "node_size": int(node_size)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic("dense_quads16_kernel_dunes4096.md"),
-                     "kernel": "dense_quads16_kernel",
+                     "frac": achieved / peak, "traffic": profiled_traffic("dense_phase_dunes4096.md"),
+                     "kernel": "dense phase: dense_quads16_kernel + dense_memo_compute_kernel",
                      "kernel_ms": dense_ms, "algorithmic_bytes": int(algo_bytes), "peak_kind": peak_kind},
         "phases": phases,
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "chunks/s", "ms": e2e_ms,
