@@ -126,6 +126,25 @@ def test_dense_terrain_matches_oracle(oracle_lib, gpu_lib, depth, patches):
     assert_same(io, ig2, to, tg2)
 
 
+@pytest.mark.parametrize("depth,n,bits,patches", [(5, 32, 8, 0), (5, 16, 16, 0), (6, 4, 8, 0), (7, 1, 8, VX_PATCH_P2)])
+def test_dense_noise_runs_the_quad_memo_out(oracle_lib, gpu_lib, depth, n, bits, patches):
+    """Random voxels: nearly every quad (4^3) is distinct, so the build's quad memo runs out of
+    records (a quarter of the quads as slots, half of those as records) and fills its slots: quads
+    computed in the streaming kernel after the records are gone, records published without a free
+    slot within 4 steps, records shared across the pieces of a host-memory build (n >= 8) and
+    uniform quads between them (value 0 on a third of the voxels) all take part."""
+    rng = np.random.default_rng(100 + depth)
+    side = 1 << depth
+    vals = rng.integers(1, 4 if bits == 8 else 4000, (n, side, side, side))
+    g = np.where(rng.random((n, side, side, side)) < 0.33, 0, vals).astype(np.uint8 if bits == 8 else np.uint16)
+    g[:, : side // 2] = 0  # uniform quads and octants too
+    io, ig = pair(oracle_lib, gpu_lib, budget=256 << 20, bits=bits, patches=patches)
+    to, tg = [VoxTree(depth) for _ in range(n)], [VoxTree(depth) for _ in range(n)]
+    io.build_dense(to, g)
+    ig.build_dense(tg, g)
+    assert_same(io, ig, to, tg)
+
+
 def test_per_chunk_equals_batched(gpu_lib):
     grids = W.dune_chunks(4, 4, depth=5, seed=3)
     ia, ta = build_terrain(gpu_lib, grids, 5)
