@@ -619,12 +619,11 @@ __device__ __forceinline__ void memo_insert(const OctArgs &a, uint32_t h1, uint3
 #pragma unroll
     for (int k = 0; k < 16; ++k) dst[k] = *quad_row<T, S>(qbase, k);
     *reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T)) = make_uint4((uint32_t)id, (uint32_t)(id >> 32), lod, 0u);
-    __threadfence();
     uint32_t slot = h1 & a.memo_mask;
     const unsigned long long v = ((unsigned long long)h2 << 32) | (r + 1u);
 #pragma unroll 1
-    for (int p = 0; p < 4; ++p) {
-        if (atomicCAS(a.memo_slots + slot, 0ull, v) == 0ull) return;
+    for (int p = 0; p < 4; ++p) {  // the CAS publishes the record (release)
+        if (atom_cas_acq_rel(a.memo_slots + slot, 0ull, v) == 0ull) return;
         slot = (slot + 1) & a.memo_mask;
     }
 }
@@ -638,7 +637,7 @@ constexpr uint32_t kQuadPending = 0xFFFFFFFFu;
 constexpr uint64_t kRecordDead = 1ull;
 
 // Claims record r for a quad that missed the memo: the record gets the quad's rows and a pending
-// tail (id 0), is fenced, then published by a CAS into the first free slot from h1. A CAS that meets
+// tail (id 0), then is published by a release CAS into the first free slot from h1. A CAS that meets
 // an identical quad published meanwhile follows that record instead (r is marked dead). Without a
 // free slot within 4 steps r stays pending and reachable only from this quad. id / val receive the
 // record to resolve (val = kQuadPending) or, for a record already computed, its node.
@@ -652,17 +651,16 @@ __device__ __forceinline__ void memo_claim(const OctArgs &a, uint32_t h1, uint32
     for (int k = 0; k < 16; ++k) dst[k] = *quad_row<T, S>(qbase, k);
     uint4 *tail = reinterpret_cast<uint4 *>(rec + 16 * 4 * sizeof(T));
     *tail = make_uint4(0u, 0u, 0u, 0u);
-    __threadfence();
     id = r;
     val = kQuadPending;
     uint32_t slot = h1 & a.memo_mask;
     const unsigned long long v = ((unsigned long long)h2 << 32) | (r + 1u);
 #pragma unroll 1
     for (int p = 0; p < 4; ++p) {
-        const unsigned long long prev = atomicCAS(a.memo_slots + slot, 0ull, v);
+        // release: the record is visible with the slot; acquire: so is a record published meanwhile
+        const unsigned long long prev = atom_cas_acq_rel(a.memo_slots + slot, 0ull, v);
         if (prev == 0ull) return;
         if ((uint32_t)(prev >> 32) == h2) {
-            __threadfence();  // the other record was fenced before its CAS: read it after ours
             uint64_t oid;
             uint32_t olod;
             if (memo_match<T, S>(a, (uint32_t)prev - 1u, qbase, oid, olod)) {

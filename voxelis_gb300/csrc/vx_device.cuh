@@ -129,6 +129,23 @@ __device__ __forceinline__ uint64_t ld_probe(const uint64_t *p) {
     return v;
 }
 
+// Publication with release semantics: every store of this thread before it is visible to a thread
+// that reads the new value with acquire semantics (ld_probe). Cheaper than a full fence before a
+// plain atomic, which also orders loads and waits for sequential consistency.
+__device__ __forceinline__ unsigned long long atom_exch_release(unsigned long long *p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+// Compare-and-swap that publishes this thread's earlier stores (release) and, whatever its outcome,
+// makes the stores published with the value it read visible to this thread (acquire).
+__device__ __forceinline__ unsigned long long atom_cas_acq_rel(unsigned long long *p, unsigned long long cmp,
+                                                               unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.acq_rel.gpu.global.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "l"(p), "l"(cmp), "l"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
     unsigned int old = atomicOr(&I.ctr->error, bit);
     if (old == 0) atomicExch(&I.ctr->error_info, info);
@@ -318,8 +335,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
                     atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
                 } else {
                     result = write_branch(I, idx, c, types, mask, h, lod);
-                    __threadfence();
-                    atomicExch((unsigned long long *)(I.table + pos), make_slot(tag, idx));
+                    atom_exch_release((unsigned long long *)(I.table + pos), make_slot(tag, idx));
                     *created = true;
                 }
                 done = true;
@@ -368,8 +384,7 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
             I.hash[idx] = 0;
             I.refcount[idx] = 0;
             I.ids[idx] = id;
-            __threadfence();
-            atomicExch(slot, id);
+            atom_exch_release(slot, id);
             *created = true;
             return id;
         }
