@@ -1749,7 +1749,7 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
 // latency chains overlap across the CTAs.
 constexpr int kTopChunks = 4;
 #ifndef VX_TOP_MINB
-#define VX_TOP_MINB 5  // resident CTAs per SM the register allocation must allow (48 registers, no spills)
+#define VX_TOP_MINB 4  // resident CTAs per SM the register allocation must allow (5 spills: measured slower)
 #endif
 
 __global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
