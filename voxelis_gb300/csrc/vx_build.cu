@@ -1801,11 +1801,26 @@ __global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInt
     }
 }
 
+// Closes the epoch: the free-list entries and fresh indices its tickets took become allocated.
+__device__ __forceinline__ void epoch_finalize_body(const DevInterner &I) {
+    DevCounters *c = I.ctr;
+    const unsigned long long alloc = c->alloc_count, fc = c->free_count;
+    const unsigned long long used_free = alloc < fc ? alloc : fc;
+    c->free_count = fc - used_free;
+    unsigned long long ni = c->next_index + (alloc - used_free);
+    if (ni > I.capacity) ni = I.capacity;
+    c->next_index = ni;
+    c->alloc_count = 0;
+}
+
 // Adds one reference per child slot of every node created in this epoch. Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
 // bottom groups), so they are summed per CTA before touching global memory: 8-bit leaves in a
 // 256-entry array indexed by value, wider leaves in an open-addressed shared table keyed by node
 // index (entries that find no slot within kLeafProbe steps go straight to global atomics).
 constexpr int kLeafTab = 4096;
+#ifndef VX_REF_FOLD
+#define VX_REF_FOLD 1  // the refcount kernel's last CTA closes the epoch (else a separate launch)
+#endif
 constexpr int kLeafProbe = 16;
 
 __device__ __forceinline__ void leaf_tab_add(uint32_t *tab_key, uint32_t *tab_cnt, const DevInterner &I,
@@ -1887,18 +1902,24 @@ __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I)
         for (unsigned k = threadIdx.x; k < kLeafTab; k += blockDim.x)
             if (tab_key[k] && tab_cnt[k]) atomicAdd(I.refcount + tab_key[k] - 1, tab_cnt[k]);
     }
+    if (VX_REF_FOLD) {  // the last CTA to finish closes the epoch (no separate launch)
+        __shared__ unsigned int last_cta;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            last_cta = atomicAdd(&I.ctr->scratch[SC_REF_DONE], 1ull) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (last_cta && threadIdx.x == 0) {
+            __threadfence();
+            epoch_finalize_body(I);
+            I.ctr->scratch[SC_REF_DONE] = 0;
+        }
+    }
 }
 
-__global__ void epoch_finalize_kernel(DevInterner I) {
-    DevCounters *c = I.ctr;
-    const unsigned long long alloc = c->alloc_count, fc = c->free_count;
-    const unsigned long long used_free = alloc < fc ? alloc : fc;
-    c->free_count = fc - used_free;
-    unsigned long long ni = c->next_index + (alloc - used_free);
-    if (ni > I.capacity) ni = I.capacity;
-    c->next_index = ni;
-    c->alloc_count = 0;
-}
+
+__global__ void epoch_finalize_kernel(DevInterner I) { epoch_finalize_body(I); }
 
 }  // namespace
 
@@ -2207,7 +2228,7 @@ cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream
     count_launches(1);
     epoch_refcount_kernel<<<num_sms * 16, kThreads, smem, s>>>(I);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || VX_REF_FOLD) return e;
     return launch_epoch_finalize(I, s);
 }
 
