@@ -372,6 +372,11 @@ __global__ void starts_kernel(DevInterner I, ApplyArgs a) {
         if (a.flags[j]) a.p_start[a.pos[j]] = j;
 }
 
+// Entries of the next level pass: the parents just reduced that are not tree roots.
+__device__ __forceinline__ void next_count(const DevInterner &I) {
+    I.ctr->scratch[SC_ENTRIES] = I.ctr->scratch[SC_PARENTS] - I.ctr->scratch[SC_ROOTS];
+}
+
 __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
     const uint32_t n_par = (uint32_t)I.ctr->scratch[SC_PARENTS];
     const int nb = buf ^ 1;
@@ -524,11 +529,10 @@ __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a
             a.e_val[nb][p] = out_val;
         }
     }
+    if (grid_last_cta(&I.ctr->scratch[SC_DONE])) next_count(I);  // entries of the next step
 }
 
-__global__ void next_count_kernel(DevInterner I) {
-    I.ctr->scratch[SC_ENTRIES] = I.ctr->scratch[SC_PARENTS] - I.ctr->scratch[SC_ROOTS];
-}
+
 
 __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -673,9 +677,7 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
             count_launches(1);
             starts_kernel<<<sb, kThreads, 0, s>>>(I, a);
             count_launches(1);
-            parents_kernel<<<g, bt, 0, s>>>(I, a, step, buf);
-            count_launches(1);
-            next_count_kernel<<<1, 1, 0, s>>>(I);
+            parents_kernel<<<g, bt, 0, s>>>(I, a, step, buf);  // its last CTA sets the next entry count
             buf ^= 1;
         }
     }

@@ -146,6 +146,24 @@ __device__ __forceinline__ unsigned long long atom_cas_acq_rel(unsigned long lon
     return old;
 }
 
+// Counts the calling CTA as done on *done and returns true in thread 0 of the last CTA of the grid to
+// finish (every other CTA's writes are visible to it), after resetting *done for the next kernel.
+// All threads of the CTA must call it. Lets a kernel's last CTA do the one-thread follow-up work that
+// would otherwise be a separate launch.
+__device__ __forceinline__ bool grid_last_cta(unsigned long long *done) {
+    __shared__ unsigned int is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        is_last = atomicAdd(done, 1ull) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0 || !is_last) return false;
+    __threadfence();
+    *done = 0;
+    return true;
+}
+
 __device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
     unsigned int old = atomicOr(&I.ctr->error, bit);
     if (old == 0) atomicExch(&I.ctr->error_info, info);

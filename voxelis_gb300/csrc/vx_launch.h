@@ -91,7 +91,7 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
 // Fills it_depth from the tree table and checks the deepest-first order (device-resident inputs).
 cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s);
 // Counter slots used by launch_apply (DevCounters::scratch indices).
-enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6 };
+enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6, SC_DONE = 7 };
 
 // Inclusive-to-exclusive scan of n u32 flags (n from the host) into pos; pos[n] = total.
 cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s);

@@ -66,6 +66,12 @@ __global__ void __launch_bounds__(kThreads) get_kernel(DevInterner I, uint64_t n
 }
 
 // ---- release -----------------------------------------------------------------------------------
+// The dying set just produced becomes the input of the next round.
+__device__ __forceinline__ void release_advance(const DevInterner &I) {
+    I.ctr->scratch[SC_REL_IN] = I.ctr->scratch[SC_REL_OUT];
+    I.ctr->scratch[SC_REL_OUT] = 0;
+}
+
 __device__ __forceinline__ void push_dying(uint32_t *list, unsigned long long *count, bool push, uint32_t idx) {
     const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
     if (!m) return;
@@ -101,6 +107,7 @@ __global__ void __launch_bounds__(kThreads) release_roots_kernel(DevInterner I, 
         }
         push_dying(out, &I.ctr->scratch[SC_REL_OUT], dies, idx);
     }
+    if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 
 // Retires the dying nodes of `in`: their children lose one reference each (children reaching zero
@@ -146,12 +153,10 @@ __global__ void __launch_bounds__(kThreads) release_round_kernel(DevInterner I, 
         if (lane == 0 && tomb) atomicAdd(&I.ctr->tombstones, (unsigned long long)__popc(tomb));
         if (rec) recycle_node(I, idx, fbase + __popc(m & ((1u << lane) - 1u)));
     }
+    if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 
-__global__ void release_advance_kernel(DevInterner I) {
-    I.ctr->scratch[SC_REL_IN] = I.ctr->scratch[SC_REL_OUT];
-    I.ctr->scratch[SC_REL_OUT] = 0;
-}
+__global__ void release_advance_kernel(DevInterner I) { release_advance(I); }
 
 // ---- single-thread reference-order operations ---------------------------------------------------
 struct Seq {
@@ -1167,9 +1172,7 @@ cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *front
     count_launches(1);
     release_roots_kernel<<<g, kThreads, 0, s>>>(I, list, frontier_a);
     uint32_t *in = frontier_a, *out = frontier_b;
-    for (int r = 0; r < rounds; ++r) {
-        count_launches(1);
-        release_advance_kernel<<<1, 1, 0, s>>>(I);
+    for (int r = 0; r < rounds; ++r) {  // each kernel's last CTA advances the dying set
         count_launches(1);
         release_round_kernel<<<g, kThreads, 0, s>>>(I, in, out);
         uint32_t *t = in;
