@@ -232,6 +232,11 @@ int vx_stage_spheres(int chunk_depth, int32_t nx, int32_t ny, int32_t nz, uint32
                      const int32_t *radii, const uint32_t *values, uint64_t cap_items, uint32_t *item_chunks,
                      uint64_t cap_records, uint32_t *rec_item, uint32_t *rec_group, uint8_t *rec_set,
                      uint8_t *rec_clear, uint16_t *rec_vals, uint64_t *n_items, uint64_t *n_records);
+/* n host -> device copies (dst_dev[k] <- src_host[k], bytes[k]) on the interner's stream, one
+ * cudaMemcpyAsync each: a serving loop stages a wave's arrays with one call. No reference
+ * counterpart (host plumbing of the serving loop). */
+int vx_copy_to_device_async(vx_interner *it, uint32_t n, void *const *dst_dev, const void *const *src_host,
+                            const uint64_t *bytes);
 /* Batched VoxOpsRead::get at world coordinates (world_xyz_dev[3i..3i+2]) over a vx_world. */
 int vx_world_get_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
                        uint8_t *found_dev, void *values_dev);

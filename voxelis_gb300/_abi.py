@@ -150,6 +150,7 @@ GPU_SIGNATURES = {
     "apply_groups_async": [_P, _U32, _P, _P, _P, _U32, _P, _P, _P, _P, _P, _P, _I],
     "tune_set": [_P, _I, _I],
     "world_get_async": [_P, _P, _U64, _P, _P, _P],
+    "copy_to_device_async": [_P, _U32, _P, _P, _P],
     "tune_get": [_P, _PI, _PI],
     "trees_to_dense": [_P, _U32, _P, _P, _I],
     "trees_to_dense_async": [_P, _U32, _P, _I, _P],

@@ -247,3 +247,24 @@ extern "C" int vx_world_get_async(vx_interner *it, const vx_world *world, uint64
     }
     return VX_OK;
 }
+
+// n host -> device copies on the interner's stream, one cudaMemcpyAsync each (serving loops stage a
+// wave's arrays with one call instead of one runtime call per array from Python).
+extern "C" int vx_copy_to_device_async(vx_interner *it, uint32_t n, void *const *dst_dev, const void *const *src_host,
+                                       const uint64_t *bytes) {
+    DevInterner D;
+    cudaStream_t s;
+    int num_sms;
+    uint32_t flags;
+    if (!interner_parts(it, &D, &s, &num_sms, &flags, false)) return VX_E_INVALID_ARG;
+    if (n && (!dst_dev || !src_host || !bytes)) return VX_E_INVALID_ARG;
+    for (uint32_t k = 0; k < n; ++k) {
+        if (!bytes[k]) continue;
+        const cudaError_t e = cudaMemcpyAsync(dst_dev[k], src_host[k], bytes[k], cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) {
+            interner_set_error(it, cudaGetErrorString(e));
+            return VX_E_CUDA;
+        }
+    }
+    return VX_OK;
+}

@@ -132,6 +132,9 @@ class Server:
         self.hset = [dict(items=pin(cap_items, torch.int32), item_trees=pin(cap_items, torch.int32),
                           ri=pin(cap_recs, torch.int32), rg=pin(cap_recs, torch.int32), rs=pin(cap_recs, torch.uint8),
                           rc=pin(cap_recs, torch.uint8), rv=pin(cap_recs * 8, torch.int16)) for _ in range(2)]
+        for k, hs in enumerate(self.hset):  # numpy views of the pinned buffers (no torch call per wave)
+            hs["k"] = k
+            hs["np"] = {"items": hs["items"].numpy(), "item_trees": hs["item_trees"].numpy()}
         self.parity = 0
         self.d_item_trees = torch.empty(cap_items, dtype=torch.int32, device=dev)
         self.d_flags = torch.full((cap_items,), 2, dtype=torch.uint8, device=dev)
@@ -141,7 +144,17 @@ class Server:
         self.d_rs = torch.empty(cap_recs, dtype=torch.uint8, device=dev)
         self.d_rc = torch.empty(cap_recs, dtype=torch.uint8, device=dev)
         self.d_rv = torch.empty(cap_recs * 8, dtype=torch.int16, device=dev)
+        # per pinned set: the 6 staged arrays' device and host addresses for one vx_copy_to_device_async
+        dsts = [self.d_item_trees, self.d_ri, self.d_rg, self.d_rs, self.d_rc, self.d_rv]
+        self.copies = [{"dst": np.array([t.data_ptr() for t in dsts], np.uint64),
+                        "src": np.array([hs[k].data_ptr() for k in ("item_trees", "ri", "rg", "rs", "rc", "rv")],
+                                        np.uint64),
+                        "bytes": np.zeros(6, np.uint64)} for hs in self.hset]
         self.d_pts = torch.empty((max_wave_gets, self.ppg, 3), dtype=torch.int32, device=dev)
+        self.pool_ptr = [p.data_ptr() for p in self.pool_h]
+        self.get_dst = np.array([self.d_pts[k].data_ptr() for k in range(max_wave_gets)], np.uint64)
+        self.get_src = np.zeros(max_wave_gets, np.uint64)
+        self.get_bytes = np.full(max_wave_gets, self.ppg * 3 * 4, np.uint64)
         self.d_found = torch.empty((max_wave_gets, self.ppg), dtype=torch.uint8, device=dev)
         vt = torch.uint8 if world.bits == 8 else torch.int16
         self.d_vals = torch.empty((max_wave_gets, self.ppg), dtype=vt, device=dev)
@@ -198,19 +211,19 @@ class Server:
                 raise RuntimeError("vx_stage_spheres failed: %d" % st)
             ni, nr = ni.value, nr.value
             if ni:
-                hs["item_trees"][:ni] = torch.from_numpy(w.trees.view(np.int32)[hs["items"][:ni].numpy()])
-                with torch.cuda.stream(w.stream):
-                    self.d_item_trees[:ni].copy_(hs["item_trees"][:ni], non_blocking=True)
-                    self.d_ri[:nr].copy_(hs["ri"][:nr], non_blocking=True)
-                    self.d_rg[:nr].copy_(hs["rg"][:nr], non_blocking=True)
-                    self.d_rs[:nr].copy_(hs["rs"][:nr], non_blocking=True)
-                    self.d_rc[:nr].copy_(hs["rc"][:nr], non_blocking=True)
-                    self.d_rv[:nr * 8].copy_(hs["rv"][:nr * 8], non_blocking=True)
+                hn = hs["np"]
+                np.take(w.trees.view(np.int32), hn["items"][:ni], out=hn["item_trees"][:ni])
+                cp = self.copies[hs["k"]]
+                cp["bytes"][:] = (4 * ni, 4 * nr, 4 * nr, nr, nr, 16 * nr)  # item trees, ri, rg, rs, rc, rv
+                w.call("copy_to_device_async", 6, cp["dst"].ctypes.data, cp["src"].ctypes.data, cp["bytes"].ctypes.data)
                 w.call("apply_groups_async", ni, P(self.d_item_trees), P(self.d_flags), P(self.d_fill), nr,
                        P(self.d_ri), P(self.d_rg), P(self.d_rs), P(self.d_rc), P(self.d_rv), None, w.depth)
+        if gets:  # the gets' point sets in one call, then one batched world get each
+            ng = len(gets)
+            self.get_src[:ng] = [self.pool_ptr[g["pool"]] for g in gets]
+            w.call("copy_to_device_async", ng, self.get_dst.ctypes.data, self.get_src.ctypes.data,
+                   self.get_bytes.ctypes.data)
         for k, g in enumerate(gets):
-            with torch.cuda.stream(w.stream):
-                self.d_pts[k].copy_(self.pool_h[g["pool"]], non_blocking=True)
             w.call("world_get_async", C.byref(w.wdesc), C.c_uint64(self.ppg), P(self.d_pts[k]), P(self.d_found[k]),
                    P(self.d_vals[k]))
         if gets:
