@@ -11,12 +11,20 @@
 //     otherwise branch(children, types = leaf bits, mask = present bits) (voxtree.rs:1052-1061).
 //   The root is the level-0 result; an all-zero grid leaves the tree unchanged (voxtree.rs:905-911).
 //
-// GB300 mapping: one CTA owns a 32^3 block (or the whole chunk when it is smaller). The block is
-// brought into shared memory by one cp.async.bulk copy (TMA bulk engine) completing on an mbarrier,
-// then the CTA reduces it level by level entirely in shared memory; only hash-consing touches global
-// memory. Warps deduplicate identical 8-voxel groups with __match_any_sync before probing the
-// branch table, and inserts are warp-cooperative (vx_device.cuh). Grids are persistent: a multiple
-// of the SM count, each CTA striding over blocks.
+// GB300 mapping, by chunk depth:
+//   5-10 (launch_dense_split): dense_quads16_kernel streams every 16^3 octant through a per-warp
+//     shared tile (4-D TMA tensor copies completing on an mbarrier; octants after a warp's first one
+//     come from a device-wide counter) and settles every quad (4^3 voxels): uniform quads directly,
+//     the others through a device-wide quad memo, where a miss claims a record;
+//     dense_memo_compute_kernel then computes each claimed record (a distinct quad of the build)
+//     once, 8 lanes per quad; one pass per level above the quads resolves them and reduces parents
+//     (fresh_level_kernel, fresh_top_kernel for the three top levels).
+//   4: dense_octants_kernel, a warp per chunk-sized octant with all levels in the warp.
+//   2-3: dense_blocks_kernel, a CTA per chunk staged by one cp.async.bulk copy.
+//   vx_build_dense_noalloc: dense_cta32_kernel, a CTA per 32^3 block with block-level scratch only.
+// Only hash-consing touches global memory besides the grids. Warps deduplicate identical keys with
+// __match_any_sync before probing the branch table, and inserts are warp-cooperative
+// (vx_device.cuh). Grids are persistent: a multiple of the SM count.
 //
 // Refcounts follow from the reference's accounting (interner/mod.rs:712-829): a hash-cons hit gives
 // back the references its children were pre-charged with, so after a build every node's count equals
