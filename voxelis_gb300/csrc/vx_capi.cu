@@ -458,8 +458,8 @@ int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
         }
         {
             Phase ph(it, VX_PROF_RELEASE);
-            // the roots that die are the first dying set (round 1); a root heads a subtree of height at
-            // most max_depth, whose leaves die in round max_depth + 1
+            // the roots that die are the first dying set, retired by the first release pass; a root heads
+            // a subtree of height at most max_depth, whose leaves are retired by pass max_depth + 1
             VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity, it->capacity,
                                    a.max_depth > 0 && a.max_depth < 10 ? a.max_depth + 1 : 11, it->num_sms, s));
         }
