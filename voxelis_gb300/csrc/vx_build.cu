@@ -1752,61 +1752,56 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
     }
 }
 
-// The three top levels of kTopChunks chunks per CTA (depths 2, 1 and 0: 64 + 8 + 1 nodes a chunk)
-// from their depth-3 nodes, level by level in shared memory: one launch instead of three, whose
-// latency chains overlap across the CTAs.
-constexpr int kTopChunks = 4;
-#ifndef VX_TOP_MINB
-#define VX_TOP_MINB 4  // resident CTAs per SM the register allocation must allow (5 spills: measured slower)
-#endif
-
-__global__ void __launch_bounds__(kThreads, VX_TOP_MINB) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
-                                                             const uint32_t *in_vals, uint32_t n_chunks,
-                                                             const uint32_t *trees, uint8_t *changed,
-                                                             PendingView P) {
-    __shared__ uint64_t s2[64 * kTopChunks], s1[8 * kTopChunks];
-    __shared__ uint32_t v2[64 * kTopChunks], v1[8 * kTopChunks];
-    const unsigned t = threadIdx.x, warp = t >> 5, lane = t & 31u;
-    for (uint64_t c0 = (uint64_t)blockIdx.x * kTopChunks; c0 < n_chunks; c0 += (uint64_t)gridDim.x * kTopChunks) {
-        {  // depth 2: thread t takes node t of the CTA's chunks
-            const uint64_t p = c0 * 64 + t;
-            const bool in = c0 + t / 64 < n_chunks;
-            uint64_t c[8];
-            uint32_t cv[8];
+// The three top levels (depths 2, 1 and 0: 64 + 8 + 1 nodes a chunk) with one warp per chunk and
+// no CTA barrier: lanes reduce the chunk's 64 depth-2 parents in two passes, lanes 0-7 its 8 depth-1
+// parents from those (shuffles), lane 0 the root. 8 chunks per CTA; a 4096-chunk build is one wave
+// of warps at 64 registers (a CTA per 4 chunks with the levels split by CTA barriers needed 1.7
+// waves and idled 7 of its 8 warps at the barriers: 0.054 against 0.050 ms).
+__global__ void __launch_bounds__(kThreads) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
+                                                                  const uint32_t *in_vals, uint32_t n_chunks,
+                                                                  const uint32_t *trees, uint8_t *changed,
+                                                                  PendingView P) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t c = (uint64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    if (c >= n_chunks) return;  // the whole warp
+    uint64_t d2[2];
+    uint32_t v2[2];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                c[k] = in ? in_ids[8 * p + k] : 0;
-                cv[k] = in ? in_vals[8 * p + k] : 0;
-                resolve_pending(P, c[k], cv[k]);
-            }
-            reduce_parent_dedup(I, in, c, cv, s2[t], v2[t]);
+    for (int r = 0; r < 2; ++r) {  // depth 2: parent lane + 32 r of the chunk
+        const uint64_t p = c * 64 + lane + 32u * r;
+        uint64_t ch[8];
+        uint32_t cv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            ch[k] = in_ids[8 * p + k];
+            cv[k] = in_vals[8 * p + k];
+            resolve_pending(P, ch[k], cv[k]);
         }
-        __syncthreads();
-        if (warp == 0) {  // depth 1: lane l takes node l (chunk l / 8)
-            const bool in = c0 + lane / 8 < n_chunks;
-            uint64_t c[8];
-            uint32_t cv[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                c[k] = s2[8 * lane + k];
-                cv[k] = v2[8 * lane + k];
-            }
-            reduce_parent_dedup(I, in, c, cv, s1[lane], v1[lane]);
-            __syncwarp();
-            // roots: lane l < kTopChunks takes chunk c0 + l
-            const bool rin = lane < kTopChunks && c0 + lane < n_chunks;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                c[k] = rin ? s1[(8 * lane + k) & (8 * kTopChunks - 1)] : 0;
-                cv[k] = rin ? v1[(8 * lane + k) & (8 * kTopChunks - 1)] : 0;
-            }
-            uint64_t out;
-            uint32_t val;
-            reduce_parent_dedup(I, rin, c, cv, out, val);
-            if (rin) commit_root(I, trees, changed, c0 + lane, out);
-        }
-        __syncthreads();
+        reduce_parent_dedup(I, true, ch, cv, d2[r], v2[r]);
     }
+    // depth 1: lane q < 8 takes depth-2 nodes 8q .. 8q+7 (pass q >> 2)
+    uint64_t ch[8];
+    uint32_t cv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int src = (8 * lane + k) & 31;
+        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, d2[0], src), a1 = __shfl_sync(0xFFFFFFFFu, d2[1], src);
+        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, v2[0], src), b1 = __shfl_sync(0xFFFFFFFFu, v2[1], src);
+        ch[k] = lane < 4 ? a0 : a1;
+        cv[k] = lane < 4 ? b0 : b1;
+    }
+    uint64_t d1;
+    uint32_t v1;
+    reduce_parent_dedup(I, lane < 8, ch, cv, d1, v1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {  // the root from lanes 0-7
+        ch[k] = __shfl_sync(0xFFFFFFFFu, d1, k);
+        cv[k] = __shfl_sync(0xFFFFFFFFu, v1, k);
+    }
+    uint64_t root;
+    uint32_t rv;
+    reduce_parent_dedup(I, lane == 0, ch, cv, root, rv);
+    if (lane == 0) commit_root(I, trees, changed, c, root);
 }
 
 // Closes the epoch: the free-list entries and fresh indices its tickets took become allocated.
@@ -2211,10 +2206,10 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
         if (e != cudaSuccess) return e;
     }
     // depths 2, 1 and 0 in one launch
-    const unsigned top_blocks = (unsigned)((n_chunks + kTopChunks - 1) / kTopChunks);
     count_launches(1);
-    fresh_top_kernel<<<top_blocks, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed,
-                                                     depth == 5 ? P : PendingView{nullptr, 0, 0});
+    const unsigned wb = (unsigned)((n_chunks + kThreads / 32 - 1) / (kThreads / 32));
+    fresh_top_kernel<<<wb, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed,
+                                             depth == 5 ? P : PendingView{nullptr, 0, 0});
     return cudaGetLastError();
 }
 
