@@ -188,6 +188,8 @@ struct vx_interner {
     uint64_t seq_queue_cap = 0;
     unsigned long long *d_live = nullptr;
     int *d_status = nullptr;
+    unsigned long long *scan_status = nullptr;  // kScanStatusTiles look-back words, zeroed at creation
+    uint32_t scan_gen = 1;                      // next scan generation (0 never used)
     // pinned staging
     DevCounters *h_ctr = nullptr;
     int *h_status = nullptr;
@@ -423,6 +425,10 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     a.flags = c.take<uint32_t>(Rp);
     a.pos = c.take<uint32_t>(Rp);
     a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
+    a.scan_status = it->scan_status;
+    a.scan_gen = it->scan_gen;  // one generation per level step and apply mode of this call
+    it->scan_gen += 32;
+    if (it->scan_gen >= (1u << 29)) it->scan_gen = 1;
     a.e_item[0] = c.take<uint32_t>(R);
     a.e_item[1] = c.take<uint32_t>(R);
     a.e_path[0] = c.take<uint32_t>(R);
@@ -724,6 +730,8 @@ int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_fla
     alloc((void **)&it->frontier, 2 * cap * 4 + 64);
     alloc((void **)&it->d_live, 2 * sizeof(unsigned long long));
     alloc((void **)&it->d_status, sizeof(int) * 4);
+    alloc((void **)&it->scan_status, (size_t)kScanStatusTiles * 8);
+    if (ok && cudaMemset(it->scan_status, 0, (size_t)kScanStatusTiles * 8) != cudaSuccess) ok = false;
     if (patch_flags & VX_PATCH_P3) {
         it->seq_queue_cap = std::max<uint64_t>(cap + 1, 32768);
         alloc((void **)&it->seq_queue, it->seq_queue_cap * 8);
@@ -765,7 +773,8 @@ int vx_interner_destroy(vx_interner *it) {
     if (it->stream) cudaStreamSynchronize(it->stream);
     DevInterner &D = it->dev;
     void *ptrs[] = {D.children, D.values, D.refcount, D.generation, D.hash, D.ids, D.free_list, D.ctr, D.table,
-                    D.leaf_table, D.roots, D.depths, it->frontier, it->seq_queue, it->d_live, it->d_status};
+                    D.leaf_table, D.roots, D.depths, it->frontier, it->seq_queue, it->d_live, it->d_status,
+                    it->scan_status};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     it->ws.release();

@@ -129,6 +129,10 @@ __device__ __forceinline__ uint64_t ld_probe(const uint64_t *p) {
     return v;
 }
 
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // Publication with release semantics: every store of this thread before it is visible to a thread
 // that reads the new value with acquire semantics (ld_probe). Cheaper than a full fence before a
 // plain atomic, which also orders loads and waits for sequential consistency.

@@ -75,6 +75,8 @@ struct ApplyArgs {
     uint32_t *flags;             // [n_records + 1]
     uint32_t *pos;               // [n_records + 1]
     uint32_t *scan_tmp;          // block sums
+    unsigned long long *scan_status;  // [kScanStatusTiles] look-back words of one-pass scans (zeroed once)
+    uint32_t scan_gen;           // generation of this call's first scan (+16 mode + level step)
     uint32_t *e_item[2];
     uint32_t *e_path[2];
     uint64_t *e_id[2];
@@ -91,7 +93,10 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
 // Fills it_depth from the tree table and checks the deepest-first order (device-resident inputs).
 cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s);
 // Counter slots used by launch_apply (DevCounters::scratch indices).
-enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6, SC_DONE = 7 };
+enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6, SC_DONE = 7, SC_SCAN_TICKET = 8 };
+// Tiles of a one-pass device scan with a status word each (ApplyArgs::scan_status); larger scans
+// take the three-launch path.
+constexpr uint32_t kScanStatusTiles = 64;
 
 // Inclusive-to-exclusive scan of n u32 flags (n from the host) into pos; pos[n] = total.
 cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uint32_t n, cudaStream_t s);
