@@ -60,3 +60,13 @@ def test_library_has_no_oracle_dependency(gpu_library_path):
     data = open(gpu_library_path, "rb").read()
     assert b"vxo_" not in data
     assert b"vx_oracle" not in data
+
+
+def test_rust_binding_declares_every_entry_point():
+    """INTEGRATION.md's extern block (what a Rust crate would bind) covers the whole header."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = text[text.index("```rust"):]
+    block = block[:block.index("\n```\n")]
+    bound = set(re.findall(r"pub fn (vx_\w+)\s*\(", block))
+    missing = [n for n in declared() if n not in bound]
+    assert not missing, missing
