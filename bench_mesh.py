@@ -20,8 +20,8 @@ import time
 
 import numpy as np
 
-from . import workloads as W
-from ._abi import gpu_lib
+from voxelis_gb300 import workloads as W
+from voxelis_gb300._abi import gpu_lib
 
 N_SIDE = 64
 MAX_MAT = 8
@@ -30,7 +30,7 @@ MAX_MAT = 8
 def run(args):
     import torch
 
-    from .build import build as build_lib
+    from voxelis_gb300.build import build as build_lib
 
     build_lib()
     lib = gpu_lib()
@@ -209,7 +209,7 @@ def run(args):
     o_ms = (time.perf_counter() - t0) * 1e3
     ol.status("interner_destroy", oh)
     call("interner_destroy")
-    from .vtm import canonical, decode
+    from voxelis_gb300.vtm import canonical, decode
 
     same_model = canonical(*decode(blob.tobytes(), 1)) == canonical(*decode(o_blob.tobytes(), 1))
     serialize = {"bytes": int(size.value), "ms": ser_ms, "MB_per_s": size.value / (ser_ms * 1e-3) / 1e6,

@@ -89,6 +89,7 @@ typedef struct {
     uint64_t table_slots;     /* device branch table size (slots), 0 for the oracle               */
     uint64_t table_tombstones;/* deleted slots awaiting a rehash                                  */
     uint64_t error_flags;     /* sticky device error bits (see vx_interner_sync)                  */
+    uint64_t nodes_created;   /* node allocations (interner misses) since creation or reset       */
 } vx_interner_stats;
 
 /* Canonical depth-first export: nodes renumbered in pre-order over the given trees (children
@@ -179,9 +180,11 @@ int vx_apply_batches(vx_interner *it, uint32_t n, const vx_tree *trees,
 int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void *grids,
                    uint8_t *changed, vx_mem mem);
 /* Asynchronous form of vx_build_dense for trees that are EMPTY (freshly created, cleared or after
- * vx_interner_reset), all arguments in device memory and every tree of depth max_depth (checked on
- * the device: a mismatch reports VX_E_INVALID_ARG at the next sync). No host synchronisation, so
- * the call can be captured in a CUDA graph. */
+ * vx_interner_reset), all arguments in device memory and every tree of depth max_depth. Both are
+ * checked on the device before a chunk is built: a tree of another depth, or one whose root is not
+ * EMPTY, is left untouched, its changed flag is 0 and VX_E_INVALID_ARG is reported at the next sync
+ * (merging into an existing tree is vx_apply_groups_async's job). No host synchronisation, so the
+ * call can be captured in a CUDA graph. */
 int vx_build_dense_async(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
                          const void *grids_dev, uint8_t *changed_dev, int max_depth);
 /* Batched to_vec (utils/common.rs:158-246): out receives n dense [y][z][x] grids of side 2^d, one
@@ -313,21 +316,23 @@ uint64_t vx_kernel_launches(void);
  * Same arguments and result as vx_build_dense_async, for callers that cannot allocate device memory
  * during the call: code recorded into a CUDA graph (allocation is not allowed during stream
  * capture), frame loops and servers that fix their memory up front, hosts whose allocator belongs
- * to another runtime. The levels above 16^3 octants are staged in a fixed device array of
- * VX_NOALLOC_SCRATCH_BYTES compiled into the library (held by every GPU until exit): chunks of depth
- * d >= 5 need 12 n (8 + ... + 8^(d-4)) + 4 n (1 + ... + 8^(d-5)) bytes, and larger requests return
- * VX_E_BUFFER without queuing work. All calls share the array: calls whose device work overlaps
- * race, so serialise them. The first call on a device resolves the array's address and must come
- * before any stream capture. */
+ * to another runtime. The levels above the 32^3 blocks (depth d >= 6) are staged in a fixed device
+ * array of VX_NOALLOC_SCRATCH_BYTES compiled into the library (held by every GPU until exit): a call
+ * needs 12 n (8 + ... + 8^(d-5)) + 4 n (1 + ... + 8^(d-6)) bytes, rounded up to 256, plus 256 (about
+ * 100 bytes a chunk at depth 6, so some 31,000 chunks; depths 2-5 need no staging), and larger
+ * requests return VX_E_BUFFER without queuing work. All calls share the array: calls whose device
+ * work overlaps race, so serialise them. The first call on a device resolves the array's address
+ * and must come before any stream capture. */
 #define VX_NOALLOC_SCRATCH_BYTES (3u << 20)
 int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree *trees_dev,
                            const void *grids_dev, uint8_t *changed_dev, int max_depth);
 /* Waits for the stream, reports the sticky status, and rebuilds the branch table when deleted slots
  * exceed a quarter of it (the synchronous entry points do this themselves). */
 int vx_interner_maintain(vx_interner *it);
-/* Returns the interner to its freshly created state (no nodes, empty tables); tree handles stay
- * valid and their roots become EMPTY. Same result as destroying it and creating a new interner with
- * the same budget, without reallocating device memory. */
+/* Returns the interner to its freshly created state (no nodes, empty tables, every slot's
+ * generation back to 0); tree handles stay valid and their roots become EMPTY. Same result as
+ * destroying it and creating a new interner with the same budget, without reallocating device
+ * memory. */
 int vx_interner_reset(vx_interner *it);
 
 #ifdef __cplusplus

@@ -446,11 +446,17 @@ class Interner {
         if (!free_indices_.empty()) {
             uint32_t i = free_indices_.back();
             free_indices_.pop_back();
+            ++created_;
             return i;
         }
-        if (next_index_ < capacity_) return next_index_++;
+        if (next_index_ < capacity_) {
+            ++created_;
+            return next_index_++;
+        }
         throw RefOOM("Out of memory");
     }
+    // allocations so far (instrumentation; the reference keeps no such count)
+    uint64_t created() const { return created_; }
 
     // get_or_create_leaf (mod.rs:627-710)
     uint64_t get_or_create_leaf(T value) {
@@ -514,6 +520,7 @@ class Interner {
     std::vector<T> values_;
     std::vector<uint64_t> hashes_;
     size_t capacity_ = 0;
+    uint64_t created_ = 0;
     uint64_t empty_branch_id_ = 0, empty_branch_hash_ = 0;
     std::vector<uint64_t> stack_;
     uint32_t flags_ = 0;

@@ -202,6 +202,7 @@ int vxo_interner_stats_get(void *h, vx_interner_stats *s) {
         s->alive_nodes = s->next_index - s->free_count;
         s->branch_patterns = o.it.branch_patterns();
         s->leaf_patterns = o.it.leaf_patterns();
+        s->nodes_created = o.it.created();
         return VX_OK;
     });
 }

@@ -31,7 +31,7 @@ def test_served_results_equal_one_by_one(gpu_lib, max_edits):
     for j in res_alone:
         np.testing.assert_array_equal(res_mix[j][0], res_alone[j][0])
         np.testing.assert_array_equal(res_mix[j][1], res_alone[j][1])
-    from bench import export
+    from voxelis_gb300.api import export_canonical as export
 
     ca, cb = export(wa.lib, wa.h, wa.trees), export(wb.lib, wb.h, wb.trees)
     for k in ca:

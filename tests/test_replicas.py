@@ -40,3 +40,24 @@ def test_two_replicas_take_the_slowest_rank():
         assert p.exitcode == 0
     assert [r[1] for r in res] == [2.5, 2.5]
     assert res[0][2] == pytest.approx(2 * 4096 / 2.5e-3)
+
+
+def test_gpus_flag_launches_that_many_ranks():
+    """`bench.py --gpus 2` outside torchrun re-launches itself as two ranks (torch.distributed.run on
+    127.0.0.1); the reference arm, which needs no GPU, shows it: rank 0 alone reports, with n_gpus 2."""
+    import json
+    import subprocess
+
+    env = dict(os.environ)
+    for k in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(ln) for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["n_gpus"] == 2 and line["impl"] == "reference" and line["steps"] == 1
+    assert line["config"]["chunks"] == 4096 and line["config"]["parallelism"] == "replicas"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0

@@ -71,7 +71,7 @@ def error_for(status, message=""):
 class vx_interner_stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "capacity", "node_size", "next_index", "free_count", "alive_nodes", "branch_patterns",
-        "leaf_patterns", "table_slots", "table_tombstones", "error_flags")]
+        "leaf_patterns", "table_slots", "table_tombstones", "error_flags", "nodes_created")]
 
 
 class vx_world(C.Structure):

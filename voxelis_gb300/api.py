@@ -33,6 +33,59 @@ def _np_ptr(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def export_canonical(lib, handle, tree_handles):
+    """Canonical DFS export (vx_export_canonical) of the DAG reachable from the trees with the given
+    handles of the interner `handle` in library `lib`: a dict of numpy arrays (kind, types, mask,
+    value, refcount, children [n, 8], roots). Two interners holding the same DAG give equal arrays
+    whatever their allocation order."""
+    handles = np.ascontiguousarray(tree_handles, dtype=np.uint32)
+    n_nodes = C.c_uint64()
+    lib.call("export_canonical", handle, len(handles), _np_ptr(handles), None, C.byref(n_nodes), handle=handle)
+    n = n_nodes.value
+    arrays = {
+        "kind": np.zeros(n, np.uint8), "types": np.zeros(n, np.uint8),
+        "mask": np.zeros(n, np.uint8), "value": np.zeros(n, np.uint32),
+        "refcount": np.zeros(n, np.uint32), "children": np.zeros((n, 8), np.int32),
+        "roots": np.zeros(len(handles), np.int32),
+    }
+    c = _abi.vx_canonical()
+    for k in ("kind", "types", "mask"):
+        setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_uint8)))
+    for k in ("value", "refcount"):
+        setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_uint32)))
+    for k in ("children", "roots"):
+        setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_int32)))
+    c.capacity = n
+    lib.call("export_canonical", handle, len(handles), _np_ptr(handles), C.byref(c), C.byref(n_nodes), handle=handle)
+    return arrays
+
+
+def level_counts(canon):
+    """collect_stats (utils/common.rs:302-333) over a canonical export: the number of nodes at each
+    depth counted with tree multiplicity (a DAG node reached by k paths counts k times). Returns a
+    list, index = depth below the roots."""
+    n = len(canon["kind"])
+    children = np.asarray(canon["children"]).reshape(n, 8)
+    roots = np.asarray(canon["roots"])
+    # multiplicity of every node at the current depth (dense over node ids; exact in float64 below
+    # 2^53 paths)
+    mult = np.bincount(roots[roots >= 0], minlength=n).astype(np.float64)
+    out = []
+    while True:
+        nodes = np.flatnonzero(mult)
+        if not len(nodes):
+            return out
+        out.append(int(mult[nodes].sum()))
+        ch = children[nodes]                      # [m, 8], -1 for EMPTY (and every leaf slot)
+        keep = ch >= 0
+        mult = np.bincount(ch[keep], weights=np.repeat(mult[nodes], keep.sum(axis=1)), minlength=n)
+
+
+def same_dag(a, b):
+    """True when two canonical exports are identical in every array."""
+    return a.keys() == b.keys() and all(np.array_equal(a[k], b[k]) for k in a)
+
+
 class VoxInterner:
     """VoxInterner<T> (interner/mod.rs:25-40): the hash-consed node store, resident on the device."""
 
@@ -175,25 +228,7 @@ class VoxInterner:
     def export_canonical(self, trees):
         """Canonical DFS export of the DAG reachable from `trees` (see vx_canonical)."""
         handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)
-        n_nodes = C.c_uint64()
-        self._call("export_canonical", len(trees), _np_ptr(handles), None, C.byref(n_nodes))
-        n = n_nodes.value
-        arrays = {
-            "kind": np.zeros(n, np.uint8), "types": np.zeros(n, np.uint8),
-            "mask": np.zeros(n, np.uint8), "value": np.zeros(n, np.uint32),
-            "refcount": np.zeros(n, np.uint32), "children": np.zeros((n, 8), np.int32),
-            "roots": np.zeros(len(trees), np.int32),
-        }
-        c = _abi.vx_canonical()
-        for k in ("kind", "types", "mask"):
-            setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_uint8)))
-        for k in ("value", "refcount"):
-            setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_uint32)))
-        for k in ("children", "roots"):
-            setattr(c, k, arrays[k].ctypes.data_as(C.POINTER(C.c_int32)))
-        c.capacity = n
-        self._call("export_canonical", len(trees), _np_ptr(handles), C.byref(c), C.byref(n_nodes))
-        return arrays
+        return export_canonical(self.lib, self.handle, handles)
 
     def validate(self, trees):
         handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)

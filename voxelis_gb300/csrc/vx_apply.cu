@@ -306,11 +306,12 @@ __global__ void __launch_bounds__(kThreads) scan_blocks_dev_kernel(const uint32_
 // counter, publish their tile sum (state 1) at once and their inclusive prefix (state 2) as soon as
 // they know it; a tile's prefix is found by walking back over earlier tiles' status words until one
 // holds an inclusive prefix. A CTA only waits on tiles whose tickets were taken earlier, by CTAs
-// that are therefore running or done, and the walk is bounded (ERR_TIMEOUT). Status words carry the
-// call's generation (bits 34-63), so stale words of earlier scans read as not ready; the CTA with
-// the last ticket resets the counter for the next scan.
+// that are therefore running or done, and the walk is bounded (ERR_TIMEOUT). Every scan starts with
+// all status words at state 0: the last CTA to finish (all look-back walks are over by then) clears
+// the words this scan used, so the state lives on the device alone and a scan replayed from a CUDA
+// graph behaves as one launched directly. The CTA with the last ticket resets the ticket counter.
 __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner I, const uint32_t *in, uint32_t *out,
-                                                                   unsigned long long *status, uint32_t gen,
+                                                                   unsigned long long *status,
                                                                    const unsigned long long *n_dev) {
     __shared__ uint32_t tile_s, prefix_s;
     __shared__ uint32_t warp_tot[kThreads / 32];
@@ -351,10 +352,9 @@ __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner 
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t agg = warp_tot[kThreads / 32 - 1];
-        const unsigned long long G = (unsigned long long)gen << 34;
         uint32_t excl = 0;
         if (tile > 0) {
-            st_release_u64(status + tile, G | (1ull << 32) | agg);
+            st_release_u64(status + tile, (1ull << 32) | agg);
             uint32_t j = tile - 1;
             for (uint32_t spin = 0;; ++spin) {
                 if (spin >= SPIN_LIMIT) {
@@ -362,13 +362,14 @@ __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner 
                     break;
                 }
                 const unsigned long long w = ld_acquire(reinterpret_cast<const uint64_t *>(status + j));
-                if ((w >> 34) != gen || ((w >> 32) & 3ull) == 0) continue;  // tile j has not published yet
+                const unsigned long long state = (w >> 32) & 3ull;
+                if (state == 0) continue;  // tile j has not published yet
                 excl += (uint32_t)w;
-                if (((w >> 32) & 3ull) == 2ull || j == 0) break;  // an inclusive prefix ends the walk
+                if (state == 2ull || j == 0) break;  // an inclusive prefix ends the walk
                 --j;
             }
         }
-        st_release_u64(status + tile, G | (2ull << 32) | (excl + agg));
+        st_release_u64(status + tile, (2ull << 32) | (excl + agg));
         prefix_s = excl;
     }
     __syncthreads();
@@ -380,6 +381,8 @@ __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner 
         if (base + k + 1 == n) out[n] = run;  // the total after the last element
     }
     if (n == 0 && tile == 0 && threadIdx.x == 0) out[0] = 0;
+    if (grid_last_cta(&I.ctr->scratch[SC_SCAN_DONE]))  // no walk reads a status word any more
+        for (uint32_t t = 0; t < gridDim.x; ++t) status[t] = 0;
 }
 
 __global__ void scan_add_dev_kernel(uint32_t *out, const uint32_t *sums, const unsigned long long *n_dev) {
@@ -678,12 +681,12 @@ size_t scan_tmp_words(uint32_t n) { return (size_t)(n + kScanBlock - 1) / kScanB
 // measured 12% slower than the three launches on 45 M edits).
 static cudaError_t launch_scan_dev(const DevInterner &I, const uint32_t *flags, uint32_t *pos, uint32_t *tmp,
                                    uint32_t n_max, const unsigned long long *n_dev, unsigned long long *status,
-                                   uint32_t gen, cudaStream_t s) {
+                                   cudaStream_t s) {
     const uint32_t nb = (n_max + kScanBlock - 1) / kScanBlock;
     if (nb == 0) return cudaSuccess;
     if (status && nb <= kScanStatusTiles) {
         count_launches(1);
-        scan_onepass_dev_kernel<<<nb, kThreads, 0, s>>>(I, flags, pos, status, gen, n_dev);
+        scan_onepass_dev_kernel<<<nb, kThreads, 0, s>>>(I, flags, pos, status, n_dev);
         return cudaGetLastError();
     }
     count_launches(1);
@@ -762,8 +765,7 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
         for (int step = 1; step <= a.max_depth - 1; ++step) {
             count_launches(1);
             heads_kernel<<<sb, kThreads, 0, s>>>(I, a, step, buf);
-            e = launch_scan_dev(I, a.flags, a.pos, a.scan_tmp, R, &I.ctr->scratch[SC_ENTRIES], a.scan_status,
-                                a.scan_gen + 16u * (uint32_t)a.mode + (uint32_t)step, s);
+            e = launch_scan_dev(I, a.flags, a.pos, a.scan_tmp, R, &I.ctr->scratch[SC_ENTRIES], a.scan_status, s);
             if (e != cudaSuccess) return e;
             count_launches(1);
             starts_kernel<<<sb, kThreads, 0, s>>>(I, a);

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
         {
             // tree handles may come from device memory: check them before any write
             const uint32_t tree = a.trees[chunk];
-            const bool bad = tree >= I.tree_cap || I.depths[tree] != a.depth;
+            const bool bad = tree >= I.tree_cap || I.depths[tree] != a.depth || I.roots[tree] != EMPTY_ID;
             if (__syncthreads_or(bad)) {
                 if (tid == 0) set_error(I, ERR_INVALID, 21);
                 continue;
@@ -946,7 +946,7 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
         const uint32_t c = (uint32_t)(o >> ob);
         uint64_t q = o & ((1ull << ob) - 1);
         const uint32_t tree = a.trees[c];
-        const bool bad = tree >= I.tree_cap || I.depths[tree] != d;
+        const bool bad = tree >= I.tree_cap || I.depths[tree] != d || I.roots[tree] != EMPTY_ID;
         if (bad) {
             if (lane == 0) set_error(I, ERR_INVALID, 26);
             if (kOctTiles == 1 && nx < n_oct && lane == 0) issue(nx, 0);
@@ -1102,7 +1102,7 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
         const uint32_t c = (uint32_t)(blk >> bb);
         uint64_t q = blk & ((1ull << bb) - 1);
         const uint32_t tree = a.trees[c];
-        if (tree >= I.tree_cap || I.depths[tree] != d) {  // the same answer in every thread
+        if (tree >= I.tree_cap || I.depths[tree] != d || I.roots[tree] != EMPTY_ID) {  // the same answer in every thread
             if (tid == 0) {
                 set_error(I, ERR_INVALID, 28);
                 if (nxt < n_blk) issue(nxt);
@@ -1519,7 +1519,7 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
         const uint64_t q = o & ((1ull << ob) - 1);
         // the tree check's two dependent loads go out before the wait, beside the tile's copy
         const uint32_t tree = a.trees[c];
-        const bool tree_ok = tree < I.tree_cap && I.depths[tree] == d;
+        const bool tree_ok = tree < I.tree_cap && I.depths[tree] == d && I.roots[tree] == EMPTY_ID;
         bool ok = false;
         for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin)
             if ((ok = mbar_try_wait(bars + b, (j / NT) & 1u))) break;
@@ -1812,6 +1812,7 @@ __device__ __forceinline__ void epoch_finalize_body(const DevInterner &I) {
     c->free_count = fc - used_free;
     unsigned long long ni = c->next_index + (alloc - used_free);
     if (ni > I.capacity) ni = I.capacity;
+    c->created += used_free + (ni - c->next_index);
     c->next_index = ni;
     c->alloc_count = 0;
 }
@@ -1980,11 +1981,19 @@ cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int nu
     return launch_persistent(dense_blocks_kernel<uint16_t>, I, a, smem, num_sms, s);
 }
 
+// log2 of the side of the unit that one CTA (32^3 blocks, depths 5-10) or one warp (16^3 octants,
+// depth 4) of launch_dense_octants reduces; the scratch holds the levels above that unit.
+static int dense_octant_unit(int depth) { return (VX_DENSE_CTA32 && depth >= 5) ? 5 : 4; }
+
+// Scratch of launch_dense_octants, laid out as it carves it: node ids (8 B) and LOD values (4 B) of
+// every level above the unit, then (from a 256-byte boundary) the arrival counts of every level
+// above the unit's parents.
 size_t dense_octant_scratch_bytes(uint64_t n_chunks, int depth) {
+    const int unit = dense_octant_unit(depth);
     size_t ids = 0, cnts = 0;
-    for (int k = 1; k <= depth - 4; ++k) ids += (size_t)n_chunks << (3 * k);
-    for (int k = 0; k <= depth - 5; ++k) cnts += (size_t)n_chunks << (3 * k);
-    return ids * 12 + cnts * 4 + 512;
+    for (int k = 1; k <= depth - unit; ++k) ids += (size_t)n_chunks << (3 * k);
+    for (int k = 0; k <= depth - unit - 1; ++k) cnts += (size_t)n_chunks << (3 * k);
+    return ((ids * 12 + 255) & ~(size_t)255) + cnts * 4 + 256;
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -2023,8 +2032,8 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
                                  void *memo, bool clear_memo, uint64_t memo_chunks) {
     if (n_chunks == 0) return cudaSuccess;
     if (depth < 4 || depth > 10) return cudaErrorInvalidValue;
-    const bool cta32 = VX_DENSE_CTA32 && depth >= 5;
-    const int unit = cta32 ? 5 : 4;  // log2 of the side of the unit one CTA (or warp) reduces
+    const int unit = dense_octant_unit(depth);
+    const bool cta32 = unit == 5;
     OctArgs a{};
     a.trees = trees;
     a.n_chunks = n_chunks;

@@ -188,8 +188,7 @@ struct vx_interner {
     uint64_t seq_queue_cap = 0;
     unsigned long long *d_live = nullptr;
     int *d_status = nullptr;
-    unsigned long long *scan_status = nullptr;  // kScanStatusTiles look-back words, zeroed at creation
-    uint32_t scan_gen = 1;                      // next scan generation (0 never used)
+    unsigned long long *scan_status = nullptr;  // kScanStatusTiles look-back words, zero between scans
     // pinned staging
     DevCounters *h_ctr = nullptr;
     int *h_status = nullptr;
@@ -426,9 +425,6 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     a.pos = c.take<uint32_t>(Rp);
     a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
     a.scan_status = it->scan_status;
-    a.scan_gen = it->scan_gen;  // one generation per level step and apply mode of this call
-    it->scan_gen += 32;
-    if (it->scan_gen >= (1u << 29)) it->scan_gen = 1;
     a.e_item[0] = c.take<uint32_t>(R);
     a.e_item[1] = c.take<uint32_t>(R);
     a.e_path[0] = c.take<uint32_t>(R);
@@ -832,6 +828,12 @@ int vx_interner_reset(vx_interner *it) {
     VX_CUDA(cudaMemsetAsync(it->dev.roots, 0, (size_t)it->tree_cap * 8, s));
     VX_CUDA(cudaMemsetAsync(it->dev.ids, 0, it->capacity * 8, s));
     VX_CUDA(cudaMemsetAsync(it->dev.refcount, 0, it->capacity * 4, s));
+    // the rest of the node records as vx_interner_create leaves them: recycled slots carry bumped
+    // generations (which become part of new BlockIds) and old records
+    VX_CUDA(cudaMemsetAsync(it->dev.generation, 0, it->capacity * 2, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.children, 0, it->capacity * 64, s));
+    VX_CUDA(cudaMemsetAsync(it->dev.values, 0, it->capacity * (it->vbits / 8), s));
+    VX_CUDA(cudaMemsetAsync(it->dev.hash, 0, it->capacity * 8, s));
     DevCounters c0{};
     c0.next_index = 1;
     *it->h_ctr = c0;
@@ -877,6 +879,7 @@ int vx_interner_stats_get(vx_interner *it, vx_interner_stats *out) {
     out->table_slots = it->table_slots;
     out->table_tombstones = it->h_ctr->tombstones;
     out->error_flags = it->h_ctr->error;
+    out->nodes_created = it->h_ctr->created;
     return st == VX_E_OOB || st == VX_E_REF_PANIC ? VX_OK : st;
 }
 

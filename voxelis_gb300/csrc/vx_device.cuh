@@ -59,6 +59,7 @@ struct DevCounters {
     unsigned int error;              // sticky ERR_* bits
     unsigned int error_info;         // first error detail
     unsigned long long scratch[10];  // per-launch counters used by the kernels
+    unsigned long long created;      // nodes allocated since the interner was created or reset
 };
 
 struct DevInterner {

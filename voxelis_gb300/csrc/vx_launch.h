@@ -22,9 +22,10 @@ struct DenseArgs {
 // Builds whole chunks of depth 2 or 3, one CTA per chunk (staged in shared memory by one bulk copy).
 cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int num_sms, cudaStream_t s);
 
-// Fused dense construction for chunk depths 4..10: warps take 16^3 octants (TMA tensor copies),
-// levels above octants are reduced by the last-arriving warp of each parent. `scratch` must hold
-// dense_octant_scratch_bytes(n, depth) bytes; it is cleared inside.
+// Fused dense construction for chunk depths 4..10: a warp per 16^3 octant at depth 4, a CTA per
+// 32^3 block at depths 5-10 (TMA tensor copies); levels above those units are reduced by the
+// last-arriving warp or CTA of each parent. `scratch` must hold dense_octant_scratch_bytes(n, depth)
+// bytes (the layout the launch carves); its arrival counts are cleared inside.
 // `memo` (optional, dense_octant_memo_bytes) holds the quad memo; it is cleared inside unless
 // clear_memo is false (later pieces of one build share the memo of the first: no release runs in
 // between, so every node it names is still alive). memo_chunks (0: n_chunks) sizes the memo and must
@@ -75,8 +76,7 @@ struct ApplyArgs {
     uint32_t *flags;             // [n_records + 1]
     uint32_t *pos;               // [n_records + 1]
     uint32_t *scan_tmp;          // block sums
-    unsigned long long *scan_status;  // [kScanStatusTiles] look-back words of one-pass scans (zeroed once)
-    uint32_t scan_gen;           // generation of this call's first scan (+16 mode + level step)
+    unsigned long long *scan_status;  // [kScanStatusTiles] look-back words of one-pass scans (all 0 between scans)
     uint32_t *e_item[2];
     uint32_t *e_path[2];
     uint64_t *e_id[2];
@@ -93,9 +93,12 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
 // Fills it_depth from the tree table and checks the deepest-first order (device-resident inputs).
 cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s);
 // Counter slots used by launch_apply (DevCounters::scratch indices).
-enum : int { SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6, SC_DONE = 7, SC_SCAN_TICKET = 8 };
-// Tiles of a one-pass device scan with a status word each (ApplyArgs::scan_status); larger scans
-// take the three-launch path.
+enum : int {
+    SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6,
+    SC_DONE = 7, SC_SCAN_TICKET = 8, SC_SCAN_DONE = 9
+};
+// Tiles of a one-pass device scan with a status word each (ApplyArgs::scan_status, zero between
+// scans: the scan's last CTA clears them); larger scans take the three-launch path.
 constexpr uint32_t kScanStatusTiles = 64;
 
 // Inclusive-to-exclusive scan of n u32 flags (n from the host) into pos; pos[n] = total.

@@ -8,10 +8,12 @@
 // array compiled into the library.
 //
 // Limits and sharing: the array holds VX_NOALLOC_SCRATCH_BYTES (3 MiB of device memory that every
-// GPU loading the library keeps until the process exits). For chunks of depth d >= 5 a call needs
-// 12 * n * (8 + 8^2 + ... + 8^(d-4)) + 4 * n * (1 + 8 + ... + 8^(d-5)) bytes (node rows above the
-// 16^3 octants plus their arrival counts; nothing below depth 5); larger requests are rejected with
-// VX_E_BUFFER before any work is queued. All calls share the one array: two calls whose device work
+// GPU loading the library keeps until the process exits). Chunks of depth 5-10 are reduced one CTA
+// per 32^3 block (dense_cta32_kernel); for depth d >= 6 a call stages the node rows of the levels
+// above those blocks and their arrival counts, 12 * n * (8 + 8^2 + ... + 8^(d-5)) bytes rounded up to
+// 256 plus 4 * n * (1 + 8 + ... + 8^(d-6)) + 256 bytes (dense_octant_scratch_bytes, the layout the
+// launch carves). Depths 2-5 stage nothing. Larger requests are rejected with VX_E_BUFFER before
+// any work is queued. All calls share the one array: two calls whose device work
 // overlaps (different streams or interners at the same time) race on it, so serialise them. The
 // arrival counts a call uses are cleared (cudaMemsetAsync) before its kernel runs; every node row is
 // written before it is read.
@@ -35,7 +37,7 @@ using namespace vxg;
 namespace {
 
 constexpr uint64_t kBytes = VX_NOALLOC_SCRATCH_BYTES;
-// node rows (ids, LOD values) of the levels above 16^3 octants, then their arrival counts
+// node rows (ids, LOD values) of the levels above the 32^3 blocks, then their arrival counts
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
 constexpr int kMaxDevices = 64;
@@ -82,7 +84,7 @@ extern "C" int vx_build_dense_noalloc(vx_interner *it, uint32_t n, const vx_tree
         interner_set_error(it, "grids must be 16-byte aligned");
         return VX_E_INVALID_ARG;
     }
-    const uint64_t need = max_depth >= 5 ? dense_octant_scratch_bytes(n, max_depth) : 0;
+    const uint64_t need = max_depth >= 4 ? dense_octant_scratch_bytes(n, max_depth) : 0;
     if (need > kBytes) {
         interner_set_error(it, "request exceeds the fixed scratch of vx_build_dense_noalloc");
         return VX_E_BUFFER;

@@ -170,6 +170,7 @@ __device__ uint32_t seq_alloc(Seq &S) {
     DevCounters *c = S.I.ctr;
     if (c->free_count > 0) {
         c->free_count -= 1;
+        c->created += 1;
         return S.I.free_list[c->free_count];
     }
     if (c->next_index >= S.I.capacity) {
@@ -177,6 +178,7 @@ __device__ uint32_t seq_alloc(Seq &S) {
         S.ok = false;
         return NO_NODE;
     }
+    c->created += 1;
     return (uint32_t)(c->next_index++);
 }
 

@@ -167,6 +167,8 @@ class Server:
         self.stage = self.lib.lib.vx_stage_spheres
         self.stage.restype = C.c_int
         self.waves = 0
+        # work done, for the algorithmic-bytes count: staged group records, items (chunk applies), points read
+        self.records = self.items = self.points = 0
 
     # -- wave formation ------------------------------------------------------------------------------
     def form_wave(self, pending, start):
@@ -210,6 +212,8 @@ class Server:
             if st != 0:
                 raise RuntimeError("vx_stage_spheres failed: %d" % st)
             ni, nr = ni.value, nr.value
+            self.records += nr
+            self.items += ni
             if ni:
                 hn = hs["np"]
                 np.take(w.trees.view(np.int32), hn["items"][:ni], out=hn["item_trees"][:ni])
@@ -220,6 +224,7 @@ class Server:
                        P(self.d_ri), P(self.d_rg), P(self.d_rs), P(self.d_rc), P(self.d_rv), None, w.depth)
         if gets:  # the gets' point sets in one call, then one batched world get each
             ng = len(gets)
+            self.points += ng * self.ppg
             self.get_src[:ng] = [self.pool_ptr[g["pool"]] for g in gets]
             w.call("copy_to_device_async", ng, self.get_dst.ctypes.data, self.get_src.ctypes.data,
                    self.get_bytes.ctypes.data)
