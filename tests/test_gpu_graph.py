@@ -8,14 +8,13 @@ import numpy as np
 import pytest
 
 from voxelis_gb300 import workloads as W
+from voxelis_gb300.api import export_canonical as export
 
 pytestmark = pytest.mark.gpu
 
 
 def test_dense_build_and_gets_replay_from_a_cuda_graph(gpu_lib):
     import torch
-
-    from voxelis_gb300.api import export_canonical as export
 
     dev = torch.device("cuda", 0)
     n = 64

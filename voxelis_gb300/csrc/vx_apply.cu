@@ -25,9 +25,13 @@
 // Trees are processed deepest first, so the trees whose root is produced at a step are the tail
 // of that step's list and the next list is a prefix of the parents.
 //
-// Refcounts. After the build every count is the in-degree from newly created nodes plus tree roots
-// (counted once per epoch over the allocation log), plus these corrections, which reproduce where
-// the reference's increments differ from the references its nodes hold:
+// Refcounts. After the build every count is the in-degree from newly created nodes plus tree roots,
+// plus the corrections below. The lane that creates a branch adds its children's references right
+// away, from the key it still holds in registers (no re-read of the node): branch children by a
+// global reduction, leaf children into a per-CTA table indexed by leaf value that the CTA flushes
+// once (leaves are the hot spots: a few values are named by most bottom groups). The last CTA of
+// the root-commit kernel closes the allocation epoch. The corrections reproduce where the
+// reference's increments differ from the references its nodes hold:
 //   Q5 (voxtree.rs:835-839, 846-868): an ancestor leaf is charged 8 - |set| references, but only
 //      8 - |modified| slots keep it: + (|modified| - |set|), or + (8 - |set|) when nothing changed.
 //   Q6 (voxtree.rs:1062-1072): a collapse with c cloned children gives back min(c, 7) instead of
@@ -40,11 +44,93 @@ namespace vxg {
 namespace {
 
 constexpr int kThreads = 256;
+// minimum resident CTAs of 512 threads the branch-creating kernels are compiled for (2: at most 64
+// registers a thread)
+#ifndef VX_APPLY_MIN_BLOCKS
+#define VX_APPLY_MIN_BLOCKS 2
+#endif
 constexpr int kScanPer = 8;
 constexpr int kScanBlock = kThreads * kScanPer;
 
 __device__ __forceinline__ void add_ref_delta(const DevInterner &I, uint64_t id, int delta) {
     if (delta != 0 && id != EMPTY_ID) atomicAdd(I.refcount + id_index(id), (unsigned)delta);
+}
+
+// Per-CTA counts of leaf-child references (dynamic shared memory, leaf_refs_smem bytes). 8-bit
+// voxels: one counter per value. 16-bit voxels: kLeafSlots counters direct-mapped by value with the
+// owning value as a tag; a value whose slot another value owns goes straight to a global reduction.
+constexpr uint32_t kLeafSlots = 4096;
+struct LeafRefs {
+    uint32_t *cnt;
+    uint32_t *tag;  // value + 1 owning the slot, 0 = free (16-bit voxels only)
+    uint32_t slots;
+    bool direct;
+};
+
+__device__ __forceinline__ LeafRefs leaf_refs_init(const DevInterner &I) {
+    extern __shared__ uint32_t leaf_smem[];
+    LeafRefs L;
+    L.direct = I.vbits == 8;
+    L.slots = L.direct ? 256u : kLeafSlots;
+    L.cnt = leaf_smem;
+    L.tag = leaf_smem + L.slots;
+    for (uint32_t k = threadIdx.x; k < (L.direct ? L.slots : 2 * L.slots); k += blockDim.x) leaf_smem[k] = 0;
+    __syncthreads();
+    return L;
+}
+
+__device__ __forceinline__ void leaf_ref_add(const DevInterner &I, const LeafRefs &L, uint64_t leaf, uint32_t value,
+                                             uint32_t n) {
+    if (L.direct) {
+        atomicAdd(L.cnt + value, n);
+        return;
+    }
+    const uint32_t s = value & (kLeafSlots - 1u), key = value + 1u;
+    uint32_t t = L.tag[s];
+    if (t == 0) {
+        t = atomicCAS(L.tag + s, 0u, key);
+        if (t == 0) t = key;
+    }
+    if (t == key)
+        atomicAdd(L.cnt + s, n);
+    else
+        atomicAdd(I.refcount + id_index(leaf), n);
+}
+
+// One reference per child slot of a node this lane just created (equal children summed first).
+__device__ __forceinline__ void add_child_refs(const DevInterner &I, const LeafRefs &L, const uint64_t c[8],
+                                               const uint32_t cv[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (c[k] == EMPTY_ID) continue;
+        bool seen = false;
+        uint32_t n = 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < k && c[j] == c[k]) seen = true;
+            if (j > k && c[j] == c[k]) ++n;
+        }
+        if (seen) continue;
+        if (id_is_leaf(c[k]))
+            leaf_ref_add(I, L, c[k], cv[k], n);
+        else
+            atomicAdd(I.refcount + id_index(c[k]), n);
+    }
+}
+
+// Adds the CTA's leaf counts to the leaves' global counts (every thread of the CTA calls it).
+__device__ __forceinline__ void leaf_refs_flush(const DevInterner &I, const LeafRefs &L) {
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < L.slots; s += blockDim.x) {
+        const uint32_t n = L.cnt[s];
+        if (n == 0) continue;
+        const uint32_t v = L.direct ? s : L.tag[s] - 1u;
+        const uint64_t lid = I.leaf_table[v];
+        if (lid > LEAF_BUSY)
+            atomicAdd(I.refcount + id_index(lid), n);
+        else
+            set_error(I, ERR_INTERNAL, 47);
+    }
 }
 
 __global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
@@ -71,7 +157,8 @@ __global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
     a.it_new[i] = (f & 2) ? INVALID_ID : init;
 }
 
-__global__ void __launch_bounds__(512) bottom_kernel(DevInterner I, ApplyArgs a) {
+__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInterner I, ApplyArgs a) {
+    const LeafRefs L = leaf_refs_init(I);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.n_records; base += stride) {
         const uint64_t r = base + threadIdx.x;
@@ -206,6 +293,7 @@ __global__ void __launch_bounds__(512) bottom_kernel(DevInterner I, ApplyArgs a)
         }
         bool created;
         const uint64_t id = warp_intern_branch_inl(I, want_branch, c, types, mask, lod, &created);
+        if (created) add_child_refs(I, L, c, cv);
         if (want_branch) out = id;
         if (r < a.n_records) {
             a.flags[r] = changed;
@@ -213,6 +301,7 @@ __global__ void __launch_bounds__(512) bottom_kernel(DevInterner I, ApplyArgs a)
             a.rec_val[r] = lod;
         }
     }
+    leaf_refs_flush(I, L);
 }
 
 // Exclusive scan of n flags: per-block scan, scan of block sums, add-back. pos[n] = total.
@@ -461,7 +550,8 @@ __device__ __forceinline__ void next_count(const DevInterner &I) {
     I.ctr->scratch[SC_ENTRIES] = I.ctr->scratch[SC_PARENTS] - I.ctr->scratch[SC_ROOTS];
 }
 
-__global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    const LeafRefs L = leaf_refs_init(I);
     const uint32_t n_par = (uint32_t)I.ctr->scratch[SC_PARENTS];
     const int nb = buf ^ 1;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -498,12 +588,18 @@ __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a
                 leaf = eq;
                 eq = EMPTY_ID;
             }
-            // gather the run of new children (voxtree.rs:959-1000)
+            // gather the run of new children (voxtree.rs:959-1000); slots by select, so that the
+            // arrays stay in registers
             for (uint32_t j = b; j < e; ++j) {
                 const uint32_t ti = (a.e_path[buf][j] >> (3 * (d - t))) & 7u;
                 const uint64_t id = a.e_id[buf][j];
-                c[ti] = id;
-                cv[ti] = a.e_val[buf][j];
+                const uint32_t ev = a.e_val[buf][j];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if ((uint32_t)k == ti) {
+                        c[k] = id;
+                        cv[k] = ev;
+                    }
                 types |= (id_is_leaf(id) ? 1u : 0u) << ti;
                 mask |= 1u << ti;
             }
@@ -598,6 +694,7 @@ __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a
             }
         bool created;
         const uint64_t id = warp_intern_branch_inl(I, want_branch, c, types, mask, lod, &created);
+        if (created) add_child_refs(I, L, c, cv);
         if (!in) continue;
         if (want_branch) {
             out = id;
@@ -613,14 +710,13 @@ __global__ void __launch_bounds__(512) parents_kernel(DevInterner I, ApplyArgs a
             a.e_val[nb][p] = out_val;
         }
     }
+    leaf_refs_flush(I, L);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) next_count(I);  // entries of the next step
 }
 
 
 
-__global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_items) return;
+__device__ __forceinline__ void finish_item(const DevInterner &I, const ApplyArgs &a, uint32_t i) {
     if (a.mode == 1) {
         const uint64_t nw = a.it_new[i], old = a.it_old[i];
         if (nw == INVALID_ID) return;
@@ -651,6 +747,14 @@ __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
     a.it_changed[i] = 1;
 }
 
+// Commits every item's root, then (last CTA) closes the allocation epoch: every node of this apply
+// pass has been created and has added its children's references by now.
+__global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.n_items) finish_item(I, a, i);
+    if (grid_last_cta(&I.ctr->scratch[SC_DONE])) epoch_finalize_body(I);
+}
+
 __global__ void zero_counter_kernel(DevInterner I, int slot) { I.ctr->scratch[slot] = 0; }
 
 __global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
@@ -674,6 +778,9 @@ __global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
 }  // namespace
 
 size_t scan_tmp_words(uint32_t n) { return (size_t)(n + kScanBlock - 1) / kScanBlock + 32; }
+
+// Dynamic shared memory of the kernels that create branches (their LeafRefs table).
+static size_t leaf_refs_smem(const DevInterner &I) { return I.vbits == 8 ? 256 * 4 : 2 * kLeafSlots * 4; }
 
 // Scan of the first *n_dev of n_max flags (count in device memory): one launch with the look-back
 // status words for up to kScanStatusTiles tiles (a serving wave's records: 4 fewer launches per
@@ -742,7 +849,7 @@ cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int nu
         const unsigned need = (R + bt - 1) / bt;
         const unsigned g = need < cap ? need : cap;
         count_launches(1);
-        bottom_kernel<<<g, bt, 0, s>>>(I, a);
+        bottom_kernel<<<g, bt, leaf_refs_smem(I), s>>>(I, a);
     }
     return cudaGetLastError();
 }
@@ -770,14 +877,14 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
             count_launches(1);
             starts_kernel<<<sb, kThreads, 0, s>>>(I, a);
             count_launches(1);
-            parents_kernel<<<g, bt, 0, s>>>(I, a, step, buf);  // its last CTA sets the next entry count
+            parents_kernel<<<g, bt, leaf_refs_smem(I), s>>>(I, a, step, buf);  // its last CTA sets the next entry count
             buf ^= 1;
         }
     }
     count_launches(1);
     zero_counter_kernel<<<1, 1, 0, s>>>(I, SC_RELEASE);
     count_launches(1);
-    finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
+    finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);  // its last CTA closes the epoch
     return cudaGetLastError();
 }
 

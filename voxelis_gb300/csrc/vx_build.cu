@@ -1804,19 +1804,6 @@ __global__ void __launch_bounds__(kThreads) fresh_top_kernel(DevInterner I, cons
     if (lane == 0) commit_root(I, trees, changed, c, root);
 }
 
-// Closes the epoch: the free-list entries and fresh indices its tickets took become allocated.
-__device__ __forceinline__ void epoch_finalize_body(const DevInterner &I) {
-    DevCounters *c = I.ctr;
-    const unsigned long long alloc = c->alloc_count, fc = c->free_count;
-    const unsigned long long used_free = alloc < fc ? alloc : fc;
-    c->free_count = fc - used_free;
-    unsigned long long ni = c->next_index + (alloc - used_free);
-    if (ni > I.capacity) ni = I.capacity;
-    c->created += used_free + (ni - c->next_index);
-    c->next_index = ni;
-    c->alloc_count = 0;
-}
-
 // Adds one reference per child slot of every node created in this epoch. Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
 // bottom groups), so they are summed per CTA before touching global memory: 8-bit leaves in a
 // 256-entry array indexed by value, wider leaves in an open-addressed shared table keyed by node

@@ -440,8 +440,8 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     return VX_OK;
 }
 
-// The set phase, its refcount epoch and release, then (P4) the clear pass with its own epoch and
-// release. No host synchronisation.
+// The set phase (its kernels count references as they create nodes and close the allocation epoch)
+// and its release, then (P4) the clear pass with its own epoch and release. No host synchronisation.
 int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
     cudaStream_t s = it->stream;
     for (int mode = 0; mode < (clear_pass ? 2 : 1); ++mode) {
@@ -453,10 +453,6 @@ int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
         {
             Phase ph(it, VX_PROF_APPLY);
             VX_CUDA(launch_apply_levels(it->dev, a, it->num_sms, s));
-        }
-        {
-            Phase ph(it, VX_PROF_REFCOUNT);
-            VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
         }
         {
             Phase ph(it, VX_PROF_RELEASE);

@@ -248,6 +248,20 @@ __device__ __forceinline__ uint32_t node_for_ticket(const DevInterner &I, unsign
     return node_for_ticket(I, t, I.ctr->free_count, I.ctr->next_index);
 }
 
+// Closes the epoch (one thread, after every allocation of the epoch): the free-list entries and
+// fresh indices its tickets took become allocated.
+__device__ __forceinline__ void epoch_finalize_body(const DevInterner &I) {
+    DevCounters *c = I.ctr;
+    const unsigned long long alloc = c->alloc_count, fc = c->free_count;
+    const unsigned long long used_free = alloc < fc ? alloc : fc;
+    c->free_count = fc - used_free;
+    unsigned long long ni = c->next_index + (alloc - used_free);
+    if (ni > I.capacity) ni = I.capacity;
+    c->created += used_free + (ni - c->next_index);
+    c->next_index = ni;
+    c->alloc_count = 0;
+}
+
 // Writes a new branch record (children, LOD value, fingerprint, live id); rc starts at 0.
 __device__ __forceinline__ uint64_t write_branch(const DevInterner &I, uint32_t idx, const uint64_t c[8],
                                                  uint32_t types, uint32_t mask, uint64_t h, uint32_t lod) {
@@ -391,33 +405,31 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
     unsigned long long *slot = (unsigned long long *)(I.leaf_table + v);
     uint64_t s = ld_volatile(I.leaf_table + v);
     if (s > LEAF_BUSY) return s;
-    if (s == 0) {
-        uint64_t prev = atomicCAS(slot, 0ull, LEAF_BUSY);
-        if (prev == 0) {
-            unsigned long long t = atomicAdd(&I.ctr->alloc_count, 1ull);
-            uint32_t idx = node_for_ticket(I, t);
-            if (idx == NO_NODE) {
-                set_error(I, ERR_OOM, 2);
-                atomicExch(slot, 0ull);
-                return INVALID_ID;
-            }
-            uint32_t gen = I.generation[idx];
-            uint64_t id = make_leaf_id(idx, gen);
-            set_node_value(I, idx, v);
-            I.hash[idx] = 0;
-            I.refcount[idx] = 0;
-            I.ids[idx] = id;
-            atom_exch_release(slot, id);
-            *created = true;
-            return id;
-        }
-        if (prev > LEAF_BUSY) return prev;
-    }
     for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin) {
+        if (s == 0) {  // free (or its creator ran out of memory and backed off): claim it
+            const uint64_t prev = atomicCAS(slot, 0ull, LEAF_BUSY);
+            if (prev == 0) {
+                const unsigned long long t = atomicAdd(&I.ctr->alloc_count, 1ull);
+                const uint32_t idx = node_for_ticket(I, t);
+                if (idx == NO_NODE) {
+                    set_error(I, ERR_OOM, 2);
+                    atomicExch(slot, 0ull);
+                    return INVALID_ID;
+                }
+                const uint64_t id = make_leaf_id(idx, I.generation[idx]);
+                set_node_value(I, idx, v);
+                I.hash[idx] = 0;
+                I.refcount[idx] = 0;
+                I.ids[idx] = id;
+                atom_exch_release(slot, id);
+                *created = true;
+                return id;
+            }
+            if (prev > LEAF_BUSY) return prev;
+        }
+        __nanosleep(64);  // being created by another thread
         s = ld_volatile(I.leaf_table + v);
         if (s > LEAF_BUSY) return s;
-        if (s == 0) return intern_leaf(I, v, created);  // creator ran out of memory and backed off
-        __nanosleep(64);
     }
     set_error(I, ERR_TIMEOUT, 3);
     return INVALID_ID;
