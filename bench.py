@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--check", action="store_true", help="large: compare with the CPU oracle after every step")
     p.add_argument("--edits-chunks", type=int, default=512,
                    help="edits: chunks per depth (512 is the benchmark; fewer for profiling)")
+    p.add_argument("--launch", type=int, choices=[0, 1], default=None,
+                   help="edits: apply as one cooperative launch (1) or one launch per phase (0) instead of autotuning")
     p.add_argument("--quick", action="store_true",
                    help="timed build steps and gets only (no per-chunk, e2e or CPU legs); for profiling")
     return p.parse_args()
@@ -415,7 +417,7 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
-    launches = (lib.kernel_launches() - launches0) / max(1, args.steps)
+    launches = lib.kernel_launches() - launches0  # this library's kernels in the timed region
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -546,7 +548,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(grids_np.nbytes + 4 * n), "d2h_bytes_per_step": int(n),
                 "same_dag": e2e_same},
         "clocks": clk,
-        "gpu_launches": launches,
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": launches / max(1, args.steps),
     }
     ok = pc_same and e2e_same and gets_ok
     if rank == 0 and not args.no_cpu:
@@ -576,11 +579,20 @@ def run_extras(args):
     import torch
 
     out = {}
+    prepared = None
+    try:  # the large tree's grid, and the oracle's minute-long build of it started in the background
+        import bench_large
+
+        prepared = bench_large.Prepared(check=True)
+    except Exception as e:
+        out["large_tree"] = {"error": "%s: %s" % (type(e).__name__, e), "trace": traceback.format_exc()[-600:]}
     for key, mod in (("uneven_edits", "bench_edits"), ("served_world", "bench_serve"), ("large_tree", "bench_large")):
+        if key in out:
+            continue
         t0 = time.time()
         try:
             m = __import__(mod)
-            out[key] = m.measure(args)
+            out[key] = m.measure(args, prepared=prepared) if key == "large_tree" else m.measure(args)
         except Exception as e:  # keep the headline line; the entry says what failed
             out[key] = {"error": "%s: %s" % (type(e).__name__, e), "trace": traceback.format_exc()[-600:]}
         out[key]["wall_s"] = time.time() - t0

@@ -156,8 +156,14 @@ def measure(args, full_line=False):
         e1.synchronize()
         return e0.elapsed_time(e1)
 
-    tune = {"skipped": True} if args.quick else autotune_apply(lib, h, rebuild, lambda: timed(apply_all),
-                                                               signature="edits%d" % per_depth)
+    launch = getattr(args, "launch", None)
+    if launch is not None:  # a fixed launch form instead of the autotuner's choice
+        call("tune_set_launch", int(launch))
+        tune = {"fixed_single_launch": int(launch)}
+    elif args.quick:
+        tune = {"skipped": True}
+    else:
+        tune = autotune_apply(lib, h, rebuild, lambda: timed(apply_all), signature="edits%d" % per_depth)
     prof_ms = (C.c_double * VX_PROF_N)()
     prof_n = (C.c_uint64 * VX_PROF_N)()
     for _ in range(args.warmup):

@@ -48,7 +48,55 @@ def compare(lib, h, tree, oracle):
     return rep
 
 
-def measure(args, full_line=False, check=None):
+class Prepared:
+    """The caves grid generated on the GPU and, when checking, the oracle's build of the same tree
+    running in a background thread (it takes about a minute of one core; the oracle's C calls release
+    the interpreter, so other work proceeds meanwhile)."""
+
+    def __init__(self, check):
+        import threading
+
+        import torch
+
+        import bench as B
+
+        self.dev = torch.device("cuda", 0)
+        self.stream = torch.cuda.Stream(device=self.dev)
+        t0 = time.time()
+        with torch.cuda.stream(self.stream):
+            self.grid = W.caves_torch(DEPTH, seed=99, device=self.dev)
+        self.stream.synchronize()
+        self.gen_s = time.time() - t0
+        self.check = check
+        self.oracle = self.error = None
+        self.oracle_build_s = None
+        self.done = threading.Event()
+        if not check:
+            self.done.set()
+            return
+        host = self.grid.cpu().numpy()
+
+        def work():
+            try:
+                ol = B.oracle_lib()
+                oh = C.c_void_p()
+                ol.call("interner_create", C.c_uint64(BUDGET), 8, PATCHES, 0, C.byref(oh))
+                ot = C.c_uint32()
+                ol.call("tree_create", oh, DEPTH, C.byref(ot), handle=oh)
+                otr = np.array([ot.value], np.uint32)
+                t1 = time.time()
+                ol.call("build_dense", oh, 1, C.c_void_p(otr.ctypes.data), C.c_void_p(host.ctypes.data), None, 0,
+                        handle=oh)
+                self.oracle_build_s = time.time() - t1
+                self.oracle = (ol, oh, ot.value)
+            except Exception as e:  # reported by measure()
+                self.error = e
+            self.done.set()
+
+        threading.Thread(target=work, daemon=True).start()
+
+
+def measure(args, full_line=False, check=None, prepared=None):
     import torch
 
     import bench as B
@@ -58,13 +106,9 @@ def measure(args, full_line=False, check=None):
         check = not getattr(args, "no_check", False)
     build_lib()
     lib = gpu_lib()
-    dev = torch.device("cuda", 0)
-    stream = torch.cuda.Stream(device=dev)
-    t0 = time.time()
-    with torch.cuda.stream(stream):
-        grid = W.caves_torch(DEPTH, seed=99, device=dev)
-    stream.synchronize()
-    gen_s = time.time() - t0
+    pre = prepared if prepared is not None else Prepared(check)
+    check = pre.check
+    dev, stream, grid, gen_s = pre.dev, pre.stream, pre.grid, pre.gen_s
     h = C.c_void_p()
     lib.call("interner_create", C.c_uint64(BUDGET), 8, PATCHES, 0, C.byref(h))
     call = lambda name, *a: lib.call(name, h, *a, handle=h)  # noqa: E731
@@ -113,18 +157,11 @@ def measure(args, full_line=False, check=None):
 
     oracle, checks = None, []
     if check:
-        ol = B.oracle_lib()
-        oh = C.c_void_p()
-        ol.call("interner_create", C.c_uint64(BUDGET), 8, PATCHES, 0, C.byref(oh))
-        ot = C.c_uint32()
-        ol.call("tree_create", oh, DEPTH, C.byref(ot), handle=oh)
-        g_host = grid.cpu().numpy()
-        otr = np.array([ot.value], np.uint32)
-        t1 = time.time()
-        ol.call("build_dense", oh, 1, C.c_void_p(otr.ctypes.data), C.c_void_p(g_host.ctypes.data), None, 0, handle=oh)
-        report["oracle_build_s"] = time.time() - t1
-        del g_host
-        oracle = (ol, oh, ot.value)
+        pre.done.wait()
+        if pre.error is not None:
+            raise pre.error
+        oracle = pre.oracle
+        report["oracle_build_s"] = pre.oracle_build_s
         checks.append(dict(after="build", **compare(lib, h, tree, oracle)))
 
     # 16M uniform-random gets, every result checked against the grid

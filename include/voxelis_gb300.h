@@ -218,6 +218,12 @@ int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *tree
  * autotuner in voxelis_gb300/tune.py. */
 int vx_tune_set(vx_interner *it, int apply_threads, int apply_blocks_per_sm);
 int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm);
+/* How a batched apply is launched (no counterpart in the reference; autotuned): 1 (the default) runs
+ * the whole apply, its level passes and the release of the replaced roots as one cooperative launch
+ * whose phases meet at grid barriers (blocks per SM capped by what can be resident); 0 launches one
+ * kernel per phase. Results are identical. */
+int vx_tune_set_launch(vx_interner *it, int single_launch);
+int vx_tune_get_launch(vx_interner *it, int *single_launch);
 
 /* ---- world helpers for serving (no counterpart in the reference) ---------------------------- */
 /* A grid of nx x ny x nz chunks of depth chunk_depth; the chunk holding world voxel (x, y, z) is

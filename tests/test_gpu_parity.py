@@ -185,6 +185,7 @@ def edit_batches(trees, interner, depth, density, seed, max_material):
     return bs
 
 
+@pytest.mark.parametrize("launch", [1, 0], ids=["single_launch", "per_phase"])
 @pytest.mark.parametrize("bits,depths,patches", [
     (8, [5, 5, 5, 5], VX_PATCH_P1),
     (16, [5, 6, 5, 6], VX_PATCH_P1),
@@ -192,8 +193,11 @@ def edit_batches(trees, interner, depth, density, seed, max_material):
     (8, [5, 5, 6], VX_PATCH_P1 | VX_PATCH_P4),
     (16, [7, 5], VX_PATCH_P1 | VX_PATCH_P2 | VX_PATCH_P3 | VX_PATCH_P4),
 ])
-def test_batched_edits_match_sequential_oracle(oracle_lib, gpu_lib, bits, depths, patches):
+def test_batched_edits_match_sequential_oracle(oracle_lib, gpu_lib, bits, depths, patches, launch):
+    """Batched apply_batch of several trees (both launch forms of the device apply) equals the
+    oracle's apply_batch one tree after the other."""
     io, ig = pair(oracle_lib, gpu_lib, 256 << 20, bits, patches)
+    gpu_lib.call("tune_set_launch", ig.handle, launch, handle=ig.handle)
     to = [VoxTree(d) for d in depths]
     tg = [VoxTree(d) for d in depths]
     for k, d in enumerate(depths):
@@ -275,8 +279,9 @@ def test_rebuild_after_release_reuses_slots(gpu_lib):
     assert s2["next_index"] == s1["next_index"]
 
 
+@pytest.mark.parametrize("launch", [1, 0], ids=["single_launch", "per_phase"])
 @pytest.mark.parametrize("patches", [VX_PATCH_P1 | VX_PATCH_P2, VX_PATCH_P1 | VX_PATCH_P2 | VX_PATCH_P3 | VX_PATCH_P4])
-def test_device_group_records_match_oracle(oracle_lib, gpu_lib, patches):
+def test_device_group_records_match_oracle(oracle_lib, gpu_lib, patches, launch):
     """vx_apply_groups_async (compacted groups already in HBM) equals sequential apply_batch."""
     import ctypes as C
 
@@ -284,6 +289,7 @@ def test_device_group_records_match_oracle(oracle_lib, gpu_lib, patches):
 
     depths = [7, 6, 6, 5, 5, 5]  # deepest first, as the entry point requires
     io, ig = pair(oracle_lib, gpu_lib, 256 << 20, 16, patches)
+    gpu_lib.call("tune_set_launch", ig.handle, launch, handle=ig.handle)
     to = [VoxTree(d) for d in depths]
     tg = [VoxTree(d) for d in depths]
     for k, d in enumerate(depths):

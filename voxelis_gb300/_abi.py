@@ -152,6 +152,8 @@ GPU_SIGNATURES = {
     "world_get_async": [_P, _P, _U64, _P, _P, _P],
     "copy_to_device_async": [_P, _U32, _P, _P, _P],
     "tune_get": [_P, _PI, _PI],
+    "tune_set_launch": [_P, _I],
+    "tune_get_launch": [_P, _PI],
     "trees_to_dense": [_P, _U32, _P, _P, _I],
     "trees_to_dense_async": [_P, _U32, _P, _I, _P],
     "occupancy_masks_async": [_P, _U32, _U32, _P, _P, _P, _I, _U32, _P, _P, _P, _P, _P, _P],

@@ -133,15 +133,13 @@ __device__ __forceinline__ void leaf_refs_flush(const DevInterner &I, const Leaf
     }
 }
 
-__global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_items) return;
+__device__ __forceinline__ void prep_item(const DevInterner &I, const ApplyArgs &a, int mode, uint32_t i) {
     const uint32_t t = a.it_tree[i];
     const uint64_t old = I.roots[t];
     const uint8_t f = a.it_flags[i];
     uint64_t init = old;
     a.it_old[i] = old;
-    if (a.mode == 1) {  // the clear pass starts from the root the set phase left
+    if (mode == 1) {  // the clear pass starts from the root the set phase left
         a.it_init[i] = old;
         a.it_new[i] = INVALID_ID;
         return;
@@ -157,10 +155,16 @@ __global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
     a.it_new[i] = (f & 2) ? INVALID_ID : init;
 }
 
-__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInterner I, ApplyArgs a) {
-    const LeafRefs L = leaf_refs_init(I);
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.n_records; base += stride) {
+__global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.n_items) prep_item(I, a, a.mode, i);
+}
+
+// Phase 1 for records cta_base + threadIdx.x, + stride, ... (a CTA-uniform loop: whole warps take
+// part in the warp-cooperative interning).
+__device__ __forceinline__ void bottom_range(const DevInterner &I, const ApplyArgs &a, int mode, const LeafRefs &L,
+                                             uint64_t cta_base, uint64_t stride) {
+    for (uint64_t base = cta_base; base < a.n_records; base += stride) {
         const uint64_t r = base + threadIdx.x;
         bool active = r < a.n_records;
         uint32_t i = 0, set = 0, changed = 0;
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
         if (active) {
             i = a.rec_item[r];
             d = a.it_depth[i];
-            set = a.mode ? a.rec_clear[r] : a.rec_set[r];
+            set = mode ? a.rec_clear[r] : a.rec_set[r];
             if (set == 0 || a.it_panic[i]) active = false;
         }
         bool uniform = false;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
 #pragma unroll
             for (int k = 1; k < 8; ++k) uniform = uniform && v[k] == v[0];
             if (cur != EMPTY_ID && id_is_leaf(cur)) {
-                if ((I.flags & 1u) || a.mode == 1) {  // P1 (removals always split a leaf)
+                if ((I.flags & 1u) || mode == 1) {  // P1 (removals always split a leaf)
                     anc = cur;
                     cur = EMPTY_ID;
                 } else if (!uniform) {  // the reference panics in BlockId::types()
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
                 }
             }
         }
-        if (active && a.mode == 1) {  // remove_at_depth_branch / _leaf at depth d-1
+        if (active && mode == 1) {  // remove_at_depth_branch / _leaf at depth d-1
             uint32_t modified = 0;
             if (cur != EMPTY_ID) {
                 const uint64_t *src = I.children + 8ull * id_index(cur);
@@ -269,18 +273,27 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
                 }
                 types = mask = 0xFF;
             }
+            // the set voxels whose value differs from the existing leaf become new leaves: their
+            // leaf-table slots are read together (one round trip for all of them); only a leaf not
+            // created yet takes the claiming path
             uint32_t modified = 0;
 #pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (((set >> k) & 1) && !(c[k] != EMPTY_ID && cv[k] == v[k])) modified |= 1u << k;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if ((modified >> k) & 1) c[k] = ld_cg(I.leaf_table + v[k]);
+#pragma unroll
             for (int k = 0; k < 8; ++k) {
-                if (!((set >> k) & 1)) continue;
-                if (c[k] != EMPTY_ID && cv[k] == v[k]) continue;
-                bool created;
-                c[k] = intern_leaf(I, v[k], &created);
+                if (!((modified >> k) & 1)) continue;
+                if (c[k] <= LEAF_BUSY) {
+                    bool created;
+                    c[k] = intern_leaf(I, v[k], &created);
+                }
                 cv[k] = v[k];
-                types |= 1u << k;
-                mask |= 1u << k;
-                modified |= 1u << k;
             }
+            types |= modified;
+            mask |= modified;
             if (anc != EMPTY_ID && cur == EMPTY_ID) {  // Q5
                 const int ds = __popc(set), dm = __popc(modified);
                 add_ref_delta(I, anc, modified ? dm - ds : 8 - ds);
@@ -301,6 +314,11 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
             a.rec_val[r] = lod;
         }
     }
+}
+
+__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInterner I, ApplyArgs a) {
+    const LeafRefs L = leaf_refs_init(I);
+    bottom_range(I, a, a.mode, L, (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
     leaf_refs_flush(I, L);
 }
 
@@ -502,10 +520,8 @@ __global__ void scan_total_kernel(const uint32_t *in, uint32_t *out, uint32_t n)
     out[n] = n ? out[n - 1] + in[n - 1] : 0u;
 }
 
-__global__ void scatter_bottom_kernel(DevInterner I, ApplyArgs a) {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) I.ctr->scratch[SC_ENTRIES] = a.pos[a.n_records];
-    if (r >= a.n_records || !a.flags[r]) return;
+__device__ __forceinline__ void scatter_record(const ApplyArgs &a, uint32_t r) {
+    if (!a.flags[r]) return;
     const uint32_t e = a.pos[r];
     a.e_item[0][e] = a.rec_item[r];
     a.e_path[0][e] = a.rec_group[r] << 3;
@@ -513,34 +529,47 @@ __global__ void scatter_bottom_kernel(DevInterner I, ApplyArgs a) {
     a.e_val[0][e] = a.rec_val[r];
 }
 
+__global__ void scatter_bottom_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) I.ctr->scratch[SC_ENTRIES] = a.pos[a.n_records];
+    if (r < a.n_records) scatter_record(a, r);
+}
+
 __device__ __forceinline__ uint32_t parent_key_path(uint32_t path, int d, int t) {
     return t == 1 ? 0u : (path & path_mask(d, t - 2));
 }
 
+// Run heads of a level step: entry j starts a sibling run unless entry j-1 has the same parent.
+__device__ __forceinline__ void head_flag(const ApplyArgs &a, int step, int buf, uint32_t j) {
+    const uint32_t i = a.e_item[buf][j];
+    const int d = a.it_depth[i];
+    const int t = d - step;
+    uint32_t head = 1;
+    if (j > 0) {
+        const uint32_t ip = a.e_item[buf][j - 1];
+        if (ip == i && parent_key_path(a.e_path[buf][j - 1], d, t) == parent_key_path(a.e_path[buf][j], d, t))
+            head = 0;
+    }
+    a.flags[j] = head;
+}
+
 __global__ void heads_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
-        const uint32_t i = a.e_item[buf][j];
-        const int d = a.it_depth[i];
-        const int t = d - step;
-        uint32_t head = 1;
-        if (j > 0) {
-            const uint32_t ip = a.e_item[buf][j - 1];
-            if (ip == i && parent_key_path(a.e_path[buf][j - 1], d, t) == parent_key_path(a.e_path[buf][j], d, t))
-                head = 0;
-        }
-        a.flags[j] = head;
-    }
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
+        head_flag(a, step, buf, j);
+}
+
+// After the scan of the head flags: the number of parents and where each one's run starts.
+__device__ __forceinline__ void starts_head(const DevInterner &I, const ApplyArgs &a, uint32_t count) {
+    const uint32_t np = a.pos[count];
+    a.p_start[np] = count;
+    I.ctr->scratch[SC_PARENTS] = np;
+    I.ctr->scratch[SC_ROOTS] = 0;
 }
 
 __global__ void starts_kernel(DevInterner I, ApplyArgs a) {
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const uint32_t np = a.pos[count];
-        a.p_start[np] = count;
-        I.ctr->scratch[SC_PARENTS] = np;
-        I.ctr->scratch[SC_ROOTS] = 0;
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) starts_head(I, a, count);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
         if (a.flags[j]) a.p_start[a.pos[j]] = j;
 }
@@ -550,12 +579,12 @@ __device__ __forceinline__ void next_count(const DevInterner &I) {
     I.ctr->scratch[SC_ENTRIES] = I.ctr->scratch[SC_PARENTS] - I.ctr->scratch[SC_ROOTS];
 }
 
-__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
-    const LeafRefs L = leaf_refs_init(I);
-    const uint32_t n_par = (uint32_t)I.ctr->scratch[SC_PARENTS];
+// Phase 2 for one level: parents cta_base + threadIdx.x, + stride, ... of the n_par run heads
+// (a CTA-uniform loop, as in bottom_range).
+__device__ __forceinline__ void parents_range(const DevInterner &I, const ApplyArgs &a, int mode, const LeafRefs &L,
+                                              int step, int buf, uint32_t n_par, uint64_t cta_base, uint64_t stride) {
     const int nb = buf ^ 1;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_par; base += stride) {
+    for (uint64_t base = cta_base; base < n_par; base += stride) {
         const uint64_t p = base + threadIdx.x;
         const bool in = p < n_par;
         uint64_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -603,7 +632,7 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevIn
                 types |= (id_is_leaf(id) ? 1u : 0u) << ti;
                 mask |= 1u << ti;
             }
-            if (a.mode == 1) {  // remove_at_depth_branch / _leaf one level up (voxtree.rs:559-706)
+            if (mode == 1) {  // remove_at_depth_branch / _leaf one level up (voxtree.rs:559-706)
                 const uint32_t ch = mask;
                 uint64_t nc[8];
                 uint32_t nv[8];
@@ -710,14 +739,20 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevIn
             a.e_val[nb][p] = out_val;
         }
     }
+}
+
+__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    const LeafRefs L = leaf_refs_init(I);
+    parents_range(I, a, a.mode, L, step, buf, (uint32_t)I.ctr->scratch[SC_PARENTS],
+                  (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
     leaf_refs_flush(I, L);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) next_count(I);  // entries of the next step
 }
 
 
 
-__device__ __forceinline__ void finish_item(const DevInterner &I, const ApplyArgs &a, uint32_t i) {
-    if (a.mode == 1) {
+__device__ __forceinline__ void finish_item(const DevInterner &I, const ApplyArgs &a, int mode, uint32_t i) {
+    if (mode == 1) {
         const uint64_t nw = a.it_new[i], old = a.it_old[i];
         if (nw == INVALID_ID) return;
         if (nw != EMPTY_ID) atomicAdd(I.refcount + id_index(nw), 1u);
@@ -751,15 +786,13 @@ __device__ __forceinline__ void finish_item(const DevInterner &I, const ApplyArg
 // pass has been created and has added its children's references by now.
 __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < a.n_items) finish_item(I, a, i);
+    if (i < a.n_items) finish_item(I, a, a.mode, i);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) epoch_finalize_body(I);
 }
 
 __global__ void zero_counter_kernel(DevInterner I, int slot) { I.ctr->scratch[slot] = 0; }
 
-__global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_items) return;
+__device__ __forceinline__ void item_depth(const DevInterner &I, const ApplyArgs &a, uint32_t i) {
     const uint32_t t = a.it_tree[i];
     const int d = t < I.tree_cap ? I.depths[t] : TREE_UNUSED;
     int prev = 0xFF;
@@ -773,6 +806,139 @@ __global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
         return;
     }
     const_cast<uint8_t *>(a.it_depth)[i] = (uint8_t)d;
+}
+
+__global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.n_items) item_depth(I, a, i);
+}
+
+// ---- the whole apply in one cooperative launch -------------------------------------------------------
+// Exclusive scan of one value per thread across the CTA (blockDim.x a multiple of 32, at most 1024);
+// *total receives the CTA's sum. Every thread of the CTA calls it.
+__device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t x, uint32_t *total) {
+    __shared__ uint32_t wsum[32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (unsigned)o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? wsum[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (unsigned)o) w += y;
+        }
+        if (lane < nw) wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t excl = incl - x + (warp ? wsum[warp - 1] : 0u);
+    *total = wsum[nw - 1];
+    __syncthreads();  // wsum is reused by the next call
+    return excl;
+}
+
+// Exclusive scan of in[0..n) into out (out[n] = the total) by the whole cooperative grid: each CTA
+// sums a contiguous range, the sums meet at a grid barrier, then each CTA scans its range from the
+// sum of the ranges before it. Ends with a grid barrier (out is read across CTAs afterwards).
+__device__ __forceinline__ bool grid_exclusive_scan(const DevInterner &I, const uint32_t *in, uint32_t *out,
+                                                    uint32_t n, uint32_t *partials) {
+    const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+    const uint32_t lo = min(n, blockIdx.x * per), hi = min(n, lo + per);
+    uint32_t s = 0, tot;
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) s += in[k];
+    cta_exclusive_scan(s, &tot);
+    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+    if (!grid_sync(I)) return false;
+    uint32_t before = 0;
+    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) before += partials[b];
+    cta_exclusive_scan(before, &tot);
+    uint32_t carry = tot;
+    for (uint32_t base = lo; base < hi; base += blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        const uint32_t x = k < hi ? in[k] : 0u;
+        const uint32_t e = cta_exclusive_scan(x, &tot);
+        if (k < hi) out[k] = carry + e;
+        carry += tot;
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = carry;
+    return grid_sync(I);
+}
+
+// The set phase (mode 0) and, when `clear_pass`, the clear pass (mode 1) with their releases: the
+// launch sequence of launch_apply_bottom / launch_apply_levels / launch_release in one kernel whose
+// phases are separated by grid barriers. Counts stay in device memory and are read by every CTA
+// after the barrier that follows their last write.
+__global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) apply_single_kernel(const DevInterner I, const ApplyArgs a,
+                                                                                   int check_depths, int clear_pass,
+                                                                                   uint32_t *frontier_a,
+                                                                                   uint32_t *frontier_b, int rounds) {
+    const uint64_t cta_base = (uint64_t)blockIdx.x * blockDim.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t gt = cta_base + threadIdx.x;
+    const bool t0 = gt == 0;
+    DevCounters *ctr = I.ctr;
+    if (check_depths) {
+        for (uint64_t i = gt; i < a.n_items; i += stride) item_depth(I, a, (uint32_t)i);
+        if (!grid_sync(I)) return;
+    }
+    for (int mode = 0; mode <= clear_pass; ++mode) {
+        const LeafRefs L = leaf_refs_init(I);
+        for (uint64_t i = gt; i < a.n_items; i += stride) prep_item(I, a, mode, (uint32_t)i);
+        if (!grid_sync(I)) return;
+        // Phase 1, then the changed groups become the first level's entries
+        bottom_range(I, a, mode, L, cta_base, stride);
+        if (!grid_sync(I)) return;
+        if (!grid_exclusive_scan(I, a.flags, a.pos, a.n_records, a.scan_tmp)) return;
+        for (uint64_t r = gt; r < a.n_records; r += stride) scatter_record(a, (uint32_t)r);
+        uint32_t count = a.pos[a.n_records];
+        if (!grid_sync(I)) return;
+        // Phase 2, one level step at a time
+        int buf = 0;
+        for (int step = 1; step <= a.max_depth - 1; ++step) {
+            for (uint64_t j = gt; j < count; j += stride) head_flag(a, step, buf, (uint32_t)j);
+            if (!grid_sync(I)) return;
+            if (!grid_exclusive_scan(I, a.flags, a.pos, count, a.scan_tmp)) return;
+            const uint32_t np = a.pos[count];
+            if (t0) {
+                a.p_start[np] = count;
+                ctr->scratch[SC_ROOTS] = 0;
+            }
+            for (uint64_t j = gt; j < count; j += stride)
+                if (a.flags[j]) a.p_start[a.pos[j]] = (uint32_t)j;
+            if (!grid_sync(I)) return;
+            parents_range(I, a, mode, L, step, buf, np, cta_base, stride);
+            if (!grid_sync(I)) return;
+            count = np - (uint32_t)ctr->scratch[SC_ROOTS];  // parents that are not tree roots
+            buf ^= 1;
+        }
+        // roots, the epoch, the release of the replaced roots
+        if (t0) ctr->scratch[SC_RELEASE] = 0;
+        if (!grid_sync(I)) return;
+        for (uint64_t i = gt; i < a.n_items; i += stride) finish_item(I, a, mode, (uint32_t)i);
+        leaf_refs_flush(I, L);
+        if (t0) {
+            ctr->rel_count[0] = 0;
+            ctr->rel_count[1] = 0;
+        }
+        if (!grid_sync(I)) return;
+        if (t0) epoch_finalize_body(I);
+        release_roots_range(I, a.release_list, frontier_a, &ctr->rel_count[0], cta_base, stride);
+        if (!grid_sync(I)) return;
+        // round r reads set r % 3 and writes set (r + 1) % 3; set (r + 2) % 3 was read by round r - 1
+        // and is written by round r + 1, so it is cleared now
+        uint32_t *fr[2] = {frontier_a, frontier_b};
+        for (int r = 0; r < rounds; ++r) {
+            if (t0) ctr->rel_count[(r + 2) % 3] = 0;
+            release_round_range(I, fr[r & 1], fr[(r + 1) & 1], &ctr->rel_count[r % 3], &ctr->rel_count[(r + 1) % 3],
+                                cta_base, stride);
+            if (!grid_sync(I)) return;
+        }
+    }
 }
 
 }  // namespace
@@ -886,6 +1052,34 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
     count_launches(1);
     finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);  // its last CTA closes the epoch
     return cudaGetLastError();
+}
+
+size_t apply_single_scan_words(int num_sms) { return (size_t)num_sms * 32 + 64; }
+
+// The whole apply sequence in one cooperative launch: as many CTAs as can be resident at once (the
+// grid barrier needs every CTA running).
+cudaError_t launch_apply_single(const DevInterner &I, const ApplyArgs &a, bool check_depths, bool clear_pass,
+                                uint32_t *frontier_a, uint32_t *frontier_b, int rounds, int num_sms, cudaStream_t s) {
+    const int bt = a.threads > 0 ? a.threads : kThreads;
+    const size_t smem = leaf_refs_smem(I);
+    static int per_sm_cache[2][17] = {};  // [vbits == 16][threads / 32]
+    int &per_sm = per_sm_cache[I.vbits == 16][bt / 32];
+    if (per_sm == 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_single_kernel, bt, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    }
+    int want = a.blocks_per_sm > 0 ? a.blocks_per_sm : per_sm;
+    if (want > per_sm) want = per_sm;
+    if ((size_t)num_sms * want > apply_single_scan_words(num_sms) - 64) want = 32;  // partials of the grid scan
+    const unsigned grid = (unsigned)(num_sms * want);
+    DevInterner Ic = I;
+    ApplyArgs ac = a;
+    int cd = check_depths ? 1 : 0, cp = clear_pass ? 1 : 0;
+    void *args[] = {&Ic, &ac, &cd, &cp, &frontier_a, &frontier_b, &rounds};
+    count_launches(1);
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(apply_single_kernel), dim3(grid), dim3(bt), args,
+                                       smem, s);
 }
 
 cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {

@@ -171,6 +171,7 @@ struct vx_interner {
     int num_sms = 148;
     int apply_threads = 256;       // launch shape of the batched-apply kernels (autotuned)
     int apply_blocks_per_sm = 8;
+    int apply_single = 1;          // 1: the whole apply as one cooperative launch; 0: a launch per phase
     // tree table
     uint32_t tree_cap = 0;
     std::vector<uint8_t> tree_depth, tree_used, tree_maybe_nonempty;
@@ -387,6 +388,12 @@ struct Item {
     uint32_t caller_index;
 };
 
+// Words of scan scratch an apply over Rp = R + 1 flags needs (block sums of the per-phase scans, or
+// the per-CTA partial sums of the single-launch path).
+size_t scan_words(vx_interner *it, size_t Rp) {
+    return std::max(scan_tmp_words((uint32_t)Rp) * 4, apply_single_scan_words(it->num_sms));
+}
+
 // Device scratch of one batched apply over n items and R touched groups. With `own_inputs` the
 // item and record input arrays are carved from the workspace too (host-staging path).
 int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyArgs &a) {
@@ -394,7 +401,7 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     const size_t in_items = own_inputs ? 1 : 0, in_recs = own_inputs ? 1 : 0;
     const size_t need = Carve::need({n * 4 * in_items, n, n * in_items, n * 4 * in_items, n * 8, n * 8, n * 8, n,
                                      n, R * 4 * in_recs, R * 4 * in_recs, R * in_recs, R * in_recs, R * 16 * in_recs,
-                                     Rp * 4, Rp * 4, scan_tmp_words((uint32_t)Rp) * 4 * 4, R * 4, R * 4, R * 4,
+                                     Rp * 4, Rp * 4, scan_words(it, Rp) * 4, R * 4, R * 4, R * 4,
                                      R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8});
     VX_CUDA(it->ws.reserve(need));
     Carve c(it->ws.p);
@@ -423,7 +430,7 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     }
     a.flags = c.take<uint32_t>(Rp);
     a.pos = c.take<uint32_t>(Rp);
-    a.scan_tmp = c.take<uint32_t>(scan_tmp_words((uint32_t)Rp) * 4);
+    a.scan_tmp = c.take<uint32_t>(scan_words(it, Rp));
     a.scan_status = it->scan_status;
     a.e_item[0] = c.take<uint32_t>(R);
     a.e_item[1] = c.take<uint32_t>(R);
@@ -442,8 +449,18 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
 
 // The set phase (its kernels count references as they create nodes and close the allocation epoch)
 // and its release, then (P4) the clear pass with its own epoch and release. No host synchronisation.
-int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
+int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass, bool check_depths = false) {
     cudaStream_t s = it->stream;
+    // the roots that die are the first dying set, retired by the first release pass; a root heads a
+    // subtree of height at most max_depth, whose leaves are retired by pass max_depth + 1
+    const int rounds = a.max_depth > 0 && a.max_depth < 10 ? a.max_depth + 1 : 11;
+    if (it->apply_single) {
+        Phase ph(it, VX_PROF_APPLY);
+        VX_CUDA(launch_apply_single(it->dev, a, check_depths, clear_pass, it->frontier, it->frontier + it->capacity,
+                                    rounds, it->num_sms, s));
+        return VX_OK;
+    }
+    if (check_depths) VX_CUDA(launch_item_depths(it->dev, a, s));
     for (int mode = 0; mode < (clear_pass ? 2 : 1); ++mode) {
         a.mode = mode;
         {
@@ -456,10 +473,8 @@ int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass) {
         }
         {
             Phase ph(it, VX_PROF_RELEASE);
-            // the roots that die are the first dying set, retired by the first release pass; a root heads
-            // a subtree of height at most max_depth, whose leaves are retired by pass max_depth + 1
             VX_CUDA(launch_release(it->dev, a.release_list, it->frontier, it->frontier + it->capacity, it->capacity,
-                                   a.max_depth > 0 && a.max_depth < 10 ? a.max_depth + 1 : 11, it->num_sms, s));
+                                   rounds, it->num_sms, s));
         }
     }
     return VX_OK;
@@ -1180,8 +1195,7 @@ int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *tree
     a.rec_clear = rec_clear_dev;
     a.rec_vals = rec_values_dev;
     a.max_depth = max_depth;
-    VX_CUDA(launch_item_depths(it->dev, a, it->stream));
-    st = apply_sequence(it, a, (it->flags & VX_PATCH_P4) != 0);
+    st = apply_sequence(it, a, (it->flags & VX_PATCH_P4) != 0, true);
     if (st != VX_OK) return st;
     if (changed_dev) VX_CUDA(cudaMemcpyAsync(changed_dev, a.it_changed, n_items, cudaMemcpyDeviceToDevice, it->stream));
     return VX_OK;
@@ -1200,6 +1214,18 @@ int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm) {
     if (!it || !apply_threads || !apply_blocks_per_sm) return VX_E_INVALID_ARG;
     *apply_threads = it->apply_threads;
     *apply_blocks_per_sm = it->apply_blocks_per_sm;
+    return VX_OK;
+}
+
+int vx_tune_set_launch(vx_interner *it, int single_launch) {
+    if (!it || (single_launch != 0 && single_launch != 1)) return VX_E_INVALID_ARG;
+    it->apply_single = single_launch;
+    return VX_OK;
+}
+
+int vx_tune_get_launch(vx_interner *it, int *single_launch) {
+    if (!it || !single_launch) return VX_E_INVALID_ARG;
+    *single_launch = it->apply_single;
     return VX_OK;
 }
 

@@ -60,6 +60,9 @@ struct DevCounters {
     unsigned int error_info;         // first error detail
     unsigned long long scratch[10];  // per-launch counters used by the kernels
     unsigned long long created;      // nodes allocated since the interner was created or reset
+    unsigned long long bar_count;    // grid barrier of single-launch kernels: CTAs arrived
+    unsigned long long bar_gen;      //   and the barrier's generation
+    unsigned long long rel_count[3]; // dying-set sizes of single-launch release rounds (rotating)
 };
 
 struct DevInterner {
@@ -469,6 +472,137 @@ __device__ __forceinline__ void recycle_node(const DevInterner &I, uint32_t idx,
     if (g >= MAX_GENERATION) g = 0;
     I.generation[idx] = (uint16_t)g;
     I.free_list[free_pos] = idx;
+}
+
+// ---- grid barrier of single-launch (cooperative) kernels -------------------------------------------
+// Every CTA of the grid must call it (all CTAs are resident: cooperative launch). Thread 0 arrives
+// with a fence and waits, bounded, for the generation to move; the last to arrive resets the count
+// and moves the generation with release semantics. Writes before the barrier are visible to every
+// thread of the grid after it. Returns false if the wait gave up (ERR_TIMEOUT recorded).
+__device__ __forceinline__ bool grid_sync(const DevInterner &I) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned long long gen = ld_acquire(reinterpret_cast<const uint64_t *>(&I.ctr->bar_gen));
+        __threadfence();
+        if (atomicAdd(&I.ctr->bar_count, 1ull) == gridDim.x - 1) {
+            I.ctr->bar_count = 0;
+            st_release_u64(&I.ctr->bar_gen, gen + 1);
+        } else {
+            uint32_t spin = 0;
+            while (ld_acquire(reinterpret_cast<const uint64_t *>(&I.ctr->bar_gen)) == gen) {
+                // a CTA that gave up at an earlier barrier never arrives: stop waiting at once
+                const bool gave_up = (spin & 1023u) == 1023u &&
+                                     (*reinterpret_cast<volatile unsigned int *>(&I.ctr->error) & ERR_TIMEOUT);
+                if (++spin >= SPIN_LIMIT || gave_up) {
+                    set_error(I, ERR_TIMEOUT, 49);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// ---- release (dec_ref_recursive, interner/mod.rs:419-534, breadth first) ------------------------
+// Counter slots of the release rounds in DevCounters::scratch (the batched-apply launcher's table
+// lists every slot).
+constexpr int kScRelease = 3, kScRelIn = 4, kScRelOut = 5;
+
+// The dying set just produced becomes the input of the next round.
+__device__ __forceinline__ void release_advance(const DevInterner &I) {
+    I.ctr->scratch[kScRelIn] = I.ctr->scratch[kScRelOut];
+    I.ctr->scratch[kScRelOut] = 0;
+}
+
+__device__ __forceinline__ void push_dying(uint32_t *list, unsigned long long *count, bool push, uint32_t idx) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
+    if (!m) return;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long base = 0;
+    const int leader = __ffs(m) - 1;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (push) list[base + __popc(m & ((1u << lane) - 1u))] = idx;
+}
+
+// Decrements each listed root (count at scratch[kScRelease]); roots whose count reaches zero become
+// the first dying set. Entry cta_base + threadIdx.x, then + stride, ...: the loop is uniform across
+// the CTA, so the warp votes inside see whole warps.
+__device__ __forceinline__ void release_roots_range(const DevInterner &I, const uint64_t *list, uint32_t *out,
+                                                    unsigned long long *n_out, uint64_t cta_base, uint64_t stride) {
+    const uint64_t n = I.ctr->scratch[kScRelease];
+    for (uint64_t base = cta_base; base < n; base += stride) {
+        const uint64_t j = base + threadIdx.x;
+        bool dies = false;
+        uint32_t idx = 0;
+        if (j < n) {
+            const uint64_t id = list[j];
+            if (id != EMPTY_ID) {
+                idx = id_index(id);
+                const unsigned old = atomicSub(I.refcount + idx, 1u);
+                if (old == 0) {
+                    atomicAdd(I.refcount + idx, 1u);
+                    set_error(I, ERR_REF_UB, 60);
+                } else {
+                    dies = old == 1;
+                }
+            }
+        }
+        push_dying(out, n_out, dies, idx);
+    }
+}
+
+// Retires the *n_in dying nodes of `in`: their children lose one reference each (children reaching
+// zero are the next dying set, appended to `out` and counted in *n_out) and the nodes are recycled.
+__device__ __forceinline__ void release_round_range(const DevInterner &I, const uint32_t *in, uint32_t *out,
+                                                    const unsigned long long *n_in, unsigned long long *n_out,
+                                                    uint64_t cta_base, uint64_t stride) {
+    const uint64_t n = *n_in;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t base = cta_base; base < n; base += stride) {
+        const uint64_t j = base + threadIdx.x;
+        const bool in_range = j < n;
+        const uint32_t idx = in_range ? in[j] : 0u;
+        const uint64_t id = in_range ? I.ids[idx] : 0ull;
+        const bool branch = in_range && id != 0 && id_is_branch(id);
+        for (int k = 0; k < 8; ++k) {
+            bool dies = false;
+            uint32_t cidx = 0;
+            if (branch) {
+                const uint64_t c = I.children[8ull * idx + k];
+                if (c != EMPTY_ID) {
+                    cidx = id_index(c);
+                    const unsigned old = atomicSub(I.refcount + cidx, 1u);
+                    if (old == 0) {
+                        atomicAdd(I.refcount + cidx, 1u);
+                        set_error(I, ERR_REF_UB, 61);
+                    } else {
+                        dies = old == 1;
+                    }
+                }
+            }
+            push_dying(out, n_out, dies, cidx);
+        }
+        const bool rec = in_range && id != 0;
+        if (in_range && id == 0) set_error(I, ERR_INTERNAL, 62);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, rec);
+        unsigned long long fbase = 0;
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            if ((int)lane == leader) fbase = atomicAdd(&I.ctr->free_count, (unsigned long long)__popc(m));
+            fbase = __shfl_sync(0xFFFFFFFFu, fbase, leader);
+        }
+        const unsigned tomb = __ballot_sync(0xFFFFFFFFu, rec && branch);
+        if (lane == 0 && tomb) atomicAdd(&I.ctr->tombstones, (unsigned long long)__popc(tomb));
+        if (rec) recycle_node(I, idx, fbase + __popc(m & ((1u << lane) - 1u)));
+    }
 }
 
 }  // namespace vxg

@@ -87,6 +87,12 @@ struct ApplyArgs {
     uint64_t *release_list;      // [n_items]
 };
 cudaError_t launch_apply(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
+// The same sequence (with the item depth check when check_depths, the clear pass when clear_pass and
+// the release of the replaced roots in `rounds` rounds) as one cooperative launch: every CTA
+// resident, phases separated by grid barriers. a.scan_tmp must hold apply_single_scan_words words.
+cudaError_t launch_apply_single(const DevInterner &I, const ApplyArgs &a, bool check_depths, bool clear_pass,
+                                uint32_t *frontier_a, uint32_t *frontier_b, int rounds, int num_sms, cudaStream_t s);
+size_t apply_single_scan_words(int num_sms);
 // The same sequence in two parts: items + bottom groups, then the level passes and the commit.
 cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s);
@@ -97,6 +103,8 @@ enum : int {
     SC_ENTRIES = 0, SC_PARENTS = 1, SC_ROOTS = 2, SC_RELEASE = 3, SC_REL_IN = 4, SC_REL_OUT = 5, SC_REF_DONE = 6,
     SC_DONE = 7, SC_SCAN_TICKET = 8, SC_SCAN_DONE = 9
 };
+static_assert(SC_RELEASE == kScRelease && SC_REL_IN == kScRelIn && SC_REL_OUT == kScRelOut,
+              "release slots shared with vx_device.cuh");
 // Tiles of a one-pass device scan with a status word each (ApplyArgs::scan_status, zero between
 // scans: the scan's last CTA clears them); larger scans take the three-launch path.
 constexpr uint32_t kScanStatusTiles = 64;

@@ -65,94 +65,17 @@ __global__ void __launch_bounds__(kThreads) get_kernel(DevInterner I, uint64_t n
     if (bad) set_error(I, ERR_INVALID, 51);
 }
 
-// ---- release -----------------------------------------------------------------------------------
-// The dying set just produced becomes the input of the next round.
-__device__ __forceinline__ void release_advance(const DevInterner &I) {
-    I.ctr->scratch[SC_REL_IN] = I.ctr->scratch[SC_REL_OUT];
-    I.ctr->scratch[SC_REL_OUT] = 0;
-}
-
-__device__ __forceinline__ void push_dying(uint32_t *list, unsigned long long *count, bool push, uint32_t idx) {
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
-    if (!m) return;
-    const unsigned lane = threadIdx.x & 31u;
-    unsigned long long base = 0;
-    const int leader = __ffs(m) - 1;
-    if ((int)lane == leader) base = atomicAdd(count, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (push) list[base + __popc(m & ((1u << lane) - 1u))] = idx;
-}
-
-// Decrements each listed root; roots whose count reaches zero become the first dying set.
+// ---- release (bodies in vx_device.cuh, shared with the single-launch apply) ------------------------
 __global__ void __launch_bounds__(kThreads) release_roots_kernel(DevInterner I, const uint64_t *list,
                                                                 uint32_t *out) {
-    const uint64_t n = I.ctr->scratch[SC_RELEASE];
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint64_t j = base + threadIdx.x;
-        bool dies = false;
-        uint32_t idx = 0;
-        if (j < n) {
-            const uint64_t id = list[j];
-            if (id != EMPTY_ID) {
-                idx = id_index(id);
-                const unsigned old = atomicSub(I.refcount + idx, 1u);
-                if (old == 0) {
-                    atomicAdd(I.refcount + idx, 1u);
-                    set_error(I, ERR_REF_UB, 60);
-                } else {
-                    dies = old == 1;
-                }
-            }
-        }
-        push_dying(out, &I.ctr->scratch[SC_REL_OUT], dies, idx);
-    }
+    release_roots_range(I, list, out, &I.ctr->scratch[SC_REL_OUT], (uint64_t)blockIdx.x * blockDim.x,
+                        (uint64_t)gridDim.x * blockDim.x);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 
-// Retires the dying nodes of `in`: their children lose one reference each (children reaching zero
-// are the next dying set) and the nodes are recycled.
 __global__ void __launch_bounds__(kThreads) release_round_kernel(DevInterner I, const uint32_t *in, uint32_t *out) {
-    const uint64_t n = I.ctr->scratch[SC_REL_IN];
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const unsigned lane = threadIdx.x & 31u;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint64_t j = base + threadIdx.x;
-        const bool in_range = j < n;
-        const uint32_t idx = in_range ? in[j] : 0u;
-        const uint64_t id = in_range ? I.ids[idx] : 0ull;
-        const bool branch = in_range && id != 0 && id_is_branch(id);
-        for (int k = 0; k < 8; ++k) {
-            bool dies = false;
-            uint32_t cidx = 0;
-            if (branch) {
-                const uint64_t c = I.children[8ull * idx + k];
-                if (c != EMPTY_ID) {
-                    cidx = id_index(c);
-                    const unsigned old = atomicSub(I.refcount + cidx, 1u);
-                    if (old == 0) {
-                        atomicAdd(I.refcount + cidx, 1u);
-                        set_error(I, ERR_REF_UB, 61);
-                    } else {
-                        dies = old == 1;
-                    }
-                }
-            }
-            push_dying(out, &I.ctr->scratch[SC_REL_OUT], dies, cidx);
-        }
-        const bool rec = in_range && id != 0;
-        if (in_range && id == 0) set_error(I, ERR_INTERNAL, 62);
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, rec);
-        unsigned long long fbase = 0;
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            if ((int)lane == leader) fbase = atomicAdd(&I.ctr->free_count, (unsigned long long)__popc(m));
-            fbase = __shfl_sync(0xFFFFFFFFu, fbase, leader);
-        }
-        unsigned tomb = __ballot_sync(0xFFFFFFFFu, rec && branch);
-        if (lane == 0 && tomb) atomicAdd(&I.ctr->tombstones, (unsigned long long)__popc(tomb));
-        if (rec) recycle_node(I, idx, fbase + __popc(m & ((1u << lane) - 1u)));
-    }
+    release_round_range(I, in, out, &I.ctr->scratch[SC_REL_IN], &I.ctr->scratch[SC_REL_OUT],
+                        (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 

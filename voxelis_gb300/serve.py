@@ -243,7 +243,7 @@ class Server:
         """Serves `reqs` (sorted by arrival). Returns per-request latencies (s) and, optionally, the
         get results."""
         t0 = time.perf_counter()
-        pending, results = [], {}
+        pending, pend_reqs, results = [], [], {}  # arrived requests: indices and the requests themselves
         lat = np.full(len(reqs), np.nan)
         nxt, start = 0, 0
         inflight = None
@@ -251,15 +251,15 @@ class Server:
             now = time.perf_counter() - t0
             while nxt < len(reqs) and (not realtime or reqs[nxt]["t"] <= now):
                 pending.append(nxt)
+                pend_reqs.append(reqs[nxt])
                 nxt += 1
             wave = None
             if start < len(pending):
-                view = [reqs[j] for j in pending]
                 if one_by_one:
-                    r = view[start]
+                    r = pend_reqs[start]
                     e, g, end = ([r], [], start + 1) if r["kind"] == EDIT else ([], [r], start + 1)
                 else:
-                    e, g, end = self.form_wave(view, start)
+                    e, g, end = self.form_wave(pend_reqs, start)
                 if end > start:
                     wave = (pending[start:end], e, g)
                     ev = self.launch(e, g)
