@@ -321,3 +321,16 @@ def test_device_group_records_match_oracle(oracle_lib, gpu_lib, patches, launch)
     for x in tg:
         x._dirty = True
     assert_same(io, ig, to, tg)
+
+
+def test_dense_small_depths_in_any_order(oracle_lib, gpu_lib):
+    """Dense builds of chunks of depth 2 and 3 (one CTA per chunk, a shared-memory size per depth),
+    with a smaller build between two larger ones, equal the oracle's: a kernel's shared-memory
+    opt-in must not shrink when it is launched with less."""
+    for depth, bits in ((3, 8), (2, 8), (3, 8), (3, 16), (2, 16), (3, 16)):
+        side = 1 << depth
+        grids = W.dune_chunks(2, 4, depth=depth, seed=60 + depth, base=side // 2, amp=side // 3, scale=side * 1.5,
+                              dtype=np.uint8 if bits == 8 else np.uint16)
+        io, to = build_terrain(oracle_lib, grids, depth, bits=bits)
+        ig, tg = build_terrain(gpu_lib, grids, depth, bits=bits)
+        assert_same(io, ig, to, tg)

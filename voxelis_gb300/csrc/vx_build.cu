@@ -1915,7 +1915,9 @@ __global__ void epoch_finalize_kernel(DevInterner I) { epoch_finalize_body(I); }
 }  // namespace
 
 // Opts `kernel` in to `smem` bytes of dynamic shared memory and returns its resident CTAs per SM,
-// cached per (kernel, threads, smem): both calls cost host time on every launch otherwise.
+// cached per (kernel, threads, smem): both calls cost host time on every launch otherwise. The
+// opt-in is a property of the kernel, so it only ever rises (a kernel launched with several sizes,
+// such as the dense-block kernel at depths 2 and 3, keeps the largest size it was opted in to).
 static int prepare_kernel(const void *kernel, int threads, size_t smem, cudaError_t *err) {
     struct Entry {
         const void *k;
@@ -1923,18 +1925,29 @@ static int prepare_kernel(const void *kernel, int threads, size_t smem, cudaErro
         size_t smem;
         int per_sm;
     };
-    static Entry cache[32];
-    static int used = 0;
+    struct OptIn {
+        const void *k;
+        size_t smem;
+    };
+    static Entry cache[64];
+    static OptIn opted[32];
+    static int used = 0, n_opted = 0;
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);
     for (int i = 0; i < used; ++i)
         if (cache[i].k == kernel && cache[i].threads == threads && cache[i].smem == smem) return cache[i].per_sm;
-    *err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (*err != cudaSuccess) return 0;
+    int o = 0;
+    while (o < n_opted && opted[o].k != kernel) ++o;
+    if (o == n_opted || opted[o].smem < smem) {
+        *err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (*err != cudaSuccess) return 0;
+        if (o == n_opted && n_opted < 32) ++n_opted;
+        if (o < 32) opted[o] = OptIn{kernel, smem};
+    }
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     if (per_sm < 1) per_sm = 1;
-    if (used < 32) cache[used++] = Entry{kernel, threads, smem, per_sm};
+    if (used < 64) cache[used++] = Entry{kernel, threads, smem, per_sm};
     return per_sm;
 }
 
