@@ -113,6 +113,14 @@ typedef struct {
 int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_flags,
                        int table_log2, vx_interner **out);
 int vx_interner_destroy(vx_interner *it);
+/* Bounds of the device's waits for this interner (no counterpart in the reference, whose waits
+ * cannot fail): max_probes branch-table probes per insert before VX_E_TABLE_FULL (at most the table's
+ * slots; 1..65536 by default), round_limit rounds of the warp-cooperative insert loop and spin_limit
+ * iterations of a wait on another thread (a leaf being created, a grid barrier, a scan's look-back)
+ * before VX_E_TIMEOUT. Later calls use the new values; every wait ends, and the context stays usable
+ * (vx_interner_reset clears the sticky status). Defaults: 2^20 rounds, 2^22 spins. */
+int vx_interner_set_limits(vx_interner *it, uint32_t max_probes, uint32_t round_limit, uint32_t spin_limit);
+int vx_interner_get_limits(vx_interner *it, uint32_t *max_probes, uint32_t *round_limit, uint32_t *spin_limit);
 /* Orders all later work of this interner on `cuda_stream` (a cudaStream_t; NULL = the
  * interner's own stream). */
 int vx_interner_set_stream(vx_interner *it, void *cuda_stream);

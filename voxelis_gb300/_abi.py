@@ -143,6 +143,8 @@ GPU_SIGNATURES = {
     "interner_reset": [_P],
     "interner_maintain": [_P],
     "interner_set_stream": [_P, _P],
+    "interner_set_limits": [_P, _U32, _U32, _U32],
+    "interner_get_limits": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "interner_sync": [_P],
     "trees_create": [_P, _U32, _P, _P],
     "build_dense_async": [_P, _U32, _P, _P, _P, _I],

@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner 
             st_release_u64(status + tile, (1ull << 32) | agg);
             uint32_t j = tile - 1;
             for (uint32_t spin = 0;; ++spin) {
-                if (spin >= SPIN_LIMIT) {
+                if (spin >= I.spin_limit) {
                     set_error(I, ERR_TIMEOUT, 40);
                     break;
                 }

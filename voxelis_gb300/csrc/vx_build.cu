@@ -87,7 +87,7 @@ __device__ __forceinline__ uint64_t leaf_of(const DevInterner &I, uint64_t *leaf
         if (id) return id;
         bool created;
         id = intern_leaf(I, v, &created);
-        if (id != INVALID_ID) leaf_cache[v] = id;
+        if (id != EMPTY_ID) leaf_cache[v] = id;
         return id;
     }
     uint64_t id = ld_volatile(I.leaf_table + v);
@@ -504,7 +504,7 @@ __device__ __forceinline__ void reduce_parent_cached(const DevInterner &I, const
         const uint64_t nid = warp_intern_branch_inl(I, need, c, types, mask, lod, &created);
         if (need) {
             id = nid;
-            if (nid != INVALID_ID) nc_insert(N, c, 1u, nid, lod);
+            if (nid != EMPTY_ID) nc_insert(N, c, 1u, nid, lod);
         }
     }
     if (mask == 0) {
@@ -737,7 +737,7 @@ __device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache
             bool created;
             uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
             nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-            if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+            if (lead && nid != EMPTY_ID) kc_insert(C, lo, hi, nid, lod);
             if (need) id = nid;
         }
         if (set == 0) {
@@ -838,7 +838,7 @@ __device__ __forceinline__ void reduce_tile16(const DevInterner &I, const OctArg
             if (active) {
                 qid[q] = pid;
                 qval[q] = pval;
-                if (memo && pid != INVALID_ID) memo_insert<T>(a, h1[q], h2[q], qb[q], pid, pval);
+                if (memo && pid != EMPTY_ID) memo_insert<T>(a, h1[q], h2[q], qb[q], pid, pval);
             }
         }
         l3[q] = qid[q];
@@ -1188,7 +1188,7 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
                 if (active) {
                     qidv[p] = pid;
                     qvalv[p] = pval;
-                    if (memo && pid != INVALID_ID) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
+                    if (memo && pid != EMPTY_ID) memo_insert<T, 32>(a, h1[p], h2[p], qb[p], pid, pval);
                 }
             }
             qid_s[qm[p]] = qidv[p];
@@ -1425,7 +1425,7 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
             if (active) {
                 qidv[p] = pid;
                 qvalv[p] = pval;
-                if (memo && !VX_QUAD_DEFER && pid != INVALID_ID) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
+                if (memo && !VX_QUAD_DEFER && pid != EMPTY_ID) memo_insert<T, S>(a, h1[p], h2[p], qb[p], pid, pval);
             }
         }
         const uint64_t lid = __shfl_sync(0xFFFFFFFFu, qidv[p], leader[p]);
@@ -1627,7 +1627,7 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
             bool created;
             uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
             nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
-            if (lead && nid != INVALID_ID) kc_insert(C, lo, hi, nid, lod);
+            if (lead && nid != EMPTY_ID) kc_insert(C, lo, hi, nid, lod);
             if (need) id = nid;
         }
         uint64_t gid;

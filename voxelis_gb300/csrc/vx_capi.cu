@@ -718,6 +718,8 @@ int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_fla
     D.flags = patch_flags;
     D.table_mask = slots - 1;
     D.max_probes = (uint32_t)std::min<uint64_t>(slots, 1u << 16);
+    D.round_limit = ROUND_LIMIT;
+    D.spin_limit = SPIN_LIMIT;
     const size_t vb = voxel_bits / 8;
     bool ok = true;
     auto alloc = [&](void **p, size_t bytes) {
@@ -852,6 +854,23 @@ int vx_interner_reset(vx_interner *it) {
     VX_CUDA(cudaStreamSynchronize(s));
     std::fill(it->tree_maybe_nonempty.begin(), it->tree_maybe_nonempty.end(), 0);
     it->all_trees_unknown = false;
+    return VX_OK;
+}
+
+int vx_interner_set_limits(vx_interner *it, uint32_t max_probes, uint32_t round_limit, uint32_t spin_limit) {
+    if (!it || max_probes == 0) return VX_E_INVALID_ARG;
+    VX_CUDA(cudaStreamSynchronize(it->stream));  // kernels already queued keep the limits they were given
+    it->dev.max_probes = (uint32_t)std::min<uint64_t>(max_probes, it->table_slots);
+    it->dev.round_limit = round_limit;
+    it->dev.spin_limit = spin_limit;
+    return VX_OK;
+}
+
+int vx_interner_get_limits(vx_interner *it, uint32_t *max_probes, uint32_t *round_limit, uint32_t *spin_limit) {
+    if (!it || !max_probes || !round_limit || !spin_limit) return VX_E_INVALID_ARG;
+    *max_probes = it->dev.max_probes;
+    *round_limit = it->dev.round_limit;
+    *spin_limit = it->dev.spin_limit;
     return VX_OK;
 }
 

@@ -48,6 +48,10 @@ enum : uint32_t {
 
 constexpr uint8_t TREE_UNUSED = 0xFF;  // depth marker of a free tree slot
 
+// Bounds of every wait. The copy waits of the dense kernels (TMA tiles, and the drain of a warp's
+// own copies after giving up) always use SPIN_LIMIT; the waits on other threads (leaf creation, grid
+// barriers, scan look-back) use the interner's spin_limit and the warp-intern loop its round_limit,
+// both settable per interner (vx_interner_set_limits) and SPIN_LIMIT / ROUND_LIMIT by default.
 constexpr uint32_t SPIN_LIMIT = 1u << 22;   // bounded waits (~tens of ms with nanosleep)
 constexpr uint32_t ROUND_LIMIT = 1u << 20;  // bounded warp-intern rounds
 
@@ -83,7 +87,9 @@ struct DevInterner {
     uint32_t capacity;
     int vbits;
     uint32_t flags;
-    uint32_t max_probes;
+    uint32_t max_probes;   // branch-table probes before ERR_TABLE_FULL
+    uint32_t round_limit;  // warp-intern rounds before ERR_TIMEOUT
+    uint32_t spin_limit;   // iterations of a wait on another thread before ERR_TIMEOUT
 };
 
 // ---- BlockId (core/block_id.rs:19-418) -------------------------------------------------------
@@ -303,7 +309,10 @@ __device__ __forceinline__ bool key_equal(const DevInterner &I, uint32_t idx, co
 // one non-blocking probe step; lanes that claimed an empty slot receive node indices from a single
 // warp-aggregated ticket range, write their node and publish it. A lane that meets a slot still being
 // written retries it next round, so no lane ever waits inside a divergent branch.
-// Returns the BlockId, or INVALID_ID on error; *created tells whether this lane inserted the node.
+// Returns the BlockId; *created tells whether this lane inserted the node. On failure (probe limit,
+// round limit, out of nodes: a sticky error bit is set) the lane gets EMPTY_ID, which every consumer
+// handles without dereferencing it, so a failed call leaves wrong but memory-safe results until
+// vx_interner_reset.
 #ifndef VX_INTERN_INLINE
 #define VX_INTERN_INLINE __noinline__
 #endif
@@ -317,7 +326,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
     uint64_t pos = 0;
     uint32_t probes = 0;
     bool done = !active;
-    uint64_t result = INVALID_ID;
+    uint64_t result = EMPTY_ID;
     *created = false;
     // constant during an epoch: loaded beside the first probe instead of after a ticket is taken
     const unsigned long long fc = I.ctr->free_count, ni = I.ctr->next_index;
@@ -382,7 +391,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
             }
         }
         if (!__any_sync(0xFFFFFFFFu, !done)) break;
-        if (round >= ROUND_LIMIT) {
+        if (round >= I.round_limit) {
             if (!done) {
                 set_error(I, ERR_TIMEOUT, 2);
                 done = true;
@@ -402,13 +411,14 @@ static __device__ VX_INTERN_INLINE uint64_t warp_intern_branch(const DevInterner
 }
 
 // Find-or-create of the leaf for value v (v != 0) through the direct-mapped leaf table.
-// *created tells whether this call allocated the leaf (its refcount starts at 0).
+// *created tells whether this call allocated the leaf (its refcount starts at 0). On failure (out of
+// nodes, wait limit: sticky error bit set) it returns EMPTY_ID, like warp_intern_branch.
 __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v, bool *created) {
     *created = false;
     unsigned long long *slot = (unsigned long long *)(I.leaf_table + v);
     uint64_t s = ld_volatile(I.leaf_table + v);
     if (s > LEAF_BUSY) return s;
-    for (uint32_t spin = 0; spin < SPIN_LIMIT; ++spin) {
+    for (uint32_t spin = 0; spin < I.spin_limit; ++spin) {
         if (s == 0) {  // free (or its creator ran out of memory and backed off): claim it
             const uint64_t prev = atomicCAS(slot, 0ull, LEAF_BUSY);
             if (prev == 0) {
@@ -417,7 +427,7 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
                 if (idx == NO_NODE) {
                     set_error(I, ERR_OOM, 2);
                     atomicExch(slot, 0ull);
-                    return INVALID_ID;
+                    return EMPTY_ID;
                 }
                 const uint64_t id = make_leaf_id(idx, I.generation[idx]);
                 set_node_value(I, idx, v);
@@ -435,7 +445,7 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
         if (s > LEAF_BUSY) return s;
     }
     set_error(I, ERR_TIMEOUT, 3);
-    return INVALID_ID;
+    return EMPTY_ID;
 }
 
 // Removes a dead node from its table, clears the record, bumps the generation and pushes the slot
@@ -495,7 +505,7 @@ __device__ __forceinline__ bool grid_sync(const DevInterner &I) {
                 // a CTA that gave up at an earlier barrier never arrives: stop waiting at once
                 const bool gave_up = (spin & 1023u) == 1023u &&
                                      (*reinterpret_cast<volatile unsigned int *>(&I.ctr->error) & ERR_TIMEOUT);
-                if (++spin >= SPIN_LIMIT || gave_up) {
+                if (++spin >= I.spin_limit || gave_up) {
                     set_error(I, ERR_TIMEOUT, 49);
                     ok = 0;
                     break;
