@@ -258,6 +258,25 @@ int vx_copy_to_device_async(vx_interner *it, uint32_t n, void *const *dst_dev, c
 int vx_world_get_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
                        uint8_t *found_dev, void *values_dev);
 
+/* Snapshot reads for serving waves that mix edits and gets (no counterpart in the reference; built
+ * on VoxInterner::inc_ref and dec_ref_recursive, interner/mod.rs:235-260 and 419-534). Before a wave's
+ * apply, vx_world_hold_async takes one more reference on the current root of each of the n listed
+ * chunks (their ids go to held_dev[k] and old_roots_dev[chunk]) and records ranks_dev[k], the
+ * position of the wave's edit of that chunk, in edit_rank_dev[chunk]. old_roots_dev and
+ * edit_rank_dev are world-sized device arrays of the caller; edit_rank_dev starts as 0xFFFFFFFF for
+ * every chunk. vx_world_get_at_async is vx_world_get_async except that a chunk whose edit rank is
+ * `cut` or more is read at its held root: a get issued with cut = the number of the wave's edits
+ * that precede it sees exactly those edits. After the wave's gets, vx_world_release_async resets
+ * the ranks of the listed chunks to 0xFFFFFFFF and releases the held roots (a root the apply
+ * replaced is freed then). */
+int vx_world_hold_async(vx_interner *it, const vx_world *world, uint32_t n, const uint32_t *chunks_dev,
+                        const uint32_t *ranks_dev, uint64_t *held_dev, uint64_t *old_roots_dev, uint32_t *edit_rank_dev);
+int vx_world_get_at_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
+                          uint8_t *found_dev, void *values_dev, const uint64_t *old_roots_dev,
+                          const uint32_t *edit_rank_dev, uint32_t cut);
+int vx_world_release_async(vx_interner *it, const vx_world *world, uint32_t n, const uint32_t *chunks_dev,
+                           uint64_t *held_dev, uint32_t *edit_rank_dev);
+
 /* Occupancy masks for greedy meshing (generate_occupancy_masks + fill_masks_for_region,
  * utils/mesh.rs:418-597; OccupancyDataBuilder, mesh.rs:181-193): the non-default voxels of n_trees
  * trees of one MaxDepth d (1..6) placed into one 64^3 builder, tree k at voxel offset

@@ -152,6 +152,9 @@ GPU_SIGNATURES = {
     "apply_groups_async": [_P, _U32, _P, _P, _P, _U32, _P, _P, _P, _P, _P, _P, _I],
     "tune_set": [_P, _I, _I],
     "world_get_async": [_P, _P, _U64, _P, _P, _P],
+    "world_hold_async": [_P, _P, _U32, _P, _P, _P, _P, _P],
+    "world_get_at_async": [_P, _P, _U64, _P, _P, _P, _P, _P, _U32],
+    "world_release_async": [_P, _P, _U32, _P, _P, _P],
     "copy_to_device_async": [_P, _U32, _P, _P, _P],
     "tune_get": [_P, _PI, _PI],
     "tune_set_launch": [_P, _I],

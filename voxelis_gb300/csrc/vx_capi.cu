@@ -672,6 +672,14 @@ bool interner_parts(vx_interner *it, DevInterner *dev, cudaStream_t *stream, int
 void interner_set_error(vx_interner *it, const char *msg) {
     if (it) it->last_error = msg;
 }
+// Releases (dec_ref_recursive) the ids in list_dev, as many as the release slot counts, in `rounds`
+// breadth-first rounds, on the interner's stream.
+int interner_release_list(vx_interner *it, uint64_t *list_dev, int rounds) {
+    Phase ph(it, VX_PROF_RELEASE);
+    VX_CUDA(launch_release(it->dev, list_dev, it->frontier, it->frontier + it->capacity, it->capacity, rounds,
+                           it->num_sms, it->stream));
+    return VX_OK;
+}
 }  // namespace vxg
 
 extern "C" {

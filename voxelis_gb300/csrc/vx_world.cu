@@ -85,9 +85,13 @@ struct RecMap {
     }
 };
 
+// Gets at world coordinates. With old_roots, a chunk whose edit_rank is cut or more (and not
+// kNoRank) is read at the root held for it before the wave's apply (see vx_world_hold_async).
+constexpr uint32_t kNoRank = 0xFFFFFFFFu;
+
 template <class T>
 __global__ void world_get_kernel(DevInterner I, vx_world W, uint64_t n, const int32_t *xyz, uint8_t *found,
-                                 T *values) {
+                                 T *values, const uint64_t *old_roots, const uint32_t *edit_rank, uint32_t cut) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const int d = W.chunk_depth;
     const int32_t side = 1 << d;
@@ -103,6 +107,10 @@ __global__ void world_get_kernel(DevInterner I, vx_world W, uint64_t n, const in
             const uint32_t t = __ldg(W.trees_dev + chunk);
             const int32_t lx = x & (side - 1), ly = y & (side - 1), lz = z & (side - 1);
             uint64_t node = t < I.tree_cap ? I.roots[t] : EMPTY_ID;
+            if (old_roots) {
+                const uint32_t r = __ldg(edit_rank + chunk);
+                if (r != kNoRank && r >= cut) node = __ldg(reinterpret_cast<const unsigned long long *>(old_roots) + chunk);
+            }
             int depth = 0;
             while (node != EMPTY_ID) {
                 if (depth >= d) {
@@ -129,6 +137,35 @@ __global__ void world_get_kernel(DevInterner I, vx_world W, uint64_t n, const in
         values[q] = (T)val;
     }
     if (oob) set_error(I, ERR_OOB, 90);
+}
+
+// Holds the current root of each listed chunk for the gets of a wave that must not see the wave's
+// edits: one more reference on it (VoxInterner::inc_ref, interner/mod.rs:235-260), its id in
+// held[k] and old_roots[chunk], the rank of the wave's edit of that chunk in edit_rank[chunk].
+__global__ void world_hold_kernel(DevInterner I, vx_world W, uint32_t n, const uint32_t *chunks, const uint32_t *ranks,
+                                  uint64_t *held, uint64_t *old_roots, uint32_t *edit_rank) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t c = chunks[k];
+    if (c >= (uint32_t)(W.nx * W.ny * W.nz)) {
+        set_error(I, ERR_OOB, 91);
+        held[k] = EMPTY_ID;
+        return;
+    }
+    const uint32_t t = W.trees_dev[c];
+    const uint64_t root = t < I.tree_cap ? I.roots[t] : EMPTY_ID;
+    held[k] = root;
+    old_roots[c] = root;
+    edit_rank[c] = ranks[k];
+    if (root != EMPTY_ID) atomicAdd(I.refcount + id_index(root), 1u);
+}
+
+// Ends the holds: the listed chunks read their current roots again, and the held ids become the
+// list of the release that follows (count in the release slot).
+__global__ void world_unhold_kernel(DevInterner I, vx_world W, uint32_t n, const uint32_t *chunks, uint32_t *edit_rank) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) I.ctr->scratch[SC_RELEASE] = n;
+    if (k < n && chunks[k] < (uint32_t)(W.nx * W.ny * W.nz)) edit_rank[chunks[k]] = kNoRank;
 }
 
 }  // namespace
@@ -236,16 +273,95 @@ extern "C" int vx_world_get_async(vx_interner *it, const vx_world *world, uint64
     count_launches(1);
     if (D.vbits == 8)
         world_get_kernel<uint8_t><<<(unsigned)blocks, 256, 0, s>>>(D, *world, n, world_xyz_dev, found_dev,
-                                                                   (uint8_t *)values_dev);
+                                                                   (uint8_t *)values_dev, nullptr, nullptr, 0);
     else
         world_get_kernel<uint16_t><<<(unsigned)blocks, 256, 0, s>>>(D, *world, n, world_xyz_dev, found_dev,
-                                                                    (uint16_t *)values_dev);
+                                                                    (uint16_t *)values_dev, nullptr, nullptr, 0);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         interner_set_error(it, cudaGetErrorString(e));
         return VX_E_CUDA;
     }
     return VX_OK;
+}
+
+extern "C" int vx_world_hold_async(vx_interner *it, const vx_world *world, uint32_t n, const uint32_t *chunks_dev,
+                                   const uint32_t *ranks_dev, uint64_t *held_dev, uint64_t *old_roots_dev,
+                                   uint32_t *edit_rank_dev) {
+    DevInterner D;
+    cudaStream_t s;
+    int num_sms;
+    uint32_t flags;
+    if (!interner_parts(it, &D, &s, &num_sms, &flags, false) || !world) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    if (!world->trees_dev || !chunks_dev || !ranks_dev || !held_dev || !old_roots_dev || !edit_rank_dev)
+        return VX_E_INVALID_ARG;
+    count_launches(1);
+    world_hold_kernel<<<(n + 255) / 256, 256, 0, s>>>(D, *world, n, chunks_dev, ranks_dev, held_dev, old_roots_dev,
+                                                      edit_rank_dev);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        interner_set_error(it, cudaGetErrorString(e));
+        return VX_E_CUDA;
+    }
+    return VX_OK;
+}
+
+extern "C" int vx_world_get_at_async(vx_interner *it, const vx_world *world, uint64_t n, const int32_t *world_xyz_dev,
+                                     uint8_t *found_dev, void *values_dev, const uint64_t *old_roots_dev,
+                                     const uint32_t *edit_rank_dev, uint32_t cut) {
+    DevInterner D;
+    cudaStream_t s;
+    int num_sms;
+    uint32_t flags;
+    if (!interner_parts(it, &D, &s, &num_sms, &flags, false) || !world) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    if (!world->trees_dev || !world_xyz_dev || !found_dev || !values_dev || !old_roots_dev || !edit_rank_dev ||
+        world->chunk_depth < 0 || world->chunk_depth > 10)
+        return VX_E_INVALID_ARG;
+    uint64_t blocks = (n + 255) / 256;
+    if (blocks > (uint64_t)num_sms * 16) blocks = (uint64_t)num_sms * 16;
+    count_launches(1);
+    if (D.vbits == 8)
+        world_get_kernel<uint8_t><<<(unsigned)blocks, 256, 0, s>>>(D, *world, n, world_xyz_dev, found_dev,
+                                                                   (uint8_t *)values_dev, old_roots_dev, edit_rank_dev,
+                                                                   cut);
+    else
+        world_get_kernel<uint16_t><<<(unsigned)blocks, 256, 0, s>>>(D, *world, n, world_xyz_dev, found_dev,
+                                                                    (uint16_t *)values_dev, old_roots_dev,
+                                                                    edit_rank_dev, cut);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        interner_set_error(it, cudaGetErrorString(e));
+        return VX_E_CUDA;
+    }
+    return VX_OK;
+}
+
+namespace vxg {
+int interner_release_list(vx_interner *it, uint64_t *list_dev, int rounds);
+}
+
+extern "C" int vx_world_release_async(vx_interner *it, const vx_world *world, uint32_t n, const uint32_t *chunks_dev,
+                                      uint64_t *held_dev, uint32_t *edit_rank_dev) {
+    DevInterner D;
+    cudaStream_t s;
+    int num_sms;
+    uint32_t flags;
+    if (!interner_parts(it, &D, &s, &num_sms, &flags, false) || !world) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    if (!world->trees_dev || !chunks_dev || !held_dev || !edit_rank_dev || world->chunk_depth < 0 ||
+        world->chunk_depth > 10)
+        return VX_E_INVALID_ARG;
+    count_launches(1);
+    world_unhold_kernel<<<(n + 255) / 256, 256, 0, s>>>(D, *world, n, chunks_dev, edit_rank_dev);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        interner_set_error(it, cudaGetErrorString(e));
+        return VX_E_CUDA;
+    }
+    // dec_ref_recursive of every held root: a held root the apply replaced dies here
+    return interner_release_list(it, held_dev, world->chunk_depth + 1);
 }
 
 // n host -> device copies on the interner's stream, one cudaMemcpyAsync each (serving loops stage a

@@ -7,14 +7,21 @@ Requests arrive over time; each is either
         into one Batch per touched chunk, then apply_batch on each of those chunks, or
   get   a set of world points read with VoxTree::get.
 Semantics are those of executing the requests one by one in arrival order. The loop executes them in
-waves: a wave is the longest arrival-order prefix of pending requests made of edits touching pairwise
-disjoint chunks followed by gets; its edits run as one batched apply (vx_apply_groups_async) and its
-gets as batched world gets after them, so every result equals the one-by-one result. Requests that
-arrive while a wave is on the GPU are admitted into the next one, which is staged on the host
-(vx_stage_spheres, pinned buffers, async copies) while the device works. Edits are admitted only
-while the interner's free node headroom covers a conservative estimate of the nodes they can create;
-replaced roots are released (nodes recycled with a new generation) by every apply, and the branch
-table is rebuilt from live nodes when deletions pile up (vx_interner_maintain).
+waves, scanning the pending requests in arrival order: an edit joins the wave unless one of its
+chunks is already edited in the wave or belongs to an edit held back before it (then it is held back
+too, so the edits of a chunk keep their order); a get joins the wave with its cut, the number of the
+wave's edits that arrived before it, unless an edit before it was held back (the wave ends there).
+The wave's edits run as one batched apply (vx_apply_groups_async). When a get must not see some of
+them, the current roots of the edited chunks are held first (vx_world_hold_async: one more
+reference each) and the get reads every chunk edited at or after its cut at the held root
+(vx_world_get_at_async); the holds are released after the wave's gets (vx_world_release_async). So
+every get sees exactly the edits that arrived before it, every result equals the one-by-one result,
+and a backlog forms large waves. Requests that arrive while a wave is on the GPU are admitted into
+the next one, which is staged on the host (vx_stage_spheres, pinned buffers, async copies) while the
+device works. Edits are admitted only while the interner's free node headroom covers a conservative
+estimate of the nodes they can create; replaced roots are released (nodes recycled with a new
+generation) by every apply, and the branch table is rebuilt from live nodes when deletions pile up
+(vx_interner_maintain).
 """
 import ctypes as C
 import math
@@ -52,6 +59,9 @@ class World:
         self.call("trees_create", n, depths.ctypes.data, self.trees.ctypes.data)
         self.trees_d = torch.from_numpy(self.trees.view(np.int32)).to(self.dev)
         self.wdesc = vx_world(nx, ny, nz, depth, C.c_void_p(self.trees_d.data_ptr()))
+        # per chunk: the root held for reads before a wave's edit, and that edit's rank in the wave
+        self.old_roots = torch.zeros(n, dtype=torch.int64, device=self.dev)
+        self.edit_rank = torch.full((n,), -1, dtype=torch.int32, device=self.dev)
 
     def call(self, name, *args):
         return self.lib.call(name, self.h, *args, handle=self.h)
@@ -131,11 +141,16 @@ class Server:
         # two sets of pinned staging buffers: wave k+1 is staged while wave k's copies may be queued
         self.hset = [dict(items=pin(cap_items, torch.int32), item_trees=pin(cap_items, torch.int32),
                           ri=pin(cap_recs, torch.int32), rg=pin(cap_recs, torch.int32), rs=pin(cap_recs, torch.uint8),
-                          rc=pin(cap_recs, torch.uint8), rv=pin(cap_recs * 8, torch.int16)) for _ in range(2)]
+                          rc=pin(cap_recs, torch.uint8), rv=pin(cap_recs * 8, torch.int16),
+                          ranks=pin(cap_items, torch.int32)) for _ in range(2)]
         for k, hs in enumerate(self.hset):  # numpy views of the pinned buffers (no torch call per wave)
             hs["k"] = k
-            hs["np"] = {"items": hs["items"].numpy(), "item_trees": hs["item_trees"].numpy()}
+            hs["np"] = {"items": hs["items"].numpy(), "item_trees": hs["item_trees"].numpy(),
+                        "ranks": hs["ranks"].numpy()}
         self.parity = 0
+        self.d_item_chunks = torch.empty(cap_items, dtype=torch.int32, device=dev)
+        self.d_ranks = torch.empty(cap_items, dtype=torch.int32, device=dev)
+        self.d_held = torch.empty(cap_items, dtype=torch.int64, device=dev)
         self.d_item_trees = torch.empty(cap_items, dtype=torch.int32, device=dev)
         self.d_flags = torch.full((cap_items,), 2, dtype=torch.uint8, device=dev)
         self.d_fill = torch.zeros(cap_items, dtype=torch.int32, device=dev)
@@ -144,12 +159,14 @@ class Server:
         self.d_rs = torch.empty(cap_recs, dtype=torch.uint8, device=dev)
         self.d_rc = torch.empty(cap_recs, dtype=torch.uint8, device=dev)
         self.d_rv = torch.empty(cap_recs * 8, dtype=torch.int16, device=dev)
-        # per pinned set: the 6 staged arrays' device and host addresses for one vx_copy_to_device_async
-        dsts = [self.d_item_trees, self.d_ri, self.d_rg, self.d_rs, self.d_rc, self.d_rv]
+        # per pinned set: the staged arrays' device and host addresses for one vx_copy_to_device_async
+        # (the item chunks and their edit ranks only go over when the wave holds roots)
+        dsts = [self.d_item_trees, self.d_ri, self.d_rg, self.d_rs, self.d_rc, self.d_rv, self.d_item_chunks,
+                self.d_ranks]
+        names = ("item_trees", "ri", "rg", "rs", "rc", "rv", "items", "ranks")
         self.copies = [{"dst": np.array([t.data_ptr() for t in dsts], np.uint64),
-                        "src": np.array([hs[k].data_ptr() for k in ("item_trees", "ri", "rg", "rs", "rc", "rv")],
-                                        np.uint64),
-                        "bytes": np.zeros(6, np.uint64)} for hs in self.hset]
+                        "src": np.array([hs[k].data_ptr() for k in names], np.uint64),
+                        "bytes": np.zeros(len(names), np.uint64)} for hs in self.hset]
         self.d_pts = torch.empty((max_wave_gets, self.ppg, 3), dtype=torch.int32, device=dev)
         self.pool_ptr = [p.data_ptr() for p in self.pool_h]
         self.get_dst = np.array([self.d_pts[k].data_ptr() for k in range(max_wave_gets)], np.uint64)
@@ -171,34 +188,51 @@ class Server:
         self.records = self.items = self.points = 0
 
     # -- wave formation ------------------------------------------------------------------------------
-    def form_wave(self, pending, start):
-        """Longest prefix pending[start:] of chunk-disjoint edits then gets (bounded sizes)."""
-        edits, gets, touched = [], [], set()
-        i = start
-        while i < len(pending):
-            r = pending[i]
+    def form_wave(self, pending, scan_limit=None):
+        """The next wave from `pending` (unserved requests in arrival order): (edits, gets, taken), the
+        edits touching pairwise disjoint chunks, each get as (request, cut) where cut is the number of
+        the wave's edits that arrived before it, and `taken` the positions in `pending` of the
+        requests the wave serves. An edit whose chunks meet an edit of the wave, or an edit held back
+        before it, is held back; a get after a held-back edit ends the wave, as do the size limits
+        and memory admission."""
+        edits, gets, taken = [], [], []
+        touched, blocked = set(), set()
+        held_back = False
+        limit = scan_limit if scan_limit is not None else 4 * (self.max_e + self.max_g)
+        for i, r in enumerate(pending):
+            if i >= limit:
+                break
             if r["kind"] == EDIT:
-                if gets or len(edits) >= self.max_e or (r["chunks"] & touched):
+                if len(edits) >= self.max_e:
                     break
+                if r["chunks"] & touched or r["chunks"] & blocked:
+                    blocked |= r["chunks"]
+                    held_back = True
+                    continue
                 est = 2 * math.ceil((4.19 * r["radius"] ** 3) / 8 + 1) * self.w.depth
                 if self.alive_est + est > self.capacity - self.headroom:
-                    break  # memory admission: wait for releases
+                    break  # memory admission: this and later requests wait for releases
                 self.alive_est += est
                 edits.append(r)
+                taken.append(i)
                 touched |= r["chunks"]
             else:
-                if len(gets) >= self.max_g:
+                if held_back or len(gets) >= self.max_g:
                     break
-                gets.append(r)
-            i += 1
-        return edits, gets, i
+                gets.append((r, len(edits)))
+                taken.append(i)
+        return edits, gets, taken
 
     # -- staging and launch ----------------------------------------------------------------------------
     def launch(self, edits, gets):
+        """Queues a wave: its edits as one batched apply, then its gets (each a (request, cut) pair),
+        with the edited chunks' roots held for the gets that must not see every edit."""
         w, torch = self.w, self.torch
         P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
         hs = self.hset[self.parity]
         self.parity ^= 1
+        ni = 0
+        hold = bool(edits) and any(cut < len(edits) for _, cut in gets)
         if edits:
             n = len(edits)
             cen = np.array([e["center"] for e in edits], np.int32)
@@ -214,23 +248,37 @@ class Server:
             ni, nr = ni.value, nr.value
             self.records += nr
             self.items += ni
+            hold = hold and ni > 0
             if ni:
                 hn = hs["np"]
                 np.take(w.trees.view(np.int32), hn["items"][:ni], out=hn["item_trees"][:ni])
+                if hold:  # each item's chunk belongs to exactly one of the wave's edits: its rank
+                    rank_of = {c: k for k, e in enumerate(edits) for c in e["chunks"]}
+                    hn["ranks"][:ni] = [rank_of[int(c)] for c in hn["items"][:ni]]
                 cp = self.copies[hs["k"]]
-                cp["bytes"][:] = (4 * ni, 4 * nr, 4 * nr, nr, nr, 16 * nr)  # item trees, ri, rg, rs, rc, rv
-                w.call("copy_to_device_async", 6, cp["dst"].ctypes.data, cp["src"].ctypes.data, cp["bytes"].ctypes.data)
+                hb = 4 * ni if hold else 0
+                cp["bytes"][:] = (4 * ni, 4 * nr, 4 * nr, nr, nr, 16 * nr, hb, hb)
+                w.call("copy_to_device_async", 8, cp["dst"].ctypes.data, cp["src"].ctypes.data, cp["bytes"].ctypes.data)
+                if hold:
+                    w.call("world_hold_async", C.byref(w.wdesc), ni, P(self.d_item_chunks), P(self.d_ranks),
+                           P(self.d_held), P(w.old_roots), P(w.edit_rank))
                 w.call("apply_groups_async", ni, P(self.d_item_trees), P(self.d_flags), P(self.d_fill), nr,
                        P(self.d_ri), P(self.d_rg), P(self.d_rs), P(self.d_rc), P(self.d_rv), None, w.depth)
         if gets:  # the gets' point sets in one call, then one batched world get each
             ng = len(gets)
             self.points += ng * self.ppg
-            self.get_src[:ng] = [self.pool_ptr[g["pool"]] for g in gets]
+            self.get_src[:ng] = [self.pool_ptr[g["pool"]] for g, _ in gets]
             w.call("copy_to_device_async", ng, self.get_dst.ctypes.data, self.get_src.ctypes.data,
                    self.get_bytes.ctypes.data)
-        for k, g in enumerate(gets):
-            w.call("world_get_async", C.byref(w.wdesc), C.c_uint64(self.ppg), P(self.d_pts[k]), P(self.d_found[k]),
-                   P(self.d_vals[k]))
+        for k, (g, cut) in enumerate(gets):
+            if hold and cut < len(edits):
+                w.call("world_get_at_async", C.byref(w.wdesc), C.c_uint64(self.ppg), P(self.d_pts[k]),
+                       P(self.d_found[k]), P(self.d_vals[k]), P(w.old_roots), P(w.edit_rank), cut)
+            else:
+                w.call("world_get_async", C.byref(w.wdesc), C.c_uint64(self.ppg), P(self.d_pts[k]),
+                       P(self.d_found[k]), P(self.d_vals[k]))
+        if hold:
+            w.call("world_release_async", C.byref(w.wdesc), ni, P(self.d_item_chunks), P(self.d_held), P(w.edit_rank))
         if gets:
             with torch.cuda.stream(w.stream):
                 self.h_found[:len(gets)].copy_(self.d_found[:len(gets)], non_blocking=True)
@@ -243,32 +291,37 @@ class Server:
         """Serves `reqs` (sorted by arrival). Returns per-request latencies (s) and, optionally, the
         get results."""
         t0 = time.perf_counter()
-        pending, pend_reqs, results = [], [], {}  # arrived requests: indices and the requests themselves
+        pending, results = [], {}  # unserved arrived requests (indices), in arrival order
         lat = np.full(len(reqs), np.nan)
-        nxt, start = 0, 0
+        nxt, served = 0, 0
         inflight = None
-        while start < len(reqs) or inflight is not None:
+        while served < len(reqs) or inflight is not None:
             now = time.perf_counter() - t0
             while nxt < len(reqs) and (not realtime or reqs[nxt]["t"] <= now):
                 pending.append(nxt)
-                pend_reqs.append(reqs[nxt])
                 nxt += 1
             wave = None
-            if start < len(pending):
+            if pending:
                 if one_by_one:
-                    r = pend_reqs[start]
-                    e, g, end = ([r], [], start + 1) if r["kind"] == EDIT else ([], [r], start + 1)
+                    r = reqs[pending[0]]
+                    e, g, taken = ([r], [], [0]) if r["kind"] == EDIT else ([], [(r, 0)], [0])
                 else:
-                    e, g, end = self.form_wave(pend_reqs, start)
-                if end > start:
-                    wave = (pending[start:end], e, g)
+                    window = pending[:4 * (self.max_e + self.max_g)]
+                    e, g, taken = self.form_wave([reqs[j] for j in window])
+                if taken:
+                    ids = [pending[i] for i in taken]
+                    tk = set(taken)
+                    last = taken[-1]
+                    pending = [p for k, p in enumerate(pending[:last + 1]) if k not in tk] + pending[last + 1:]
+                    served += len(ids)
+                    get_ids = [j for j in ids if reqs[j]["kind"] != EDIT]
+                    wave = (ids, get_ids)
                     ev = self.launch(e, g)
-                    start = end
             if inflight is not None:
-                ids, e_, g_, ev_ = inflight
+                ids_, _, ev_ = inflight
                 ev_.synchronize()
                 done = time.perf_counter() - t0
-                for j in ids:
+                for j in ids_:
                     lat[j] = done - reqs[j]["t"] if realtime else 0.0
                 self.waves += 1
                 if self.waves % 64 == 0:
@@ -276,12 +329,12 @@ class Server:
                     self.alive_est = self.w.stats().alive_nodes
                 inflight = None
             if wave is not None:
-                ids, e, g = wave
-                if keep_results and g:
+                ids, get_ids = wave
+                if keep_results and get_ids:
                     ev.synchronize()
-                    for k, r in enumerate(g):
-                        results[ids[len(e) + k]] = (self.h_found[k].clone().numpy(), self.h_vals[k].clone().numpy())
-                inflight = (ids, e, g, ev)
+                    for k, j in enumerate(get_ids):
+                        results[j] = (self.h_found[k].clone().numpy(), self.h_vals[k].clone().numpy())
+                inflight = (ids, get_ids, ev)
             elif inflight is None and nxt < len(reqs) and realtime:
                 time.sleep(max(0.0, min(0.0005, reqs[nxt]["t"] - (time.perf_counter() - t0))))
         self.w.call("interner_maintain")
