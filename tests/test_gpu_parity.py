@@ -334,3 +334,41 @@ def test_dense_small_depths_in_any_order(oracle_lib, gpu_lib):
         io, to = build_terrain(oracle_lib, grids, depth, bits=bits)
         ig, tg = build_terrain(gpu_lib, grids, depth, bits=bits)
         assert_same(io, ig, to, tg)
+
+
+@pytest.mark.parametrize("bits,depths,patches", [
+    (8, [5, 5, 6], VX_PATCH_P1),
+    (16, [4, 6, 5], VX_PATCH_P1),
+    (8, [3, 4, 2], 0),
+    (8, [7, 5], VX_PATCH_P1 | VX_PATCH_P2),
+])
+def test_batched_set_matches_one_by_one_set(oracle_lib, gpu_lib, bits, depths, patches):
+    """vx_trees_set_many equals VoxTree::set called one voxel at a time in order (the reference's
+    single-voxel path: collapse at every level, removal by value 0): same canonical DAG, refcounts,
+    live nodes and per-call results, on terrain trees whose uniform regions are collapsed leaves,
+    with repeated voxels, unchanged values and removals mixed in."""
+    io, ig = pair(oracle_lib, gpu_lib, 256 << 20, bits, patches)
+    to = [VoxTree(d) for d in depths]
+    tg = [VoxTree(d) for d in depths]
+    dt = np.uint8 if bits == 8 else np.uint16
+    for k, d in enumerate(depths):
+        side = 1 << d
+        g = W.dune_chunks(1, 1, depth=d, seed=70 + k, base=side // 2, amp=max(1, side // 3), scale=side * 1.5,
+                          dtype=dt)[0]
+        io.build_dense([to[k]], g[None])
+        ig.build_dense([tg[k]], g[None])
+    assert_same(io, ig, to, tg)
+    rng = np.random.default_rng(sum(depths) + bits)
+    maxm = 255 if bits == 8 else 4095
+    for rnd in range(3):
+        n = 400
+        t_idx = rng.integers(0, len(depths), n)
+        xyz = np.stack([rng.integers(0, 1 << depths[t], 3) for t in t_idx]).astype(np.int32)
+        xyz[n // 2:n // 2 + 40] = xyz[:40]  # the same voxels again, later in the sequence
+        t_idx[n // 2:n // 2 + 40] = t_idx[:40]
+        vals = rng.integers(1, 4 if rnd == 0 else maxm, n).astype(np.uint32)  # few values first: collapses
+        vals[rng.random(n) < 0.3] = 0
+        cho = [to[t].set(io, tuple(int(c) for c in p), int(v)) for t, p, v in zip(t_idx, xyz, vals)]
+        chg = ig.set_many([tg[t] for t in t_idx], xyz, vals)
+        assert list(cho) == list(chg)
+        assert_same(io, ig, to, tg)

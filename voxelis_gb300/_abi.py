@@ -151,6 +151,7 @@ GPU_SIGNATURES = {
     "get_many_async": [_P, _U64, _P, _P, _P, _P],
     "apply_groups_async": [_P, _U32, _P, _P, _P, _U32, _P, _P, _P, _P, _P, _P, _I],
     "tune_set": [_P, _I, _I],
+    "trees_set_many": [_P, _U64, _P, _P, _P, _P],
     "world_get_async": [_P, _P, _U64, _P, _P, _P],
     "world_hold_async": [_P, _P, _U32, _P, _P, _P, _P, _P],
     "world_get_at_async": [_P, _P, _U64, _P, _P, _P, _P, _P, _U32],

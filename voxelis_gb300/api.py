@@ -225,6 +225,19 @@ class VoxInterner:
                 t._dirty = True
         return out.astype(bool)
 
+    def set_many(self, trees, xyz, values):
+        """VoxOpsWrite::set (voxtree.rs:163-260) for call k = (trees[k], xyz[k], values[k]) in order,
+        in one batched device pass (vx_trees_set_many); returns each call's bool result."""
+        handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        v = np.ascontiguousarray(values, dtype=np.uint32).reshape(-1)
+        out = np.zeros(len(v), dtype=np.uint8)
+        self._call("trees_set_many", C.c_uint64(len(v)), _np_ptr(handles), _np_ptr(p), _np_ptr(v), _np_ptr(out))
+        for t, c in zip(trees, out):
+            if c:
+                t._dirty = True
+        return out.astype(bool)
+
     def export_canonical(self, trees):
         """Canonical DFS export of the DAG reachable from `trees` (see vx_canonical)."""
         handles = np.ascontiguousarray([t._bind(self) for t in trees], dtype=np.uint32)

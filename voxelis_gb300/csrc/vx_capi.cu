@@ -480,7 +480,7 @@ int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass, bool check_de
     return VX_OK;
 }
 
-int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
+int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out, bool point_edits = false) {
     const uint32_t n = (uint32_t)items.size();
     if (n == 0) return VX_OK;
     std::stable_sort(items.begin(), items.end(),
@@ -576,7 +576,9 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
         VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear, R, cudaMemcpyHostToDevice, s));
         VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals, R * 16, cudaMemcpyHostToDevice, s));
     }
-    int st1 = apply_sequence(it, a, any_clear && (it->flags & VX_PATCH_P4));
+    a.point_edits = point_edits ? 1 : 0;
+    // point edits remove voxels as VoxTree::set(pos, 0) does, whatever the patches
+    int st1 = apply_sequence(it, a, any_clear && (point_edits || (it->flags & VX_PATCH_P4)));
     if (st1 != VX_OK) return st1;
     std::vector<uint8_t> ch(n);
     VX_CUDA(cudaMemcpyAsync(ch.data(), a.it_changed, n, cudaMemcpyDeviceToHost, s));
@@ -1226,6 +1228,72 @@ int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *tree
     if (st != VX_OK) return st;
     if (changed_dev) VX_CUDA(cudaMemcpyAsync(changed_dev, a.it_changed, n_items, cudaMemcpyDeviceToDevice, it->stream));
     return VX_OK;
+}
+
+int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const int32_t *xyz, const uint32_t *values,
+                      uint8_t *changed) {
+    if (!it || (n && (!trees || !xyz || !values))) return VX_E_INVALID_ARG;
+    if (n == 0) return VX_OK;
+    bool shallow = false;
+    for (uint64_t k = 0; k < n; ++k) {  // every call is checked before any runs
+        const vx_tree t = trees[k];
+        if (!tree_ok(it, t) || !value_fits(it, values[k])) return set_err(it, VX_E_INVALID_ARG, "bad tree or value");
+        const int32_t side = 1 << it->tree_depth[t];
+        const int32_t x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
+        if (x < 0 || y < 0 || z < 0 || x >= side || y >= side || z >= side)
+            return set_err(it, VX_E_OOB, "position out of bounds");
+        shallow |= it->tree_depth[t] < 2;
+    }
+    if (shallow) {  // MaxDepth 0-1 trees: the one-thread reference sequence, call by call
+        for (uint64_t k = 0; k < n; ++k) {
+            int c = 0;
+            const int st = vx_tree_set(it, trees[k], xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2], values[k], &c);
+            if (st != VX_OK) return st;
+            if (changed) changed[k] = (uint8_t)c;
+        }
+        return VX_OK;
+    }
+    if (changed) {  // call k changes its tree iff the voxel held another value just before it
+        std::vector<uint8_t> found(n);
+        std::vector<uint16_t> vals(n);
+        const int st = vx_get_many(it, n, trees, xyz, found.data(), vals.data(), VX_MEM_HOST);
+        if (st != VX_OK) return st;
+        std::unordered_map<uint64_t, uint32_t> cur;
+        cur.reserve(n * 2);
+        for (uint64_t k = 0; k < n; ++k) {
+            const uint64_t key = ((uint64_t)trees[k] << 32) | morton_encode(xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2]);
+            auto f = cur.find(key);
+            uint32_t before;
+            if (f != cur.end()) {
+                before = f->second;
+            } else {
+                before = found[k] ? (it->vbits == 8 ? (vals[k] & 0xFFu) : vals[k]) : 0u;
+            }
+            changed[k] = before != values[k];
+            cur[key] = values[k];
+        }
+    }
+    // one Batch per tree with its calls in order (the last write to a voxel wins, zero removes)
+    std::unordered_map<vx_tree, uint32_t> slot;
+    std::vector<vx_batch *> bs;
+    std::vector<Item> items;
+    int st = VX_OK;
+    for (uint64_t k = 0; k < n && st == VX_OK; ++k) {
+        const vx_tree t = trees[k];
+        auto f = slot.find(t);
+        if (f == slot.end()) {
+            vx_batch *b = nullptr;
+            st = vx_batch_create(it->tree_depth[t], it->vbits, it->flags | VX_PATCH_P2, &b);
+            if (st != VX_OK) break;
+            f = slot.emplace(t, (uint32_t)bs.size()).first;
+            items.push_back(Item{t, b, (uint32_t)bs.size()});
+            bs.push_back(b);
+        }
+        st = vx_batch_set(bs[f->second], xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2], values[k]);
+    }
+    if (st == VX_OK) st = run_apply(it, items, nullptr, true);
+    for (vx_batch *b : bs) vx_batch_destroy(b);
+    return st;
 }
 
 int vx_tune_set(vx_interner *it, int apply_threads, int apply_blocks_per_sm) {

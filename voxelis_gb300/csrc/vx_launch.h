@@ -51,6 +51,8 @@ cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
 // ---- general batch apply (vx_apply.cu) ---------------------------------------------------------
 struct ApplyArgs {
     int mode;                    // 0: set phase (set_batch_at_depth_iterative); 1: clear pass (P4)
+    int point_edits;             // 1: VoxTree::set semantics for every voxel (set_at_depth_iterative,
+                                 // voxtree.rs:393-540): collapse at every level, exact refcounts
     int threads;                 // launch shape of the bottom/parents kernels
     int blocks_per_sm;
     uint32_t n_items;
