@@ -263,7 +263,7 @@ def measure(args, full_line=False):
         "batched_over_per_chunk": pc_ms / apply_ms,
         "phases_ms_per_step": phases_ms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": B.profiled_traffic("apply_edits_uneven1536.md"),
+                     "traffic": B.profiled_traffic("apply_edits_uneven192.md"),
                      "kernel": "whole apply sequence (bottom groups, level passes, refcount epoch, release)",
                      "algorithmic_bytes": int(algo), "peak_kind": peak_kind},
         "e2e": {"value": n_edits / (e2e_ms * 1e-3), "unit": "edits/s", "ms": e2e_ms,

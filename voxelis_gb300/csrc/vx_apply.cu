@@ -1084,13 +1084,18 @@ cudaError_t launch_apply_single(const DevInterner &I, const ApplyArgs &a, bool c
     int want = a.blocks_per_sm > 0 ? a.blocks_per_sm : per_sm;
     if (want > per_sm) want = per_sm;
     if ((size_t)num_sms * want > apply_single_scan_words(num_sms) - 64) want = 32;  // partials of the grid scan
-    const unsigned grid = (unsigned)(num_sms * want);
+    // a small apply (a serving wave) runs on as few CTAs as its records fill, no fewer than a quarter
+    // of the SMs: every grid barrier costs one arrival per CTA
+    uint64_t grid = (uint64_t)num_sms * want;
+    const uint64_t fill = ((uint64_t)(a.n_records > a.n_items ? a.n_records : a.n_items) + bt - 1) / bt;
+    const uint64_t floor_ctas = (uint64_t)(num_sms + 3) / 4;
+    if (fill < grid) grid = fill > floor_ctas ? fill : floor_ctas;
     DevInterner Ic = I;
     ApplyArgs ac = a;
     int cd = check_depths ? 1 : 0, cp = clear_pass ? 1 : 0;
     void *args[] = {&Ic, &ac, &cd, &cp, &frontier_a, &frontier_b, &rounds};
     count_launches(1);
-    return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(apply_single_kernel), dim3(grid), dim3(bt), args,
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(apply_single_kernel), dim3((unsigned)grid), dim3(bt), args,
                                        smem, s);
 }
 
