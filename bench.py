@@ -369,13 +369,21 @@ def run_ours(args):
     grids_np = np_grids()
     n = grids_np.shape[0]
     stream = torch.cuda.Stream(device=dev)
-    h = C.c_void_p()
-    lib.call("interner_create", C.c_uint64(BUDGET), 8, 0, 0, C.byref(h))
-    call = lambda name, *a: lib.call(name, h, *a, handle=h)  # noqa: E731
-    call("interner_set_stream", C.c_void_p(stream.cuda_stream))
     depths = np.full(n, DEPTH, dtype=np.uint8)
-    trees = np.zeros(n, dtype=np.uint32)
-    call("trees_create", n, depths.ctypes.data, trees.ctypes.data)
+
+    def make(table_log2):
+        """A fresh interner of the workload's budget (table_log2 0: the default branch table) with the
+        workload's trees, on the bench's stream."""
+        hh = C.c_void_p()
+        lib.call("interner_create", C.c_uint64(BUDGET), 8, 0, int(table_log2), C.byref(hh))
+        lib.call("interner_set_stream", hh, C.c_void_p(stream.cuda_stream), handle=hh)
+        tr = np.zeros(n, dtype=np.uint32)
+        lib.call("trees_create", hh, n, depths.ctypes.data, tr.ctypes.data, handle=hh)
+        return hh, tr
+
+    h, trees = make(0)
+    lib.status("interner_destroy", h)
+    call = lambda name, *a: lib.call(name, h, *a, handle=h)  # noqa: E731
 
     with torch.cuda.stream(stream):
         grids = torch.from_numpy(grids_np).to(dev)
@@ -392,6 +400,31 @@ def run_ours(args):
         with torch.cuda.stream(stream):
             flush.fill_(1)
         call("interner_reset")
+
+    # the autotuner picks the branch table's size and the quad memo's geometry on this workload; the
+    # timed interner is then created with them (same trees, same DAG)
+    tune = None
+    if not args.quick:
+        from voxelis_gb300.tune import autotune_dense
+
+        def trial(hh):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            lib.call("interner_reset", hh, handle=hh)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lib.call("build_dense_async", hh, n, C.c_void_p(trees_d.data_ptr()), C.c_void_p(grids.data_ptr()),
+                     C.c_void_p(changed.data_ptr()), DEPTH, handle=hh)
+            e1.record(stream)
+            e1.synchronize()
+            lib.call("interner_sync", hh, handle=hh)
+            return e0.elapsed_time(e1)
+
+        tune = autotune_dense(lib, lambda t: make(t)[0], trial, signature="dunes%d" % n)
+    h, trees2 = make(tune["table_log2"] if tune else 0)
+    assert np.array_equal(trees, trees2)
+    if tune:
+        call("tune_set_dense", tune["memo_shift"])
 
     for _ in range(args.warmup):
         step_prepare()
@@ -533,6 +566,7 @@ def run_ours(args):
         "dtype": "u8",
         "data": "synthetic",
         "config": config({"parallelism": "replicas" if world > 1 else "single"}),
+        "autotune": tune,
         "voxel_edits_per_s": world * grids_np.size / (ms * 1e-3),
         "gets": {"value": N_GETS / (gms * 1e-3), "unit": "gets/s", "ms": gms, "checked_all": gets_ok},
         "per_chunk_gpu": {"value": n / (pc_ms * 1e-3), "unit": "chunks/s", "ms": pc_ms, "same_dag": pc_same},

@@ -241,6 +241,11 @@ int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm);
  * kernel per phase. Results are identical. */
 int vx_tune_set_launch(vx_interner *it, int single_launch);
 int vx_tune_get_launch(vx_interner *it, int *single_launch);
+/* Geometry of the dense builds' quad memo (no counterpart in the reference; autotuned): about the
+ * call's quads >> memo_shift slots (0..8, default 2), half as many records. Results are identical;
+ * the branch table's load factor is chosen at vx_interner_create (table_log2). */
+int vx_tune_set_dense(vx_interner *it, int memo_shift);
+int vx_tune_get_dense(vx_interner *it, int *memo_shift);
 
 /* ---- world helpers for serving (no counterpart in the reference) ---------------------------- */
 /* A grid of nx x ny x nz chunks of depth chunk_depth; the chunk holding world voxel (x, y, z) is

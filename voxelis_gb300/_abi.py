@@ -160,6 +160,8 @@ GPU_SIGNATURES = {
     "tune_get": [_P, _PI, _PI],
     "tune_set_launch": [_P, _I],
     "tune_get_launch": [_P, _PI],
+    "tune_set_dense": [_P, _I],
+    "tune_get_dense": [_P, _PI],
     "trees_to_dense": [_P, _U32, _P, _P, _I],
     "trees_to_dense_async": [_P, _U32, _P, _I, _P],
     "occupancy_masks_async": [_P, _U32, _U32, _P, _P, _P, _I, _U32, _P, _P, _P, _P, _P, _P],

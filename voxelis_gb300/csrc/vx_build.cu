@@ -2009,20 +2009,20 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// Quad memo geometry for a call: slots = a power of two near a quarter of the call's quads (1 Ki to
-// 2 Mi), records = half the slots.
-static void memo_geometry(uint64_t n_chunks, int depth, uint64_t *slots, uint64_t *recs) {
+// Quad memo geometry for a call: slots = a power of two near the call's quads >> shift (a quarter by
+// default; 1 Ki to 2 Mi), records = half the slots.
+static void memo_geometry(uint64_t n_chunks, int depth, uint32_t shift, uint64_t *slots, uint64_t *recs) {
     const uint64_t quads = n_chunks << (3 * (depth - 2));
     uint64_t sl = 1024;
-    while (sl < quads / 4 && sl < (1ull << 21)) sl <<= 1;
+    while (sl < (quads >> shift) && sl < (1ull << 21)) sl <<= 1;
     *slots = sl;
     *recs = sl / 2;
 }
 
-size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits) {
+size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits, uint32_t memo_shift) {
     if (depth < 4) return 0;
     uint64_t sl, rc;
-    memo_geometry(n_chunks, depth, &sl, &rc);
+    memo_geometry(n_chunks, depth, memo_shift, &sl, &rc);
     const size_t stride = memo_stride((size_t)(vbits / 8));
     return sl * 8 + 256 + rc * stride + 256;
 }
@@ -2050,7 +2050,7 @@ cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const 
     }
     if (memo) {
         uint64_t sl, rc;
-        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, &sl, &rc);
+        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, I.memo_shift, &sl, &rc);
         char *m = static_cast<char *>(memo);
         a.memo_slots = reinterpret_cast<unsigned long long *>(m);
         a.memo_count = reinterpret_cast<unsigned int *>(m + sl * 8);
@@ -2143,7 +2143,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     a.grids = grids;
     if (memo) {
         uint64_t sl, rc;
-        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, &sl, &rc);
+        memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, I.memo_shift, &sl, &rc);
         char *m = static_cast<char *>(memo);
         a.memo_slots = reinterpret_cast<unsigned long long *>(m);
         a.memo_count = reinterpret_cast<unsigned int *>(m + sl * 8);

@@ -630,13 +630,13 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
     cudaStream_t s = it->stream;
     if (depth >= 5) {  // quad kernel, then one pass per level
         const size_t sb = (dense_split_scratch_bytes(n, depth) + 255) & ~(size_t)255;
-        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits, it->dev.memo_shift)));
         PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
         VX_CUDA(launch_dense_split(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
                                    static_cast<char *>(it->ws.p) + sb, true, 0, &PhaseSwitch::next, &ps));
     } else if (depth == 4) {  // one warp per chunk
         const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
-        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits)));
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits, it->dev.memo_shift)));
         Phase ph(it, VX_PROF_DENSE);
         VX_CUDA(launch_dense_octants(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
                                      static_cast<char *>(it->ws.p) + sb));
@@ -730,6 +730,7 @@ int vx_interner_create(uint64_t budget_bytes, int voxel_bits, uint32_t patch_fla
     D.max_probes = (uint32_t)std::min<uint64_t>(slots, 1u << 16);
     D.round_limit = ROUND_LIMIT;
     D.spin_limit = SPIN_LIMIT;
+    D.memo_shift = 2;
     const size_t vb = voxel_bits / 8;
     bool ok = true;
     auto alloc = [&](void **p, size_t bytes) {
@@ -1312,6 +1313,19 @@ int vx_tune_get(vx_interner *it, int *apply_threads, int *apply_blocks_per_sm) {
     return VX_OK;
 }
 
+int vx_tune_set_dense(vx_interner *it, int memo_shift) {
+    if (!it || memo_shift < 0 || memo_shift > 8) return VX_E_INVALID_ARG;
+    VX_CUDA(cudaStreamSynchronize(it->stream));  // queued builds keep the geometry they were given
+    it->dev.memo_shift = (uint32_t)memo_shift;
+    return VX_OK;
+}
+
+int vx_tune_get_dense(vx_interner *it, int *memo_shift) {
+    if (!it || !memo_shift) return VX_E_INVALID_ARG;
+    *memo_shift = (int)it->dev.memo_shift;
+    return VX_OK;
+}
+
 int vx_tune_set_launch(vx_interner *it, int single_launch) {
     if (!it || (single_launch != 0 && single_launch != 1)) return VX_E_INVALID_ARG;
     it->apply_single = single_launch;
@@ -1408,7 +1422,7 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
         const bool split = d >= 5;
         const size_t sb = ((split ? dense_split_scratch_bytes(n, d) : dense_octant_scratch_bytes(n, d)) + 255) &
                           ~(size_t)255;
-        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, d, it->vbits)));
+        VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, d, it->vbits, it->dev.memo_shift)));
         char *memo = static_cast<char *>(it->ws.p) + sb;
         cudaStream_t s = it->stream;
         {

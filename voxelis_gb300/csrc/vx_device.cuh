@@ -90,6 +90,7 @@ struct DevInterner {
     uint32_t max_probes;   // branch-table probes before ERR_TABLE_FULL
     uint32_t round_limit;  // warp-intern rounds before ERR_TIMEOUT
     uint32_t spin_limit;   // iterations of a wait on another thread before ERR_TIMEOUT
+    uint32_t memo_shift;   // dense builds: quad-memo slots ~ the call's quads >> memo_shift (tunable)
 };
 
 // ---- BlockId (core/block_id.rs:19-418) -------------------------------------------------------

@@ -31,7 +31,7 @@ cudaError_t launch_dense_blocks(const DevInterner &I, const DenseArgs &a, int nu
 // between, so every node it names is still alive). memo_chunks (0: n_chunks) sizes the memo and must
 // be the same for every piece that shares it.
 size_t dense_octant_scratch_bytes(uint64_t n_chunks, int depth);
-size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits);
+size_t dense_octant_memo_bytes(uint64_t n_chunks, int depth, int vbits, uint32_t memo_shift);
 cudaError_t launch_dense_octants(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                  int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s,
                                  void *memo = nullptr, bool clear_memo = true, uint64_t memo_chunks = 0);

@@ -55,3 +55,48 @@ def autotune_apply(lib, handle, reset, trial, signature="default", repeats=2):
     os.makedirs(os.path.dirname(CACHE), exist_ok=True)
     json.dump(cache, open(CACHE, "w"), indent=1)
     return {"single_launch": single, "threads": threads, "blocks_per_sm": bps, "trials_ms": results}
+
+
+# dense builds: the branch table's size relative to the default (2 x capacity, rounded up to a power
+# of two: load factor at most 1/2) and the quad memo's slots (the call's quads >> shift)
+TABLE_STEPS = (-1, 0, 1)
+MEMO_SHIFTS = (1, 2, 3)
+
+
+def autotune_dense(lib, make, build, signature="dense", repeats=3):
+    """Tries branch-table sizes (load factor) and quad-memo geometries on the caller's own dense
+    build. make(table_log2) returns a fresh interner handle (table_log2 0: the default size) with the
+    caller's trees; build(handle) resets it, runs one build and returns milliseconds. Returns the
+    fastest {table_log2, memo_shift, trials_ms} and caches it; the caller recreates its interner
+    with that table size and applies the shift with vx_tune_set_dense."""
+    import ctypes as C
+
+    from ._abi import vx_interner_stats
+
+    key = "%s|%s" % (_gpu_name(), signature)
+    results = {}
+    h0 = make(0)
+    st = vx_interner_stats()
+    lib.call("interner_stats_get", h0, C.byref(st), handle=h0)
+    lib.status("interner_destroy", h0)
+    default_log2 = int(st.table_slots).bit_length() - 1
+    for step in TABLE_STEPS:
+        t_log2 = default_log2 + step
+        h = make(t_log2)
+        for shift in MEMO_SHIFTS:
+            lib.call("tune_set_dense", h, shift, handle=h)
+            results["t%d:m%d" % (t_log2, shift)] = min(build(h) for _ in range(repeats))
+        lib.status("interner_destroy", h)
+    choice = min(results, key=results.get)
+    t_log2, shift = (int(v[1:]) for v in choice.split(":"))
+    out = {"table_log2": t_log2, "default_table_log2": default_log2, "memo_shift": shift, "trials_ms": results}
+    cache = {}
+    if os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except ValueError:
+            cache = {}
+    cache[key] = out
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    json.dump(cache, open(CACHE, "w"), indent=1)
+    return out
