@@ -209,7 +209,45 @@ def run(args):
     o_ms = (time.perf_counter() - t0) * 1e3
     ol.status("interner_destroy", oh)
     call("interner_destroy")
+    from voxelis_gb300.api import export_canonical
     from voxelis_gb300.vtm import canonical, decode
+
+    # model deserialisation of the same payload into a fresh interner (VoxModel::deserialize), GPU vs
+    # oracle: per call the host bytes go to the device, are parsed there and the nodes placed
+    h2 = C.c_void_p()
+    lib.call("interner_create", C.c_uint64(256 << 20), 8, 0, 0, C.byref(h2))
+    d_trees = np.zeros(n, np.uint32)
+    d_pos = np.zeros((n, 3), np.int32)
+    d_n = C.c_uint32()
+    des = []
+    for _ in range(5):
+        lib.call("interner_reset", h2, handle=h2)
+        t0 = time.perf_counter()
+        lib.call("deserialize_model", h2, C.c_void_p(blob.ctypes.data), C.c_uint64(size.value), 5, n,
+                 C.c_void_p(d_trees.ctypes.data), C.c_void_p(d_pos.ctypes.data), C.byref(d_n), handle=h2)
+        des.append(time.perf_counter() - t0)
+        if _ < 4:
+            for t in d_trees:
+                lib.call("tree_destroy", h2, int(t), handle=h2)
+    des_ms = statistics.median(des) * 1e3
+    oh = C.c_void_p()
+    ol.call("interner_create", C.c_uint64(256 << 20), 8, 0, 0, C.byref(oh))
+    o_dt = np.zeros(n, np.uint32)
+    o_dp = np.zeros((n, 3), np.int32)
+    t0 = time.perf_counter()
+    ol.call("deserialize_model", oh, C.c_void_p(blob.ctypes.data), C.c_uint64(size.value), 5, n,
+            C.c_void_p(o_dt.ctypes.data), C.c_void_p(o_dp.ctypes.data), C.byref(d_n), handle=oh)
+    o_des_ms = (time.perf_counter() - t0) * 1e3
+    cg, co = export_canonical(lib, h2, d_trees), export_canonical(ol, oh, o_dt)
+    des_equal = bool(np.array_equal(d_pos, o_dp) and all(np.array_equal(cg[k], co[k]) for k in co))
+    re = np.zeros(size.value, np.uint8)
+    lib.call("serialize_model", h2, n, C.c_void_p(d_trees.ctypes.data), C.c_void_p(d_pos.ctypes.data),
+             C.c_void_p(re.ctypes.data), C.c_uint64(size.value), C.byref(size), handle=h2)
+    ol.status("interner_destroy", oh)
+    lib.status("interner_destroy", h2)
+    deserialize = {"bytes": int(size.value), "ms": des_ms, "MB_per_s": size.value / (des_ms * 1e-3) / 1e6,
+                   "oracle_equal": des_equal, "round_trip_bytes_equal": bool(np.array_equal(re, blob)),
+                   "cpu_baseline": {"ms": o_des_ms, "cores": 1, "kind": "port", "sample": "the same payload"}}
 
     same_model = canonical(*decode(blob.tobytes(), 1)) == canonical(*decode(o_blob.tobytes(), 1))
     serialize = {"bytes": int(size.value), "ms": ser_ms, "MB_per_s": size.value / (ser_ms * 1e-3) / 1e6,
@@ -223,7 +261,7 @@ def run(args):
             "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "chunks/s", "ms": e2e_ms, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(out_bytes)},
             "per_builder_gpu": {"value": n / per_builder_s, "unit": "chunks/s", "same_as_batched": bool(same)},
-            "checked_against_oracle": bool(ok), "serialize_model": serialize,
+            "checked_against_oracle": bool(ok), "serialize_model": serialize, "deserialize_model": deserialize,
             "cpu_baseline": {"value": 4 * len(sample) / cpu_s, "unit": "chunks/s", "cores": 1, "kind": "port",
                              "sample": "%d builders (generate_occupancy_masks per chunk, one thread)" % len(sample)}}
     print(json.dumps(line))

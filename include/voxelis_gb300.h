@@ -330,6 +330,23 @@ int vx_occupancy_masks_async(vx_interner *it, uint32_t n_builders, uint32_t n_tr
 int vx_serialize_model(vx_interner *it, uint32_t n_chunks, const vx_tree *trees, const int32_t *positions,
                        uint8_t *out, uint64_t capacity, uint64_t *size);
 
+/* Model deserialisation (VoxModel::deserialize, world/voxmodel.rs:284-408, with deserialize_leaf /
+ * preallocate_branch_id / deserialize_branch, interner/mod.rs:930-993, and deserialize_chunk,
+ * world/voxchunk.rs:408-440) of the payload vx_serialize_model writes, parsed on the device. Record ids
+ * are slots: leaf k lands on slot k, branch L+k on slot L+k, with generation 0. Refcounts are the
+ * reference's: one per child slot naming a node (inc_all_child_refs), plus one per chunk root
+ * (set_root_id; an EMPTY root counts on the EMPTY slot). Both hash tables hold every pattern. One
+ * tree of depth max_depth is created per chunk record, in stream order: out_trees[k] at
+ * out_positions[3k..3k+2] (x, y, z); repeated positions give one tree each.
+ * VX_E_REF_PANIC where the reference panics: a stream that ends early, an id out of sequence or
+ * naming no node, a branch with an empty mask, a zero-valued leaf (a debug assertion there), the
+ * wrong chunk magic, or records while the interner already holds nodes (its ids must be the next
+ * indices allocated). The interner is left unchanged then. VX_E_OOM when L + B nodes exceed the
+ * capacity. VX_E_BUFFER when the stream holds more than max_chunks chunks; *out_n_chunks is set and
+ * nothing is created. Host memory; streams below 4 GiB. */
+int vx_deserialize_model(vx_interner *it, const uint8_t *data, uint64_t n_bytes, int max_depth, uint32_t max_chunks,
+                         vx_tree *out_trees, int32_t *out_positions, uint32_t *out_n_chunks);
+
 /* ---- verification helpers (not on the timed path) ---------------------------------------- */
 /* Canonical DFS export of the DAG reachable from `trees` (see vx_canonical). On VX_E_BUFFER
  * *n_nodes holds the required capacity. */

@@ -504,6 +504,36 @@ class Interner {
         return id;
     }
 
+    // preallocate_branch_id (mod.rs:930-941): the record's index must be the next one allocated, on
+    // a slot never recycled.
+    uint64_t preallocate_branch_id(uint32_t index, uint8_t types, uint8_t mask) {
+        if (get_next_index() != index) throw RefPanic("Invalid block id");
+        if (generations_[index] != 0) throw RefPanic("Invalid generation");
+        return bid::new_branch(index, 0, types, mask);
+    }
+    // deserialize_leaf (mod.rs:943-968); the default-value check is the reference's debug assertion.
+    uint64_t deserialize_leaf(uint32_t index, T value) {
+        if (value == T(0)) throw RefPanic("Leaf value should not be default");
+        const uint64_t hash = compute_leaf_hash(value);
+        if (get_next_index() != index) throw RefPanic("Invalid block id");
+        if (generations_[index] != 0) throw RefPanic("Invalid generation");
+        const uint64_t id = bid::new_leaf(index, 0);
+        values_[index] = value;
+        hashes_[index] = hash;
+        patterns_[1].insert(hash, id);
+        return id;
+    }
+    // deserialize_branch (mod.rs:970-993), with inc_all_child_refs (mod.rs:328-356).
+    void deserialize_branch(uint64_t id, const Children &c, uint8_t types, uint8_t mask, T average) {
+        const uint64_t hash = compute_branch_hash(c, types, mask);
+        const uint32_t i = bid::index(id);
+        children_[i] = c;
+        values_[i] = average;
+        hashes_[i] = hash;
+        patterns_[0].insert(hash, id);
+        inc_child_refs(c, 8);
+    }
+
    private:
     uint32_t checked(uint64_t id) const {
         uint32_t i = bid::index(id);
@@ -851,6 +881,11 @@ class Tree {
 
     // The tree holds one reference to its root (set_root_id, voxtree.rs:136-142).
     void set_root_raw(uint64_t r) { root_ = r; }
+    // set_root_id (voxtree.rs:135-141): counts a reference on the new root, EMPTY included.
+    void set_root_id(Interner<T> &it, uint64_t r) {
+        root_ = r;
+        it.inc_ref(r);
+    }
 
     static void decode_path(uint32_t path, int d, int32_t *x, int32_t *y, int32_t *z) {
         int32_t px = 0, py = 0, pz = 0;

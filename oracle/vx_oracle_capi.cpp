@@ -164,6 +164,43 @@ int with_batch(void *h, F f) {
 
 }  // namespace
 
+// Big-endian reader of a serialised model (the reference reads through byteorder / BufReader).
+namespace {
+struct Reader {
+    const uint8_t *b;
+    uint64_t n, p = 0;
+    void need(uint64_t k) const {
+        if (p + k > n) throw vxo::RefPanic("unexpected end of the stream");
+    }
+    uint8_t u8() {
+        need(1);
+        return b[p++];
+    }
+    uint32_t u32() {
+        need(4);
+        uint32_t v = ((uint32_t)b[p] << 24) | ((uint32_t)b[p + 1] << 16) | ((uint32_t)b[p + 2] << 8) | b[p + 3];
+        p += 4;
+        return v;
+    }
+    // decode_varint_u32_from_reader (io/varint.rs:47-69)
+    uint32_t varint() {
+        uint32_t r = 0;
+        for (int shift = 0;; shift += 7) {
+            const uint8_t c = u8();
+            r |= (uint32_t)(c & 0x7F) << shift;
+            if (c < 0x80) return r;
+            if (shift + 7 >= 32) throw vxo::RefPanic("varint longer than 5 bytes");
+        }
+    }
+    template <class T>
+    T value() {
+        uint32_t v = 0;
+        for (size_t k = 0; k < sizeof(T); ++k) v = (v << 8) | u8();
+        return (T)v;
+    }
+};
+}  // namespace
+
 extern "C" {
 
 int vxo_interner_create(uint64_t budget, int bits, uint32_t flags, int table_log2, void **out) {
@@ -567,6 +604,114 @@ int vxo_serialize_model(void *h, uint32_t n_chunks, const uint32_t *trees, const
         if (!out) return VX_OK;
         if (capacity < b.size()) return fail(&o, VX_E_BUFFER, "output buffer smaller than the serialised model");
         std::copy(b.begin(), b.end(), out);
+        return VX_OK;
+    });
+}
+
+// VoxModel::deserialize (world/voxmodel.rs:284-408) and deserialize_chunk (world/voxchunk.rs:408-440):
+// reads records in stream order with the reference's checks (every read past the end is an unwrap
+// panic). Before anything is interned, one read-only walk of the same layout finds the chunk count,
+// so that VX_E_BUFFER leaves the interner unchanged, as the C ABI promises.
+
+int vxo_deserialize_model(void *h, const uint8_t *data, uint64_t n_bytes, int max_depth, uint32_t max_chunks,
+                          uint32_t *out_trees, int32_t *out_positions, uint32_t *out_n_chunks) {
+    return with_interner(h, [&](auto &o) {
+        using T = std::decay_t<decltype(o.it.get_value(0))>;
+        using TreeT = std::remove_reference_t<decltype(*o.trees[0])>;
+        if (!out_n_chunks || (n_bytes && !data)) return VX_E_INVALID_ARG;
+        *out_n_chunks = 0;
+        TreeT probe(max_depth, o.flags);  // MaxDepth::new (max_depth.rs:77-83)
+        (void)probe;
+        {  // the layout walk
+            Reader r{data, n_bytes};
+            for (uint32_t k = 0, L = r.u32(); k < L; ++k) {
+                r.varint();
+                r.template value<T>();
+            }
+            for (uint32_t k = 0, B = r.u32(); k < B; ++k) {
+                r.varint();
+                const uint8_t mask = r.u8();
+                for (int j = 0; j < 8; ++j)
+                    if (mask >> j & 1) r.varint();
+                r.template value<T>();
+            }
+            const uint32_t C = r.u32();
+            *out_n_chunks = C;
+            if (C > max_chunks) return fail(&o, VX_E_BUFFER, "more chunks in the stream than max_chunks");
+            if (C && (!out_trees || !out_positions)) return VX_E_INVALID_ARG;
+        }
+        Reader r{data, n_bytes};
+        const uint32_t L = r.u32();
+        std::unordered_map<uint32_t, uint64_t> leaf_patterns;
+        for (uint32_t k = 0; k < L; ++k) {
+            const uint32_t id = r.varint();
+            const T value = r.template value<T>();
+            leaf_patterns[id] = o.it.deserialize_leaf(id, value);
+        }
+        struct Pattern {
+            uint64_t id;
+            uint32_t children[8];
+            T lod;
+        };
+        const uint32_t B = r.u32();
+        std::unordered_map<uint32_t, Pattern> branch_patterns;
+        branch_patterns[0] = Pattern{vxo::bid::EMPTY, {}, T(0)};
+        std::vector<uint32_t> order;
+        for (uint32_t k = 0; k < B; ++k) {
+            const uint32_t id = r.varint();
+            if (id == 0) throw vxo::RefPanic("assert_ne!(id, 0)");
+            const uint8_t mask = r.u8();
+            uint8_t types = 0;
+            Pattern p{0, {}, T(0)};
+            for (int j = 0; j < 8; ++j) {
+                if (!(mask >> j & 1)) continue;
+                p.children[j] = r.varint();
+                if (leaf_patterns.count(p.children[j])) types |= (uint8_t)(1u << j);
+            }
+            p.lod = r.template value<T>();
+            p.id = o.it.preallocate_branch_id(id, types, mask);
+            branch_patterns[id] = p;
+            order.push_back(id);
+            if (mask == 0) throw vxo::RefPanic("assert_ne!(mask, 0)");
+        }
+        for (uint32_t id : order) {  // the reference walks its map; the result does not depend on the order
+            const Pattern &p = branch_patterns.at(id);
+            const uint8_t types = (uint8_t)vxo::bid::types(p.id), mask = (uint8_t)vxo::bid::mask(p.id);
+            vxo::Children c{};
+            for (int j = 0; j < 8; ++j) {
+                if (!(mask >> j & 1)) continue;
+                auto leaf = leaf_patterns.find(p.children[j]);
+                if (types >> j & 1) {
+                    c[j] = leaf->second;
+                } else {
+                    auto br = branch_patterns.find(p.children[j]);
+                    if (br == branch_patterns.end()) throw vxo::RefPanic("child id names no pattern");
+                    c[j] = br->second.id;
+                }
+            }
+            o.it.deserialize_branch(p.id, c, types, mask, p.lod);
+        }
+        const uint32_t C = r.u32();
+        static const char magic[12] = {'V', 'o', 'x', 'T', 'r', 'e', 'e', 'C', 'h', 'u', 'n', 'k'};
+        for (uint32_t k = 0; k < C; ++k) {
+            for (int j = 0; j < 12; ++j)
+                if (r.u8() != (uint8_t)magic[j]) throw vxo::RefPanic("assert_eq!(magic, VTC_MAGIC)");
+            for (int a = 0; a < 3; ++a) out_positions[3 * k + a] = (int32_t)r.u32();
+            const uint32_t root = r.varint();
+            uint64_t block;
+            auto br = branch_patterns.find(root);
+            if (br != branch_patterns.end()) {
+                block = br->second.id;
+            } else {
+                auto leaf = leaf_patterns.find(root);
+                if (leaf == leaf_patterns.end()) throw vxo::RefPanic("root id names no pattern");
+                block = leaf->second;
+            }
+            uint32_t slot;
+            if (int st = vxo_tree_create(&o, max_depth, &slot)) return st;
+            o.tree(slot)->set_root_id(o.it, block);
+            out_trees[k] = slot;
+        }
         return VX_OK;
     });
 }

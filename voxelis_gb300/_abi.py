@@ -134,6 +134,7 @@ SIGNATURES = {
     "validate": [_P, _U32, _P],
     "occupancy_masks": [_P, _U32, _P, _P, _P, _P, _U32, _P, _P, _P, _P],
     "serialize_model": [_P, _U32, _P, _P, _P, _U64, _PU64],
+    "deserialize_model": [_P, _P, _U64, _I, _U32, _P, _P, C.POINTER(C.c_uint32)],
 }
 
 # entry points only the GPU library has

@@ -213,6 +213,28 @@ class VoxInterner:
                    C.c_uint64(size.value), C.byref(size))
         return out.tobytes()
 
+    def deserialize_model(self, data, max_depth):
+        """VoxModel::deserialize (world/voxmodel.rs:284-408) of a payload into this interner, which
+        must hold no nodes yet: returns (trees, positions), one VoxTree of MaxDepth max_depth per chunk
+        record in stream order and an int32 [C, 3] array of their positions."""
+        buf = np.frombuffer(bytes(data), np.uint8)
+        n = C.c_uint32()
+        st = self.lib.status("deserialize_model", self.handle, _np_ptr(buf), C.c_uint64(len(buf)), int(max_depth), 0,
+                             None, None, C.byref(n))
+        if st not in (_abi.VX_OK, _abi.VX_E_BUFFER):
+            raise _abi.error_for(st, self.lib.last_error(self.handle))
+        handles = np.zeros(max(1, n.value), np.uint32)
+        pos = np.zeros((max(1, n.value), 3), np.int32)
+        if st == _abi.VX_E_BUFFER:
+            self._call("deserialize_model", _np_ptr(buf), C.c_uint64(len(buf)), int(max_depth), n.value,
+                       _np_ptr(handles), _np_ptr(pos), C.byref(n))
+        trees = []
+        for h in handles[:n.value]:
+            t = VoxTree(max_depth)
+            t.interner, t.tree, t._dirty = self, int(h), True
+            trees.append(t)
+        return trees, pos[:n.value].copy()
+
     def apply_batches(self, trees, batches):
         """n apply_batch calls in one batched device pass; returns the changed flags."""
         n = len(trees)

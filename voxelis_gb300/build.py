@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libvoxelis_gb300.so")
-SOURCES = ["vx_build.cu", "vx_apply.cu", "vx_ops.cu", "vx_capi.cu", "vx_noalloc.cu", "vx_world.cu"]
+SOURCES = ["vx_build.cu", "vx_apply.cu", "vx_ops.cu", "vx_capi.cu", "vx_noalloc.cu", "vx_world.cu", "vx_vtm.cu"]
 HEADERS = ["vx_device.cuh", "vx_launch.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

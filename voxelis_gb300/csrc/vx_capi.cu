@@ -1256,7 +1256,7 @@ int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const i
     }
     if (changed) {  // call k changes its tree iff the voxel held another value just before it
         std::vector<uint8_t> found(n);
-        std::vector<uint16_t> vals(n);
+        std::vector<uint8_t> vals(n * (it->vbits / 8));  // u8 or u16 per value, as vx_get_many writes them
         const int st = vx_get_many(it, n, trees, xyz, found.data(), vals.data(), VX_MEM_HOST);
         if (st != VX_OK) return st;
         std::unordered_map<uint64_t, uint32_t> cur;
@@ -1268,7 +1268,9 @@ int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const i
             if (f != cur.end()) {
                 before = f->second;
             } else {
-                before = found[k] ? (it->vbits == 8 ? (vals[k] & 0xFFu) : vals[k]) : 0u;
+                uint16_t v16 = 0;
+                if (it->vbits == 16) std::memcpy(&v16, vals.data() + 2 * k, 2);
+                before = found[k] ? (it->vbits == 8 ? (uint32_t)vals[k] : (uint32_t)v16) : 0u;
             }
             changed[k] = before != values[k];
             cur[key] = values[k];
@@ -1821,6 +1823,75 @@ int vx_serialize_model(vx_interner *it, uint32_t n_chunks, const vx_tree *trees,
         VX_CUDA(launch_serialize_write(it->dev, w, n_chunks, dt, dp, dout, dtotal, it->num_sms, s));
     }
     VX_CUDA(cudaMemcpyAsync(out, dout, total, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(it);
+}
+
+// VoxModel::deserialize (world/voxmodel.rs:284-408) into an interner without nodes: the stream is
+// parsed on the device (launch_vtm_parse); the host reads back the three counts, creates the chunk
+// trees and launches the placement of the nodes, refcounts and roots (launch_vtm_place).
+int vx_deserialize_model(vx_interner *it, const uint8_t *data, uint64_t n_bytes, int max_depth, uint32_t max_chunks,
+                         vx_tree *out_trees, int32_t *out_positions, uint32_t *out_n_chunks) {
+    if (!it || !out_n_chunks || (n_bytes && !data)) return VX_E_INVALID_ARG;
+    *out_n_chunks = 0;
+    if (max_depth < 0 || max_depth >= depth_limit(it->flags))
+        return set_err(it, VX_E_DEPTH, "Max depth exceeds allowed limit");
+    if (n_bytes < 4) return set_err(it, VX_E_REF_PANIC, "stream too short for its leaf count");
+    if (n_bytes >= 0xFFFFFFFFull) return set_err(it, VX_E_UNSUPPORTED, "streams of 4 GiB or more");
+    int st = sync_and_check(it);
+    if (st != VX_OK) return st;
+    const unsigned long long ni = it->h_ctr->next_index, fc = it->h_ctr->free_count;
+    const VtmScratchSizes z = vtm_scratch_sizes(n_bytes);
+    const uint64_t chunk_room = std::min<uint64_t>(max_chunks, z.chunk_cap);  // a chunk record takes 25+ bytes
+    VX_CUDA(it->staging.reserve(n_bytes + 64));
+    VX_CUDA(it->ws.reserve(Carve::need({sizeof(VtmSections), z.table_words * 8, z.entry_words * 8, z.leaf_cap * 4,
+                                        z.branch_cap * 4, z.chunk_cap * 4, chunk_room * 4 + 4, chunk_room * 12 + 4})));
+    Carve c(it->ws.p);
+    VtmSections *sec = c.take<VtmSections>(1);
+    uint64_t *tables = c.take<uint64_t>(z.table_words);
+    uint64_t *entries = c.take<uint64_t>(z.entry_words);
+    uint32_t *leaf_off = c.take<uint32_t>(z.leaf_cap);
+    uint32_t *branch_off = c.take<uint32_t>(z.branch_cap);
+    uint32_t *chunk_off = c.take<uint32_t>(z.chunk_cap);
+    uint32_t *d_trees = c.take<uint32_t>(chunk_room + 1);
+    int32_t *d_pos = c.take<int32_t>(chunk_room * 3 + 1);
+    uint8_t *bytes = static_cast<uint8_t *>(it->staging.p);
+    cudaStream_t s = it->stream;
+    VtmSections h{};
+    h.start[0] = 4;
+    h.count[0] = ((uint32_t)data[0] << 24) | ((uint32_t)data[1] << 16) | ((uint32_t)data[2] << 8) | data[3];
+    h.start[1] = h.start[2] = h.start[3] = ~0ull;
+    VX_CUDA(cudaMemcpyAsync(bytes, data, n_bytes, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(sec, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    {
+        Phase ph(it, VX_PROF_GET);
+        VX_CUDA(launch_vtm_parse(it->dev, bytes, n_bytes, sec, tables, entries, leaf_off, branch_off, chunk_off,
+                                 it->num_sms, s));
+    }
+    VX_CUDA(cudaMemcpyAsync(&h, sec, sizeof(h), cudaMemcpyDeviceToHost, s));
+    st = sync_and_check(it);
+    if (st != VX_OK) return st;
+    for (int k = 0; k < 3; ++k)
+        if (!h.done[k]) return set_err(it, VX_E_REF_PANIC, "stream ends inside section " + std::to_string(k));
+    const uint64_t nodes = h.count[0] + h.count[1], C = h.count[2];
+    // deserialize_leaf / preallocate_branch_id assert that each id is the next index allocated
+    // (interner/mod.rs:930-968): with nodes in the stream the interner must hold none yet
+    if (nodes && (ni != 1 || fc != 0))
+        return set_err(it, VX_E_REF_PANIC, "deserialize needs an interner without nodes (Invalid block id)");
+    if (nodes + 1 > it->capacity) return set_err(it, VX_E_OOM, "Out of memory: node capacity exhausted");
+    *out_n_chunks = (uint32_t)C;
+    if (C > max_chunks) return set_err(it, VX_E_BUFFER, "more chunks in the stream than max_chunks");
+    if (C && (!out_trees || !out_positions)) return VX_E_INVALID_ARG;
+    std::vector<uint8_t> depths(C, (uint8_t)max_depth);
+    st = vx_trees_create(it, (uint32_t)C, depths.data(), out_trees);
+    if (st != VX_OK) return st;
+    if (C) VX_CUDA(cudaMemcpyAsync(d_trees, out_trees, C * 4, cudaMemcpyHostToDevice, s));
+    {
+        Phase ph(it, VX_PROF_GET);
+        VX_CUDA(launch_vtm_place(it->dev, bytes, sec, nodes, h.count[1] + C, leaf_off, branch_off, chunk_off, d_trees,
+                                 d_pos, it->num_sms, s));
+    }
+    if (C) VX_CUDA(cudaMemcpyAsync(out_positions, d_pos, C * 12, cudaMemcpyDeviceToHost, s));
+    for (uint64_t k = 0; k < C; ++k) it->tree_maybe_nonempty[out_trees[k]] = 1;
     return sync_and_check(it);
 }
 

@@ -147,6 +147,36 @@ cudaError_t launch_serialize_plan(const DevInterner &I, uint32_t *w, uint32_t *t
 cudaError_t launch_serialize_write(const DevInterner &I, uint32_t *w, uint32_t n_chunks, const uint32_t *trees,
                                    const int32_t *pos, uint8_t *out, unsigned long long *total, int num_sms,
                                    cudaStream_t s);
+
+// ---- model deserialisation (vx_vtm.cu) -------------------------------------------------------
+// Section state of one parse, in device memory: sections 0 leaves, 1 branches, 2 chunks. The host
+// sets start[0] = 4 and count[0] = the leaf count, start[1..3] = ~0 (unknown), the other counts and
+// done[] = 0; each section's last record sets the next section's start and count and done[kind].
+struct VtmSections {
+    unsigned long long start[4];  // first byte of section k's records; start[3] = end of the chunks
+    unsigned long long count[3];  // records announced by section k's header
+    unsigned long long done[3];   // 1 once section k's last record was found
+};
+struct VtmScratchSizes {
+    uint32_t seg_bytes;
+    uint64_t n0, n1, n2;                     // tables per level (upper bounds)
+    uint64_t table_words, entry_words;       // u64 words of the tables and the entry states
+    uint64_t leaf_cap, branch_cap, chunk_cap;  // u32 record offsets per section (upper bounds)
+};
+uint32_t vtm_segment_bytes(uint64_t n_bytes);
+VtmScratchSizes vtm_scratch_sizes(uint64_t n_bytes);
+// Parses the three sections of `bytes` (device memory, n_bytes < 2^32): record offsets by rank into
+// leaf_off / branch_off / chunk_off, counts into sec. A stream the reference panics on sets
+// ERR_REF_PANIC and leaves done[] of the failing section 0.
+cudaError_t launch_vtm_parse(const DevInterner &I, const uint8_t *bytes, uint64_t n_bytes, VtmSections *sec,
+                             uint64_t *tables, uint64_t *entries, uint32_t *leaf_off, uint32_t *branch_off,
+                             uint32_t *chunk_off, int num_sms, cudaStream_t s);
+// Writes the parsed nodes into an interner that holds none (slots 1..L+B), the branch table, the
+// refcounts and the roots of trees[k] (k < C), with the chunk positions into positions[3k..3k+2].
+cudaError_t launch_vtm_place(const DevInterner &I, const uint8_t *bytes, const VtmSections *sec, uint64_t n_nodes,
+                             uint64_t n_links, const uint32_t *leaf_off, const uint32_t *branch_off,
+                             const uint32_t *chunk_off, const uint32_t *trees, int32_t *positions, int num_sms,
+                             cudaStream_t s);
 // Releases the roots listed in `list` (count at ctr->scratch[SC_RELEASE]) with `rounds`
 // breadth-first rounds, using two frontier buffers of `frontier_cap` entries.
 cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *frontier_a, uint32_t *frontier_b,
