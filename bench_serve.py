@@ -16,7 +16,7 @@ import numpy as np
 from voxelis_gb300 import workloads as W
 from voxelis_gb300.serve import EDIT, Server, World, make_trace
 
-RATES = (1000, 2000, 5000, 10000, 20000)
+RATES = (1000, 2000, 5000, 10000, 20000, 40000)
 WORKLOAD = "served world 64x4x64 chunks of 64^3 u8, 16 GiB budget, Poisson 70/30 edits/gets, P1+P4+P5"
 
 
@@ -68,11 +68,18 @@ def measure(args, full_line=False):
     out["clocks"] = clocks.stop()
     st = world.stats()
     out["nodes_alive"] = int(st.alive_nodes)
+    # the headline: p99 at the highest offered rate that is sustained (served >= 95% of offered) with
+    # p99 <= 2 ms; beside it the highest sustained rate whatever its p99, and the most served
     held = [r for r in out["rates"] if r["served_req_per_s"] >= 0.95 * r["offered_req_per_s"]]
-    best = max(held, key=lambda r: r["offered_req_per_s"]) if held else out["rates"][0]
+    within = [r for r in held if r["edit_p99_ms"] <= 2.0]
+    best = max(within or held or out["rates"][:1], key=lambda r: r["offered_req_per_s"])
     out["value"] = best["edit_p99_ms"]
     out["at_rate"] = best["offered_req_per_s"]
     out["roofline_frac_at_rate"] = best["roofline_frac"]
+    if held:
+        top = max(held, key=lambda r: r["offered_req_per_s"])
+        out["highest_sustained"] = {"offered_req_per_s": top["offered_req_per_s"], "edit_p99_ms": top["edit_p99_ms"]}
+    out["max_served_req_per_s"] = max(r["served_req_per_s"] for r in out["rates"])
     world.close()
     if full_line:
         out.update({"n_gpus": 1, "steps": len(RATES), "warmup": 1, "dtype": "u8", "data": "synthetic",

@@ -225,10 +225,10 @@ int vx_apply_groups_async(vx_interner *it, uint32_t n_items, const vx_tree *tree
 /* Batched VoxOpsWrite::set (voxtree.rs:163-260 with set_at_depth_iterative and remove_at_depth,
  * voxtree.rs:373-705): the same result as calling vx_tree_set(trees[k], xyz[3k..3k+2], values[k])
  * for k = 0 .. n-1 in order (value 0 removes the voxel; the DAG, reference counts and live nodes are
- * those of the one-by-one calls), in one batched device pass: each tree's calls become one group
- * record per touched bottom group, applied with the set path's rules (8 equal leaves collapse at
- * every level, no batch refcount quirks, removals after sets). changed[k] (may be NULL) mirrors call
- * k's bool result. Every position is checked first (VX_E_OOB, nothing applied). */
+ * those of the one-by-one calls), in one device pass: the calls of one tree run in order, one warp
+ * per tree, trees in parallel; refcounts are settled and the replaced nodes released at the end, so
+ * the calls need up to depth + 1 free nodes each until then (VX_E_OOM otherwise). changed[k] (may be
+ * NULL) mirrors call k's bool result. Every position is checked first (VX_E_OOB, nothing applied). */
 int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const int32_t *xyz,
                       const uint32_t *values, uint8_t *changed);
 /* Launch shape of the batched-apply kernels (threads per block, blocks per SM); chosen by the

@@ -198,11 +198,11 @@ __device__ __forceinline__ void bottom_range(const DevInterner &I, const ApplyAr
                 }
                 if (cur == EMPTY_ID) break;
             }
-            uniform = set == 0xFF && !a.point_edits;  // a set of equal values is compared slot by slot
+            uniform = set == 0xFF;
 #pragma unroll
             for (int k = 1; k < 8; ++k) uniform = uniform && v[k] == v[0];
             if (cur != EMPTY_ID && id_is_leaf(cur)) {
-                if ((I.flags & 1u) || mode == 1 || a.point_edits) {  // P1 (removals and sets split a leaf)
+                if ((I.flags & 1u) || mode == 1) {  // P1 (removals always split a leaf)
                     anc = cur;
                     cur = EMPTY_ID;
                 } else if (!uniform) {  // the reference panics in BlockId::types()
@@ -294,23 +294,14 @@ __device__ __forceinline__ void bottom_range(const DevInterner &I, const ApplyAr
             }
             types |= modified;
             mask |= modified;
-            if (anc != EMPTY_ID && cur == EMPTY_ID && !a.point_edits) {  // Q5
+            if (anc != EMPTY_ID && cur == EMPTY_ID) {  // Q5
                 const int ds = __popc(set), dm = __popc(modified);
                 add_ref_delta(I, anc, modified ? dm - ds : 8 - ds);
             }
             if (modified) {
+                want_branch = true;
+                lod = calc_average8(cv);
                 changed = 1;
-                // set_at_depth_iterative collapses 8 equal leaves at every level (voxtree.rs:503)
-                bool same = a.point_edits && types == 0xFF;
-#pragma unroll
-                for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
-                if (same) {
-                    out = c[0];
-                    lod = cv[0];
-                } else {
-                    want_branch = true;
-                    lod = calc_average8(cv);
-                }
             }
         }
         bool created;
@@ -717,16 +708,13 @@ __device__ __forceinline__ void parents_range(const DevInterner &I, const ApplyA
                         mask |= inv;
                     }
                 }
-                // VoxTree::set keeps the old parent's types bits and ORs the new child's in
-                // (voxtree.rs:497-498), so a slot once a leaf keeps its bit
-                if (a.point_edits && eq != EMPTY_ID) types |= id_types(eq);
                 bool same = types == 0xFF;
     #pragma unroll
                 for (int k = 1; k < 8; ++k) same = same && c[k] == c[0];
                 if (same) {  // voxtree.rs:1062-1075
                     out = c[0];
                     out_val = cv[0];
-                    if (cloned && !a.point_edits) add_ref_delta(I, c[0], 7 - 2 * __popc(cloned));  // Q6
+                    if (cloned) add_ref_delta(I, c[0], 7 - 2 * __popc(cloned));  // Q6
                 } else {
                     want_branch = true;
                     lod = calc_average8(cv);

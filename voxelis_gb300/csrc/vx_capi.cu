@@ -480,7 +480,7 @@ int apply_sequence(vx_interner *it, ApplyArgs &a, bool clear_pass, bool check_de
     return VX_OK;
 }
 
-int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out, bool point_edits = false) {
+int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
     const uint32_t n = (uint32_t)items.size();
     if (n == 0) return VX_OK;
     std::stable_sort(items.begin(), items.end(),
@@ -576,9 +576,7 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out, bo
         VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear, R, cudaMemcpyHostToDevice, s));
         VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals, R * 16, cudaMemcpyHostToDevice, s));
     }
-    a.point_edits = point_edits ? 1 : 0;
-    // point edits remove voxels as VoxTree::set(pos, 0) does, whatever the patches
-    int st1 = apply_sequence(it, a, any_clear && (point_edits || (it->flags & VX_PATCH_P4)));
+    int st1 = apply_sequence(it, a, any_clear && (it->flags & VX_PATCH_P4));
     if (st1 != VX_OK) return st1;
     std::vector<uint8_t> ch(n);
     VX_CUDA(cudaMemcpyAsync(ch.data(), a.it_changed, n, cudaMemcpyDeviceToHost, s));
@@ -1235,7 +1233,8 @@ int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const i
                       uint8_t *changed) {
     if (!it || (n && (!trees || !xyz || !values))) return VX_E_INVALID_ARG;
     if (n == 0) return VX_OK;
-    bool shallow = false;
+    if (n >= 0xFFFFFFFFull) return set_err(it, VX_E_UNSUPPORTED, "2^32 calls or more in one call");
+    int dmax = 0;
     for (uint64_t k = 0; k < n; ++k) {  // every call is checked before any runs
         const vx_tree t = trees[k];
         if (!tree_ok(it, t) || !value_fits(it, values[k])) return set_err(it, VX_E_INVALID_ARG, "bad tree or value");
@@ -1243,60 +1242,62 @@ int vx_trees_set_many(vx_interner *it, uint64_t n, const vx_tree *trees, const i
         const int32_t x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
         if (x < 0 || y < 0 || z < 0 || x >= side || y >= side || z >= side)
             return set_err(it, VX_E_OOB, "position out of bounds");
-        shallow |= it->tree_depth[t] < 2;
+        dmax = std::max(dmax, (int)it->tree_depth[t]);
     }
-    if (shallow) {  // MaxDepth 0-1 trees: the one-thread reference sequence, call by call
-        for (uint64_t k = 0; k < n; ++k) {
-            int c = 0;
-            const int st = vx_tree_set(it, trees[k], xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2], values[k], &c);
-            if (st != VX_OK) return st;
-            if (changed) changed[k] = (uint8_t)c;
+    int st = sync_and_check(it);  // also gives the allocation state before the calls
+    if (st != VX_OK) return st;
+    const unsigned long long fc0 = it->h_ctr->free_count, ni0 = it->h_ctr->next_index;
+    // the calls grouped by tree, in call order within a tree
+    std::vector<uint32_t> order(n);
+    for (uint64_t k = 0; k < n; ++k) order[k] = (uint32_t)k;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return trees[a] < trees[b]; });
+    std::vector<uint32_t> group_tree, begin;
+    std::vector<int32_t> sx(3 * n);
+    std::vector<uint32_t> sv(n);
+    for (uint64_t k = 0; k < n; ++k) {
+        const uint32_t o = order[k];
+        if (k == 0 || trees[o] != trees[order[k - 1]]) {
+            group_tree.push_back(trees[o]);
+            begin.push_back((uint32_t)k);
         }
-        return VX_OK;
+        for (int a = 0; a < 3; ++a) sx[3 * k + a] = xyz[3 * (size_t)o + a];
+        sv[k] = values[o];
     }
-    if (changed) {  // call k changes its tree iff the voxel held another value just before it
-        std::vector<uint8_t> found(n);
-        std::vector<uint8_t> vals(n * (it->vbits / 8));  // u8 or u16 per value, as vx_get_many writes them
-        const int st = vx_get_many(it, n, trees, xyz, found.data(), vals.data(), VX_MEM_HOST);
-        if (st != VX_OK) return st;
-        std::unordered_map<uint64_t, uint32_t> cur;
-        cur.reserve(n * 2);
-        for (uint64_t k = 0; k < n; ++k) {
-            const uint64_t key = ((uint64_t)trees[k] << 32) | morton_encode(xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2]);
-            auto f = cur.find(key);
-            uint32_t before;
-            if (f != cur.end()) {
-                before = f->second;
-            } else {
-                uint16_t v16 = 0;
-                if (it->vbits == 16) std::memcpy(&v16, vals.data() + 2 * k, 2);
-                before = found[k] ? (it->vbits == 8 ? (uint32_t)vals[k] : (uint32_t)v16) : 0u;
-            }
-            changed[k] = before != values[k];
-            cur[key] = values[k];
-        }
+    begin.push_back((uint32_t)n);
+    const size_t G = group_tree.size();
+    const size_t list_cap = G + (size_t)n * (dmax + 1) + 16;  // old roots + every node the calls can create
+    VX_CUDA(it->ws.reserve(Carve::need({G * 4, (G + 1) * 4, n * 12, n * 4, n * 4, n, G * 8, list_cap * 8})));
+    Carve c(it->ws.p);
+    uint32_t *d_group = c.take<uint32_t>(G);
+    uint32_t *d_begin = c.take<uint32_t>(G + 1);
+    int32_t *d_xyz = c.take<int32_t>(3 * n);
+    uint32_t *d_vals = c.take<uint32_t>(n);
+    uint32_t *d_order = c.take<uint32_t>(n);
+    uint8_t *d_changed = c.take<uint8_t>(n);
+    uint64_t *d_roots = c.take<uint64_t>(G);
+    uint64_t *d_list = c.take<uint64_t>(list_cap);
+    cudaStream_t s = it->stream;
+    VX_CUDA(cudaMemcpyAsync(d_group, group_tree.data(), G * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_begin, begin.data(), (G + 1) * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_xyz, sx.data(), n * 12, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_vals, sv.data(), n * 4, cudaMemcpyHostToDevice, s));
+    VX_CUDA(cudaMemcpyAsync(d_order, order.data(), n * 4, cudaMemcpyHostToDevice, s));
+    SetCalls calls{(uint32_t)G, d_group, d_begin, d_xyz, d_vals, d_order, d_changed, d_roots};
+    {
+        Phase ph(it, VX_PROF_APPLY);
+        VX_CUDA(launch_trees_set(it->dev, calls, d_list, fc0, ni0, it->frontier, it->frontier + it->capacity, dmax,
+                                 it->num_sms, s));
     }
-    // one Batch per tree with its calls in order (the last write to a voxel wins, zero removes)
-    std::unordered_map<vx_tree, uint32_t> slot;
-    std::vector<vx_batch *> bs;
-    std::vector<Item> items;
-    int st = VX_OK;
-    for (uint64_t k = 0; k < n && st == VX_OK; ++k) {
-        const vx_tree t = trees[k];
-        auto f = slot.find(t);
-        if (f == slot.end()) {
-            vx_batch *b = nullptr;
-            st = vx_batch_create(it->tree_depth[t], it->vbits, it->flags | VX_PATCH_P2, &b);
-            if (st != VX_OK) break;
-            f = slot.emplace(t, (uint32_t)bs.size()).first;
-            items.push_back(Item{t, b, (uint32_t)bs.size()});
-            bs.push_back(b);
-        }
-        st = vx_batch_set(bs[f->second], xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2], values[k]);
+    std::vector<uint8_t> ch(n);
+    VX_CUDA(cudaMemcpyAsync(ch.data(), d_changed, n, cudaMemcpyDeviceToHost, s));
+    st = sync_and_check(it);
+    if (st != VX_OK) return st;
+    for (uint64_t k = 0; k < n; ++k) {
+        if (changed) changed[k] = ch[k];
+        if (ch[k]) it->tree_maybe_nonempty[trees[k]] = 1;
     }
-    if (st == VX_OK) st = run_apply(it, items, nullptr, true);
-    for (vx_batch *b : bs) vx_batch_destroy(b);
-    return st;
+    maybe_rehash(it);
+    return VX_OK;
 }
 
 int vx_tune_set(vx_interner *it, int apply_threads, int apply_blocks_per_sm) {

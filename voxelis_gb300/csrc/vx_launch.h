@@ -51,8 +51,6 @@ cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
 // ---- general batch apply (vx_apply.cu) ---------------------------------------------------------
 struct ApplyArgs {
     int mode;                    // 0: set phase (set_batch_at_depth_iterative); 1: clear pass (P4)
-    int point_edits;             // 1: VoxTree::set semantics for every voxel (set_at_depth_iterative,
-                                 // voxtree.rs:393-540): collapse at every level, exact refcounts
     int threads;                 // launch shape of the bottom/parents kernels
     int blocks_per_sm;
     uint32_t n_items;
@@ -185,6 +183,24 @@ cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *front
 // refcount order; the result status word is written to *status_out.
 cudaError_t launch_tree_set(const DevInterner &I, uint32_t tree, int32_t x, int32_t y, int32_t z, uint32_t v,
                             uint64_t *queue, uint64_t queue_cap, int *status_out, cudaStream_t s);
+// Many VoxTree::set calls (vx_trees_set_many): group g = the calls of tree group_tree[g], at
+// [begin[g], begin[g+1]) of xyz / values in call order; order[k] = the call's index for changed[].
+struct SetCalls {
+    uint32_t n_groups;
+    const uint32_t *group_tree;
+    const uint32_t *begin;
+    const int32_t *xyz;
+    const uint32_t *values;
+    const uint32_t *order;
+    uint8_t *changed;    // per call, may be null
+    uint64_t *new_root;  // per group (scratch)
+};
+// Runs the calls (one warp per tree), counts the created nodes' references, moves the roots and
+// releases the first roots and the created nodes left unreferenced. fc0 / ni0: the interner's
+// free_count and next_index before the call; `list` holds n_groups + every node the calls can create.
+cudaError_t launch_trees_set(const DevInterner &I, const SetCalls &c, uint64_t *list, unsigned long long fc0,
+                             unsigned long long ni0, uint32_t *frontier_a, uint32_t *frontier_b, int max_depth,
+                             int num_sms, cudaStream_t s);
 cudaError_t launch_tree_fill(const DevInterner &I, uint32_t tree, uint32_t v, uint64_t *queue,
                              uint64_t queue_cap, int *status_out, cudaStream_t s);
 cudaError_t launch_rehash(const DevInterner &I, uint64_t table_slots, int num_sms, cudaStream_t s);

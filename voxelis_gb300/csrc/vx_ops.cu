@@ -373,6 +373,210 @@ __global__ void tree_set_kernel(DevInterner I, uint32_t tree, int32_t x, int32_t
     *status = 1;
 }
 
+// ---- many VoxTree::set calls at once (vx_trees_set_many) ------------------------------------------
+// The calls of one tree run in call order, one warp per tree and trees in parallel. Each call is the
+// reference's set_at_depth_iterative / remove_at_depth (voxtree.rs:393-706) on the tree's current
+// root, so every node it creates, including the stale types bits of the set path (the old parent's
+// types ORed with the new child's leaf bit, voxtree.rs:513-514), is the node the reference creates.
+// All 32 lanes run the same sequence on the same values (loads of one address are one transaction);
+// lane 0 interns, through the concurrent leaf and branch inserts, and broadcasts. Refcounts are not
+// touched during the calls and nothing is released: every node stays valid until the call ends, and
+// a call that finds a node made by an earlier call gets the same node the reference would recreate.
+// Afterwards the epoch refcount kernel counts one reference per child slot of every created node,
+// the trees take their final roots (+1) and release their first ones, and created nodes that ended
+// unreferenced (the intermediate roots and paths) are released, which leaves the refcounts the
+// reference's per-call inc/dec bookkeeping gives.
+struct WSeq {
+    const DevInterner &I;
+    bool ok;
+};
+
+__device__ __forceinline__ uint64_t wchild(const DevInterner &I, uint64_t id, uint32_t k) {
+    return __ldcg((const unsigned long long *)(I.children + 8ull * id_index(id) + k));
+}
+
+__device__ uint64_t wleaf(WSeq &S, uint32_t v) {
+    uint64_t id = EMPTY_ID;
+    if ((threadIdx.x & 31u) == 0) {
+        bool created;
+        id = intern_leaf(S.I, v, &created);
+    }
+    id = __shfl_sync(0xFFFFFFFFu, id, 0);
+    if (id == EMPTY_ID) S.ok = false;
+    return id;
+}
+
+__device__ uint64_t wbranch(WSeq &S, const uint64_t c[8], uint32_t types, uint32_t mask) {
+    uint32_t cv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cv[k] = c[k] ? node_value_cg(S.I, id_index(c[k])) : 0u;
+    bool created;
+    uint64_t id = warp_intern_branch(S.I, (threadIdx.x & 31u) == 0, c, types & 0xFFu, mask & 0xFFu,
+                                     calc_average8(cv), &created);
+    id = __shfl_sync(0xFFFFFFFFu, id, 0);
+    if (id == EMPTY_ID) S.ok = false;
+    return id;
+}
+
+// set_at_depth_iterative (voxtree.rs:393-540)
+__device__ uint64_t wset(WSeq &S, uint64_t root, int32_t x, int32_t y, int32_t z, int d, uint32_t voxel) {
+    const DevInterner &I = S.I;
+    uint64_t st_node[11], st_leaf[11];
+    uint32_t st_idx[11];
+    uint64_t cur = root, leaf = EMPTY_ID;
+    int depth = 0;
+    while (depth < d) {
+        const uint32_t index = cidx(x, y, z, depth, d);
+        if (id_is_branch(cur)) {
+            st_node[depth] = cur;
+            st_leaf[depth] = leaf;
+            cur = wchild(I, cur, index);
+        } else {
+            if (node_value_cg(I, id_index(cur)) == voxel) return INVALID_ID;
+            leaf = cur;
+            cur = EMPTY_ID;
+            st_node[depth] = cur;
+            st_leaf[depth] = leaf;
+        }
+        st_idx[depth] = index;
+        ++depth;
+    }
+    if (id_is_leaf(cur) && node_value_cg(I, id_index(cur)) == voxel) return INVALID_ID;
+    cur = wleaf(S, voxel);
+    while (depth > 0 && S.ok) {
+        --depth;
+        const uint64_t pn = st_node[depth], pl = st_leaf[depth];
+        const uint32_t pi = st_idx[depth];
+        const uint32_t lbit = (id_is_leaf(cur) ? 1u : 0u) << pi;
+        uint64_t br[8];
+        if (pn != EMPTY_ID) {
+            const uint32_t types = id_types(pn) | lbit;
+            for (int k = 0; k < 8; ++k) br[k] = wchild(I, pn, k);
+            br[pi] = cur;
+            bool same = types == 0xFF;
+            for (int k = 0; k < 8; ++k) same = same && br[k] == cur;
+            if (!same) cur = wbranch(S, br, types, id_mask(pn) | (1u << pi));
+        } else if (pl == EMPTY_ID) {
+            for (int k = 0; k < 8; ++k) br[k] = EMPTY_ID;
+            br[pi] = cur;
+            cur = wbranch(S, br, lbit, 1u << pi);
+        } else {
+            for (int k = 0; k < 8; ++k) br[k] = pl;
+            br[pi] = cur;
+            cur = wbranch(S, br, ~(1u << pi) | lbit, 0xFFu);
+        }
+    }
+    return cur;
+}
+
+// remove_at_depth / _branch / _leaf (voxtree.rs:542-706)
+__device__ uint64_t wremove(WSeq &S, uint64_t root, int32_t x, int32_t y, int32_t z, int d) {
+    const DevInterner &I = S.I;
+    uint64_t frames[11];
+    int depth = 0;
+    uint64_t node = root, result = EMPTY_ID;
+    while (id_is_branch(node)) {
+        if (depth >= d) {
+            set_error(I, ERR_REF_PANIC, 80);  // "Branch node at max depth"
+            S.ok = false;
+            return INVALID_ID;
+        }
+        const uint32_t index = cidx(x, y, z, depth, d);
+        if (!((id_mask(node) >> index) & 1u)) return INVALID_ID;
+        frames[depth] = node;
+        node = wchild(I, node, index);
+        ++depth;
+    }
+    for (int k = d - 1; k >= depth && S.ok; --k) {  // remove_at_depth_leaf, built bottom-up
+        const uint32_t index = cidx(x, y, z, k, d);
+        uint64_t ch[8];
+        for (int j = 0; j < 8; ++j) ch[j] = node;
+        ch[index] = result;
+        const uint32_t types = ~(1u << index) | ((id_is_leaf(result) ? 1u : 0u) << index);
+        const uint32_t mask = ~(1u << index) | ((result != EMPTY_ID ? 1u : 0u) << index);
+        result = wbranch(S, ch, types, mask);
+    }
+    while (depth > 0 && S.ok) {  // remove_at_depth_branch on the way up
+        --depth;
+        const uint64_t pn = frames[depth];
+        const uint32_t index = cidx(x, y, z, depth, d);
+        const uint32_t mask = result == EMPTY_ID ? (id_mask(pn) & ~(1u << index)) : id_mask(pn);
+        if (mask == 0) {
+            result = EMPTY_ID;
+            continue;
+        }
+        if (!id_is_branch(result)) {
+            set_error(I, ERR_REF_PANIC, 81);  // "Removing voxel should never produce a leaf node"
+            S.ok = false;
+            return INVALID_ID;
+        }
+        uint64_t br[8];
+        for (int k = 0; k < 8; ++k) br[k] = wchild(I, pn, k);
+        br[index] = result;
+        result = wbranch(S, br, id_types(pn) & ~(1u << index), mask);
+    }
+    return result;
+}
+
+// One warp per tree group g: calls [begin[g], begin[g+1]) in call order.
+__global__ void __launch_bounds__(kThreads) trees_set_kernel(DevInterner I, const SetCalls c) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) I.ctr->scratch[SC_RELEASE] = 0;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) / 32; g < c.n_groups; g += warps) {
+        const uint32_t tree = c.group_tree[g];
+        const int d = I.depths[tree];
+        uint64_t root = I.roots[tree];
+        WSeq S{I, true};
+        for (uint32_t k = c.begin[g]; k < c.begin[g + 1] && S.ok; ++k) {
+            const int32_t x = c.xyz[3 * k], y = c.xyz[3 * k + 1], z = c.xyz[3 * k + 2];
+            const uint32_t v = c.values[k];
+            uint8_t changed = 0;
+            if (root != EMPTY_ID || v != 0) {
+                const uint64_t nw = v != 0 ? wset(S, root, x, y, z, d, v) : wremove(S, root, x, y, z, d);
+                if (!S.ok) break;
+                if (nw != INVALID_ID) {
+                    if (root != EMPTY_ID && nw == root) {  // assert_ne!(new_root_id, self.root_id)
+                        set_error(I, ERR_REF_PANIC, 82);
+                        break;
+                    }
+                    root = nw;
+                    changed = 1;
+                }
+            }
+            if ((threadIdx.x & 31u) == 0 && c.changed) c.changed[c.order[k]] = changed;
+        }
+        if ((threadIdx.x & 31u) == 0) c.new_root[g] = root;
+    }
+}
+
+// The trees take their final roots (one reference each) and list their first roots for release.
+__global__ void __launch_bounds__(kThreads) trees_set_roots_kernel(DevInterner I, const SetCalls c, uint64_t *list) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < c.n_groups; g += gridDim.x * blockDim.x) {
+        const uint32_t tree = c.group_tree[g];
+        const uint64_t old = I.roots[tree], nw = c.new_root[g];
+        if (nw == old) continue;
+        I.roots[tree] = nw;
+        if (nw != EMPTY_ID) atomicAdd(I.refcount + id_index(nw), 1u);
+        if (old != EMPTY_ID) list[atomicAdd(&I.ctr->scratch[SC_RELEASE], 1ull)] = old;
+    }
+}
+
+// Created nodes left without a reference are listed for release with a count of one. The created
+// slots are free_list[free_count .. fc0) and [ni0, next_index) once the epoch is closed.
+__global__ void __launch_bounds__(kThreads) trees_set_garbage_kernel(DevInterner I, unsigned long long fc0,
+                                                                    unsigned long long ni0, uint64_t *list) {
+    const unsigned long long fc = I.ctr->free_count, ni = I.ctr->next_index;
+    const unsigned long long n_free = fc0 - fc, n = n_free + (ni - ni0);
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < n;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t idx = t < n_free ? I.free_list[fc + t] : (uint32_t)(ni0 + (t - n_free));
+        const uint64_t id = I.ids[idx];
+        if (id == EMPTY_ID || I.refcount[idx] != 0) continue;
+        I.refcount[idx] = 1;
+        list[atomicAdd(&I.ctr->scratch[SC_RELEASE], 1ull)] = id;
+    }
+}
+
 // VoxTree::fill / clear (voxtree.rs:264-292). status: 1 if the tree was dirtied.
 __global__ void tree_fill_kernel(DevInterner I, uint32_t tree, uint32_t v, uint64_t *queue, uint64_t queue_cap,
                                  int *status) {
@@ -1112,6 +1316,24 @@ cudaError_t launch_tree_set(const DevInterner &I, uint32_t tree, int32_t x, int3
     count_launches(1);
     tree_set_kernel<<<1, 1, 0, s>>>(I, tree, x, y, z, v, queue, queue_cap, status_out);
     return cudaGetLastError();
+}
+
+cudaError_t launch_trees_set(const DevInterner &I, const SetCalls &c, uint64_t *list, unsigned long long fc0,
+                             unsigned long long ni0, uint32_t *frontier_a, uint32_t *frontier_b, int max_depth,
+                             int num_sms, cudaStream_t s) {
+    const unsigned per_block = kThreads / 32;
+    unsigned g = (c.n_groups + per_block - 1) / per_block;
+    if (g > (unsigned)num_sms * 8) g = (unsigned)num_sms * 8;
+    if (g == 0) g = 1;
+    count_launches(1);
+    trees_set_kernel<<<g, kThreads, 0, s>>>(I, c);
+    cudaError_t e = launch_epoch_refcounts(I, num_sms, s);
+    if (e != cudaSuccess) return e;
+    unsigned gr = (c.n_groups + kThreads - 1) / kThreads;
+    count_launches(2);
+    trees_set_roots_kernel<<<gr ? gr : 1, kThreads, 0, s>>>(I, c, list);
+    trees_set_garbage_kernel<<<(unsigned)num_sms * 4, kThreads, 0, s>>>(I, fc0, ni0, list);
+    return launch_release(I, list, frontier_a, frontier_b, 0, max_depth + 2, num_sms, s);
 }
 
 cudaError_t launch_tree_fill(const DevInterner &I, uint32_t tree, uint32_t v, uint64_t *queue,

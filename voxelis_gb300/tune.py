@@ -61,14 +61,18 @@ def autotune_apply(lib, handle, reset, trial, signature="default", repeats=2):
 # of two: load factor at most 1/2) and the quad memo's slots (the call's quads >> shift)
 TABLE_STEPS = (-1, 0, 1)
 MEMO_SHIFTS = (1, 2, 3)
+DEFAULT_MEMO_SHIFT = 2  # the interner's default (vx_interner_create)
 
 
-def autotune_dense(lib, make, build, signature="dense", repeats=3):
+def autotune_dense(lib, make, build, signature="dense", repeats=5, margin=0.02):
     """Tries branch-table sizes (load factor) and quad-memo geometries on the caller's own dense
     build. make(table_log2) returns a fresh interner handle (table_log2 0: the default size) with the
-    caller's trees; build(handle) resets it, runs one build and returns milliseconds. Returns the
-    fastest {table_log2, memo_shift, trials_ms} and caches it; the caller recreates its interner
-    with that table size and applies the shift with vx_tune_set_dense."""
+    caller's trees; build(handle) resets it, runs one build and returns milliseconds. Each candidate
+    is the median of `repeats` builds; the fastest replaces the default geometry only when it is
+    faster by more than `margin` (differences below that are run-to-run spread). Returns
+    {table_log2, memo_shift, trials_ms} and caches it; the caller recreates its interner with that
+    table size and applies the shift with vx_tune_set_dense."""
+    import statistics
     import ctypes as C
 
     from ._abi import vx_interner_stats
@@ -85,9 +89,12 @@ def autotune_dense(lib, make, build, signature="dense", repeats=3):
         h = make(t_log2)
         for shift in MEMO_SHIFTS:
             lib.call("tune_set_dense", h, shift, handle=h)
-            results["t%d:m%d" % (t_log2, shift)] = min(build(h) for _ in range(repeats))
+            results["t%d:m%d" % (t_log2, shift)] = statistics.median(build(h) for _ in range(repeats))
         lib.status("interner_destroy", h)
     choice = min(results, key=results.get)
+    default = "t%d:m%d" % (default_log2, DEFAULT_MEMO_SHIFT)
+    if default in results and results[choice] > (1.0 - margin) * results[default]:
+        choice = default
     t_log2, shift = (int(v[1:]) for v in choice.split(":"))
     out = {"table_log2": t_log2, "default_table_log2": default_log2, "memo_shift": shift, "trials_ms": results}
     cache = {}
