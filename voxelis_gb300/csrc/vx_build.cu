@@ -1722,7 +1722,7 @@ __device__ __forceinline__ void resolve_pending(const PendingView &P, uint64_t &
     }
 }
 
-__global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
+__global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I, const uint64_t *in_ids,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
                                                                const uint32_t *trees, uint8_t *changed,
@@ -1757,7 +1757,8 @@ __global__ void __launch_bounds__(kThreads) fresh_level_kernel(DevInterner I, co
 // parents from those (shuffles), lane 0 the root. 8 chunks per CTA; a 4096-chunk build is one wave
 // of warps at 64 registers (a CTA per 4 chunks with the levels split by CTA barriers needed 1.7
 // waves and idled 7 of its 8 warps at the barriers: 0.054 against 0.050 ms).
-__global__ void __launch_bounds__(kThreads) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
+// 4 resident CTAs per SM: the 4096-chunk build's 512 CTAs then run in a single wave on 152 SMs
+__global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
                                                                   const uint32_t *in_vals, uint32_t n_chunks,
                                                                   const uint32_t *trees, uint8_t *changed,
                                                                   PendingView P) {
