@@ -79,6 +79,17 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
         : "memory");
 }
 
+// Fills the CTA's 8-bit leaf cache from the leaf table (one coalesced 2 KB read): leaves already
+// interned (every value a build has met so far) are found in shared memory from the first lookup,
+// instead of one dependent global read per value and CTA. Leaves cannot be released during a build.
+// All threads of the CTA call it; a barrier follows before the first lookup.
+__device__ __forceinline__ void leaf_cache_warm(const DevInterner &I, uint64_t *leaf_cache, unsigned tid) {
+    for (unsigned k = tid; k < 256; k += blockDim.x) {
+        const uint64_t s = ld_volatile(I.leaf_table + k);
+        leaf_cache[k] = s > LEAF_BUSY ? s : 0ull;
+    }
+}
+
 // Leaf id of value v (v != 0): a per-CTA shared cache for 8-bit voxels, the global table otherwise.
 template <class T>
 __device__ __forceinline__ uint64_t leaf_of(const DevInterner &I, uint64_t *leaf_cache, uint32_t v) {
@@ -113,7 +124,7 @@ __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, D
 
     const unsigned tid = threadIdx.x, lane = tid & 31u;
     if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+        leaf_cache_warm(I, leaf_cache, tid);
     if (tid == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -904,7 +915,7 @@ __global__ void VX_OCT_BOUNDS dense_octants_kernel(DevInterner I, OctArgs a,
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     for (unsigned k = tid; k < kNodeCache; k += blockDim.x) N.id[k] = 0;
     if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+        leaf_cache_warm(I, leaf_cache, tid);
     if (lane == 0) {
         mbar_init(bars, 1);
         mbar_init(bars + 1, 1);
@@ -1065,7 +1076,7 @@ __global__ void __launch_bounds__(kCtaThreads) dense_cta32_kernel(DevInterner I,
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     for (unsigned k = tid; k < kNodeCache; k += blockDim.x) N.id[k] = 0;
     if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+        leaf_cache_warm(I, leaf_cache, tid);
     if (tid == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1479,7 +1490,7 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
     KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(smem + L::kcval)};
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+        leaf_cache_warm(I, leaf_cache, tid);
     if (lane == 0) {
         for (int b = 0; b < NT; ++b) mbar_init(bars + b, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1572,7 +1583,7 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
     KeyCache C{kc, kc + kKeyCache, kc + 2 * kKeyCache, reinterpret_cast<uint32_t *>(leaf_cache + 256)};
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     if (sizeof(T) == 1)
-        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_cache[k] = 0;
+        leaf_cache_warm(I, leaf_cache, tid);
     __syncthreads();
     using W = typename QuadWord<T>::type;
     const bool wide = sizeof(T) == 2;
