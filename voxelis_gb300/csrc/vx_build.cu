@@ -1479,6 +1479,7 @@ template <class T>
 __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_kernel(DevInterner I, OctArgs a, uint64_t *q_ids,
                                                                        uint32_t *q_vals,
                                                                        const __grid_constant__ CUtensorMap tmap) {
+    pdl_release();  // the record kernel may launch early: it waits for this grid before it starts
     using L = Q16Smem<T>;
     constexpr int NT = VX_Q16_TILES;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1576,6 +1577,8 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
 // reduces the quad node and writes the record's tail. Group keys go through the CTA's key cache.
 template <class T>
 __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevInterner I, OctArgs a) {
+    pdl_wait();
+    pdl_release();
     extern __shared__ __align__(128) unsigned char smem[];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint64_t *kc = reinterpret_cast<uint64_t *>(smem);
@@ -1738,6 +1741,8 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
                                                                const uint32_t *trees, uint8_t *changed,
                                                                PendingView P) {
+    pdl_wait();
+    pdl_release();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_parents; base += stride) {
         const uint64_t p = base + threadIdx.x;
@@ -1773,6 +1778,8 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, c
                                                                   const uint32_t *in_vals, uint32_t n_chunks,
                                                                   const uint32_t *trees, uint8_t *changed,
                                                                   PendingView P) {
+    pdl_wait();
+    pdl_release();
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t c = (uint64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
     if (c >= n_chunks) return;  // the whole warp
@@ -1844,6 +1851,7 @@ __device__ __forceinline__ void leaf_tab_add(uint32_t *tab_key, uint32_t *tab_cn
 }
 
 __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I) {
+    pdl_wait();
     // 8-bit leaves: 256 counters; wider leaves: the kLeafTab-entry table (dynamic shared memory, so
     // the 8-bit case keeps its occupancy)
     extern __shared__ uint32_t ref_smem[];
@@ -1925,6 +1933,31 @@ __global__ void __launch_bounds__(kThreads) epoch_refcount_kernel(DevInterner I)
 __global__ void epoch_finalize_kernel(DevInterner I) { epoch_finalize_body(I); }
 
 }  // namespace
+
+#ifndef VX_PDL
+#define VX_PDL 1  // the dense build's kernels after the first launch early (programmatic dependent launch)
+#endif
+// Launches `kernel` with programmatic stream serialization: it may start while the previous kernel of
+// the stream finishes and waits for it in pdl_wait().
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    if (!VX_PDL) {
+        kernel<<<grid, block, smem, s>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 // Opts `kernel` in to `smem` bytes of dynamic shared memory and returns its resident CTAs per SM,
 // cached per (kernel, threads, smem): both calls cost host time on every launch otherwise. The
@@ -2212,8 +2245,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
             const int per_sm = prepare_kernel(reinterpret_cast<const void *>(kernel), kQ16Warps * 32, smemc, &e2);
             if (e2 != cudaSuccess) return e2;
             count_launches(1);
-            kernel<<<(unsigned)(num_sms * per_sm), kQ16Warps * 32, smemc, s>>>(I, a);
-            return cudaGetLastError();
+            return launch_pdl(kernel, dim3((unsigned)(num_sms * per_sm)), dim3(kQ16Warps * 32), smemc, s, I, a);
         };
         e = es == 1 ? launchc(dense_memo_compute_kernel<uint8_t>) : launchc(dense_memo_compute_kernel<uint16_t>);
         if (e != cudaSuccess) return e;
@@ -2229,9 +2261,9 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     // depths 2, 1 and 0 in one launch
     count_launches(1);
     const unsigned wb = (unsigned)((n_chunks + kThreads / 32 - 1) / (kThreads / 32));
-    fresh_top_kernel<<<wb, kThreads, 0, s>>>(I, ids + off[3], vals + off[3], n_chunks, trees, changed,
-                                             depth == 5 ? P : PendingView{nullptr, 0, 0});
-    return cudaGetLastError();
+    return launch_pdl(fresh_top_kernel, dim3(wb), dim3(kThreads), 0, s, I, (const uint64_t *)(ids + off[3]),
+                      (const uint32_t *)(vals + off[3]), n_chunks, trees, changed,
+                      depth == 5 ? P : PendingView{nullptr, 0, 0});
 }
 
 // One level of fresh parents: n_parents = n_chunks * 8^k; children pending in P are resolved first.
@@ -2242,16 +2274,14 @@ static cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_i
     uint64_t blocks = (n_parents + kThreads - 1) / kThreads;
     if (blocks > 65535) blocks = 65535;
     count_launches(1);
-    fresh_level_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(I, in_ids, in_vals, out_ids, out_vals, n_parents,
-                                                             is_root ? 1 : 0, trees, changed, P);
-    return cudaGetLastError();
+    return launch_pdl(fresh_level_kernel, dim3((unsigned)blocks), dim3(kThreads), 0, s, I, in_ids, in_vals, out_ids,
+                      out_vals, n_parents, is_root ? 1 : 0, trees, changed, P);
 }
 
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s) {
     const size_t smem = I.vbits == 8 ? 256 * 4 : (size_t)2 * kLeafTab * 4;
     count_launches(1);
-    epoch_refcount_kernel<<<num_sms * 16, kThreads, smem, s>>>(I);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(epoch_refcount_kernel, dim3(num_sms * 16), dim3(kThreads), smem, s, I);
     if (e != cudaSuccess || VX_REF_FOLD) return e;
     return launch_epoch_finalize(I, s);
 }

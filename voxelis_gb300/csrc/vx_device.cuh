@@ -179,6 +179,14 @@ __device__ __forceinline__ bool grid_last_cta(unsigned long long *done) {
     return true;
 }
 
+// Programmatic dependent launch: a kernel launched with the programmatic-serialization attribute may
+// start while its predecessor on the stream still runs; pdl_wait() blocks until the predecessor has
+// completed and its writes are visible (a no-op for a normal launch), and pdl_release() lets the next
+// kernel of the stream launch early. A kernel calls pdl_wait() before its first access to memory the
+// predecessor writes.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void set_error(const DevInterner &I, uint32_t bit, uint32_t info = 0) {
     unsigned int old = atomicOr(&I.ctr->error, bit);
     if (old == 0) atomicExch(&I.ctr->error_info, info);
