@@ -156,6 +156,8 @@ __device__ __forceinline__ void prep_item(const DevInterner &I, const ApplyArgs 
 }
 
 __global__ void prep_items_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n_items) prep_item(I, a, a.mode, i);
 }
@@ -317,6 +319,8 @@ __device__ __forceinline__ void bottom_range(const DevInterner &I, const ApplyAr
 }
 
 __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const LeafRefs L = leaf_refs_init(I);
     bottom_range(I, a, a.mode, L, (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
     leaf_refs_flush(I, L);
@@ -325,6 +329,8 @@ __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) bottom_kernel(DevInt
 // Exclusive scan of n flags: per-block scan, scan of block sums, add-back. pos[n] = total.
 __global__ void __launch_bounds__(kThreads) scan_blocks_kernel(const uint32_t *in, uint32_t *out, uint32_t *sums,
                                                               uint32_t n) {
+    pdl_wait();
+    pdl_release();
     __shared__ uint32_t warp_tot[kThreads / 32];
     const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanPer;
     uint32_t x[kScanPer];
@@ -366,6 +372,8 @@ __global__ void __launch_bounds__(kThreads) scan_blocks_kernel(const uint32_t *i
 // count only record an empty block sum.
 __global__ void __launch_bounds__(kThreads) scan_blocks_dev_kernel(const uint32_t *in, uint32_t *out, uint32_t *sums,
                                                                   const unsigned long long *n_dev) {
+    pdl_wait();
+    pdl_release();
     const uint32_t n = (uint32_t)*n_dev;
     if (blockIdx.x * kScanBlock >= n) {
         if (threadIdx.x == 0) sums[blockIdx.x] = 0;
@@ -420,6 +428,8 @@ __global__ void __launch_bounds__(kThreads) scan_blocks_dev_kernel(const uint32_
 __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner I, const uint32_t *in, uint32_t *out,
                                                                    unsigned long long *status,
                                                                    const unsigned long long *n_dev) {
+    pdl_wait();
+    pdl_release();
     __shared__ uint32_t tile_s, prefix_s;
     __shared__ uint32_t warp_tot[kThreads / 32];
     unsigned long long *ticket = &I.ctr->scratch[SC_SCAN_TICKET];
@@ -493,6 +503,8 @@ __global__ void __launch_bounds__(kThreads) scan_onepass_dev_kernel(DevInterner 
 }
 
 __global__ void scan_add_dev_kernel(uint32_t *out, const uint32_t *sums, const unsigned long long *n_dev) {
+    pdl_wait();
+    pdl_release();
     const uint32_t n = (uint32_t)*n_dev;
     const uint32_t b = blockIdx.x;
     if (b == 0 || b * kScanBlock >= n) return;
@@ -503,11 +515,15 @@ __global__ void scan_add_dev_kernel(uint32_t *out, const uint32_t *sums, const u
 }
 
 __global__ void scan_total_dev_kernel(const uint32_t *in, uint32_t *out, const unsigned long long *n_dev) {
+    pdl_wait();
+    pdl_release();
     const uint32_t n = (uint32_t)*n_dev;
     out[n] = n ? out[n - 1] + in[n - 1] : 0u;
 }
 
 __global__ void scan_add_kernel(uint32_t *out, const uint32_t *sums, uint32_t n) {
+    pdl_wait();
+    pdl_release();
     const uint32_t b = blockIdx.x;
     if (b == 0) return;
     const uint32_t add = sums[b];
@@ -517,6 +533,8 @@ __global__ void scan_add_kernel(uint32_t *out, const uint32_t *sums, uint32_t n)
 }
 
 __global__ void scan_total_kernel(const uint32_t *in, uint32_t *out, uint32_t n) {
+    pdl_wait();
+    pdl_release();
     out[n] = n ? out[n - 1] + in[n - 1] : 0u;
 }
 
@@ -530,6 +548,8 @@ __device__ __forceinline__ void scatter_record(const ApplyArgs &a, uint32_t r) {
 }
 
 __global__ void scatter_bottom_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r == 0) I.ctr->scratch[SC_ENTRIES] = a.pos[a.n_records];
     if (r < a.n_records) scatter_record(a, r);
@@ -554,6 +574,8 @@ __device__ __forceinline__ void head_flag(const ApplyArgs &a, int step, int buf,
 }
 
 __global__ void heads_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    pdl_wait();
+    pdl_release();
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
         head_flag(a, step, buf, j);
@@ -568,6 +590,8 @@ __device__ __forceinline__ void starts_head(const DevInterner &I, const ApplyArg
 }
 
 __global__ void starts_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const uint32_t count = (uint32_t)I.ctr->scratch[SC_ENTRIES];
     if (blockIdx.x == 0 && threadIdx.x == 0) starts_head(I, a, count);
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
@@ -742,6 +766,8 @@ __device__ __forceinline__ void parents_range(const DevInterner &I, const ApplyA
 }
 
 __global__ void __launch_bounds__(512, VX_APPLY_MIN_BLOCKS) parents_kernel(DevInterner I, ApplyArgs a, int step, int buf) {
+    pdl_wait();
+    pdl_release();
     const LeafRefs L = leaf_refs_init(I);
     parents_range(I, a, a.mode, L, step, buf, (uint32_t)I.ctr->scratch[SC_PARENTS],
                   (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
@@ -785,12 +811,14 @@ __device__ __forceinline__ void finish_item(const DevInterner &I, const ApplyArg
 // Commits every item's root, then (last CTA) closes the allocation epoch: every node of this apply
 // pass has been created and has added its children's references by now.
 __global__ void finish_items_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n_items) finish_item(I, a, a.mode, i);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) epoch_finalize_body(I);
 }
 
-__global__ void zero_counter_kernel(DevInterner I, int slot) { I.ctr->scratch[slot] = 0; }
+__global__ void zero_counter_kernel(DevInterner I, int slot) { pdl_wait(); pdl_release(); I.ctr->scratch[slot] = 0; }
 
 __device__ __forceinline__ void item_depth(const DevInterner &I, const ApplyArgs &a, uint32_t i) {
     const uint32_t t = a.it_tree[i];
@@ -809,6 +837,8 @@ __device__ __forceinline__ void item_depth(const DevInterner &I, const ApplyArgs
 }
 
 __global__ void item_depths_kernel(DevInterner I, ApplyArgs a) {
+    pdl_wait();
+    pdl_release();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n_items) item_depth(I, a, i);
 }
@@ -959,20 +989,20 @@ static cudaError_t launch_scan_dev(const DevInterner &I, const uint32_t *flags, 
     if (nb == 0) return cudaSuccess;
     if (status && nb <= kScanStatusTiles) {
         count_launches(1);
-        scan_onepass_dev_kernel<<<nb, kThreads, 0, s>>>(I, flags, pos, status, n_dev);
+        (void)launch_pdl(scan_onepass_dev_kernel, dim3(nb), dim3(kThreads), 0, s, I, flags, pos, status, n_dev);
         return cudaGetLastError();
     }
     count_launches(1);
-    scan_blocks_dev_kernel<<<nb, kThreads, 0, s>>>(flags, pos, tmp, n_dev);
+    (void)launch_pdl(scan_blocks_dev_kernel, dim3(nb), dim3(kThreads), 0, s, flags, pos, tmp, n_dev);
     if (nb > 1) {
         uint32_t *tmp2 = tmp + nb;
         cudaError_t e = launch_scan(tmp, tmp2, tmp2 + nb + 1 + 32, nb, s);
         if (e != cudaSuccess) return e;
         count_launches(1);
-        scan_add_dev_kernel<<<nb, kThreads, 0, s>>>(pos, tmp2, n_dev);
+        (void)launch_pdl(scan_add_dev_kernel, dim3(nb), dim3(kThreads), 0, s, pos, tmp2, n_dev);
     }
     count_launches(1);
-    scan_total_dev_kernel<<<1, 1, 0, s>>>(flags, pos, n_dev);
+    (void)launch_pdl(scan_total_dev_kernel, dim3(1), dim3(1), 0, s, flags, pos, n_dev);
     return cudaGetLastError();
 }
 
@@ -980,34 +1010,34 @@ cudaError_t launch_scan(const uint32_t *flags, uint32_t *pos, uint32_t *tmp, uin
     const uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
     if (nb == 0) {
         count_launches(1);
-        scan_total_kernel<<<1, 1, 0, s>>>(flags, pos, 0);
+        (void)launch_pdl(scan_total_kernel, dim3(1), dim3(1), 0, s, flags, pos, 0);
         return cudaGetLastError();
     }
     count_launches(1);
-    scan_blocks_kernel<<<nb, kThreads, 0, s>>>(flags, pos, tmp, n);
+    (void)launch_pdl(scan_blocks_kernel, dim3(nb), dim3(kThreads), 0, s, flags, pos, tmp, n);
     if (nb > 1) {
         uint32_t *tmp2 = tmp + nb;  // scan of the block sums (recursive)
         cudaError_t e = launch_scan(tmp, tmp2, tmp2 + nb + 1 + 32, nb, s);
         if (e != cudaSuccess) return e;
         count_launches(1);
-        scan_add_kernel<<<nb, kThreads, 0, s>>>(pos, tmp2, n);
+        (void)launch_pdl(scan_add_kernel, dim3(nb), dim3(kThreads), 0, s, pos, tmp2, n);
     }
     count_launches(1);
-    scan_total_kernel<<<1, 1, 0, s>>>(flags, pos, n);
+    (void)launch_pdl(scan_total_kernel, dim3(1), dim3(1), 0, s, flags, pos, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_item_depths(const DevInterner &I, const ApplyArgs &a, cudaStream_t s) {
     if (a.n_items == 0) return cudaSuccess;
     count_launches(1);
-    item_depths_kernel<<<(a.n_items + kThreads - 1) / kThreads, kThreads, 0, s>>>(I, a);
+    (void)launch_pdl(item_depths_kernel, dim3((a.n_items + kThreads - 1) / kThreads), dim3(kThreads), 0, s, I, a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int num_sms, cudaStream_t s) {
     const unsigned ib = (a.n_items + kThreads - 1) / kThreads;
     count_launches(1);
-    prep_items_kernel<<<ib, kThreads, 0, s>>>(I, a);
+    (void)launch_pdl(prep_items_kernel, dim3(ib), dim3(kThreads), 0, s, I, a);
     const uint32_t R = a.n_records;
     if (R) {
         const int bt = a.threads > 0 ? a.threads : kThreads;
@@ -1015,7 +1045,7 @@ cudaError_t launch_apply_bottom(const DevInterner &I, const ApplyArgs &a, int nu
         const unsigned need = (R + bt - 1) / bt;
         const unsigned g = need < cap ? need : cap;
         count_launches(1);
-        bottom_kernel<<<g, bt, leaf_refs_smem(I), s>>>(I, a);
+        (void)launch_pdl(bottom_kernel, dim3(g), dim3(bt), leaf_refs_smem(I), s, I, a);
     }
     return cudaGetLastError();
 }
@@ -1032,25 +1062,25 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
         cudaError_t e = launch_scan(a.flags, a.pos, a.scan_tmp, R, s);
         if (e != cudaSuccess) return e;
         count_launches(1);
-        scatter_bottom_kernel<<<rb, kThreads, 0, s>>>(I, a);
+        (void)launch_pdl(scatter_bottom_kernel, dim3(rb), dim3(kThreads), 0, s, I, a);
         int buf = 0;
         const unsigned sb = rb < (unsigned)num_sms * 16 ? rb : (unsigned)num_sms * 16;
         for (int step = 1; step <= a.max_depth - 1; ++step) {
             count_launches(1);
-            heads_kernel<<<sb, kThreads, 0, s>>>(I, a, step, buf);
+            (void)launch_pdl(heads_kernel, dim3(sb), dim3(kThreads), 0, s, I, a, step, buf);
             e = launch_scan_dev(I, a.flags, a.pos, a.scan_tmp, R, &I.ctr->scratch[SC_ENTRIES], a.scan_status, s);
             if (e != cudaSuccess) return e;
             count_launches(1);
-            starts_kernel<<<sb, kThreads, 0, s>>>(I, a);
+            (void)launch_pdl(starts_kernel, dim3(sb), dim3(kThreads), 0, s, I, a);
             count_launches(1);
-            parents_kernel<<<g, bt, leaf_refs_smem(I), s>>>(I, a, step, buf);  // its last CTA sets the next entry count
+            (void)launch_pdl(parents_kernel, dim3(g), dim3(bt), leaf_refs_smem(I), s, I, a, step, buf);  // its last CTA sets the next entry count
             buf ^= 1;
         }
     }
     count_launches(1);
-    zero_counter_kernel<<<1, 1, 0, s>>>(I, SC_RELEASE);
+    (void)launch_pdl(zero_counter_kernel, dim3(1), dim3(1), 0, s, I, SC_RELEASE);
     count_launches(1);
-    finish_items_kernel<<<ib, kThreads, 0, s>>>(I, a);  // its last CTA closes the epoch
+    (void)launch_pdl(finish_items_kernel, dim3(ib), dim3(kThreads), 0, s, I, a);  // its last CTA closes the epoch
     return cudaGetLastError();
 }
 

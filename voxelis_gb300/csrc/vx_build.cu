@@ -1934,31 +1934,6 @@ __global__ void epoch_finalize_kernel(DevInterner I) { epoch_finalize_body(I); }
 
 }  // namespace
 
-#ifndef VX_PDL
-#define VX_PDL 1  // the dense build's kernels after the first launch early (programmatic dependent launch)
-#endif
-// Launches `kernel` with programmatic stream serialization: it may start while the previous kernel of
-// the stream finishes and waits for it in pdl_wait().
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                              Args... args) {
-    if (!VX_PDL) {
-        kernel<<<grid, block, smem, s>>>(args...);
-        return cudaGetLastError();
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
 // Opts `kernel` in to `smem` bytes of dynamic shared memory and returns its resident CTAs per SM,
 // cached per (kernel, threads, smem): both calls cost host time on every launch otherwise. The
 // opt-in is a property of the kernel, so it only ever rises (a kernel launched with several sizes,

@@ -8,6 +8,31 @@
 
 namespace vxg {
 
+#ifndef VX_PDL
+#define VX_PDL 1  // kernels after the first of a sequence launch early (programmatic dependent launch)
+#endif
+// Launches `kernel` with programmatic stream serialization: it may start while the previous kernel of
+// the stream finishes and waits for it in pdl_wait().
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    if (!VX_PDL) {
+        kernel<<<grid, block, smem, s>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Process-wide count of kernels launched by this library (reported by vx_kernel_launches).
 void count_launches(uint64_t n);
 

@@ -68,18 +68,22 @@ __global__ void __launch_bounds__(kThreads) get_kernel(DevInterner I, uint64_t n
 // ---- release (bodies in vx_device.cuh, shared with the single-launch apply) ------------------------
 __global__ void __launch_bounds__(kThreads) release_roots_kernel(DevInterner I, const uint64_t *list,
                                                                 uint32_t *out) {
+    pdl_wait();
+    pdl_release();
     release_roots_range(I, list, out, &I.ctr->scratch[SC_REL_OUT], (uint64_t)blockIdx.x * blockDim.x,
                         (uint64_t)gridDim.x * blockDim.x);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 
 __global__ void __launch_bounds__(kThreads) release_round_kernel(DevInterner I, const uint32_t *in, uint32_t *out) {
+    pdl_wait();
+    pdl_release();
     release_round_range(I, in, out, &I.ctr->scratch[SC_REL_IN], &I.ctr->scratch[SC_REL_OUT],
                         (uint64_t)blockIdx.x * blockDim.x, (uint64_t)gridDim.x * blockDim.x);
     if (grid_last_cta(&I.ctr->scratch[SC_DONE])) release_advance(I);
 }
 
-__global__ void release_advance_kernel(DevInterner I) { release_advance(I); }
+__global__ void release_advance_kernel(DevInterner I) { pdl_wait(); pdl_release(); release_advance(I); }
 
 // ---- single-thread reference-order operations ---------------------------------------------------
 struct Seq {
@@ -1297,13 +1301,13 @@ cudaError_t launch_release(const DevInterner &I, uint64_t *list, uint32_t *front
     (void)frontier_cap;
     const unsigned g = (unsigned)num_sms * 4;
     count_launches(1);
-    release_advance_kernel<<<1, 1, 0, s>>>(I);  // clears the output count
+    (void)launch_pdl(release_advance_kernel, dim3(1), dim3(1), 0, s, I);  // clears the output count
     count_launches(1);
-    release_roots_kernel<<<g, kThreads, 0, s>>>(I, list, frontier_a);
+    (void)launch_pdl(release_roots_kernel, dim3(g), dim3(kThreads), 0, s, I, list, frontier_a);
     uint32_t *in = frontier_a, *out = frontier_b;
     for (int r = 0; r < rounds; ++r) {  // each kernel's last CTA advances the dying set
         count_launches(1);
-        release_round_kernel<<<g, kThreads, 0, s>>>(I, in, out);
+        (void)launch_pdl(release_round_kernel, dim3(g), dim3(kThreads), 0, s, I, in, out);
         uint32_t *t = in;
         in = out;
         out = t;
