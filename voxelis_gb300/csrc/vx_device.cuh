@@ -152,6 +152,17 @@ __device__ __forceinline__ unsigned long long atom_exch_release(unsigned long lo
     asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     return old;
 }
+// Publication of a slot this thread owns (claimed in a busy state that no other thread writes): a
+// release store waits for this thread's earlier writes like the exchange, but not for a reply.
+#ifndef VX_PUB_STORE
+#define VX_PUB_STORE 1
+#endif
+__device__ __forceinline__ void publish_release(unsigned long long *p, unsigned long long v) {
+    if (VX_PUB_STORE)
+        st_release_u64(p, v);
+    else
+        atom_exch_release(p, v);
+}
 // Compare-and-swap that publishes this thread's earlier stores (release) and, whatever its outcome,
 // makes the stores published with the value it read visible to this thread (acquire).
 __device__ __forceinline__ unsigned long long atom_cas_acq_rel(unsigned long long *p, unsigned long long cmp,
@@ -393,7 +404,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
                     atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
                 } else {
                     result = write_branch(I, idx, c, types, mask, h, lod);
-                    atom_exch_release((unsigned long long *)(I.table + pos), make_slot(tag, idx));
+                    publish_release((unsigned long long *)(I.table + pos), make_slot(tag, idx));
                     *created = true;
                 }
                 done = true;
@@ -443,7 +454,7 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
                 I.hash[idx] = 0;
                 I.refcount[idx] = 0;
                 I.ids[idx] = id;
-                atom_exch_release(slot, id);
+                publish_release(slot, id);
                 *created = true;
                 return id;
             }
