@@ -112,10 +112,19 @@ struct DevBuf {
     }
 };
 
-#ifndef VX_COPY_PIECES
-#define VX_COPY_PIECES 4  // 8 and 16 measured slower: small pieces build below the copy rate
+// Pieces of a host-memory dense build (the copy of piece k+1 overlaps the build of piece k), as
+// relative sizes. Only the last piece's build is left once the copies end, so it is the smallest;
+// a piece's build is latency-bound, so pieces much smaller than a quarter build below the copy rate
+// (8 and 16 equal pieces measured slower than 4).
+#ifndef VX_PIECE_PLAN
+#define VX_PIECE_PLAN 1
 #endif
-constexpr int kCopyPieces = VX_COPY_PIECES;  // pieces of a host-memory dense build (copy of k+1 overlaps build of k)
+#if VX_PIECE_PLAN == 1
+constexpr int kPieceWeights[] = {4, 4, 4, 3, 1};
+#else
+constexpr int kPieceWeights[] = {1, 1, 1, 1};
+#endif
+constexpr int kCopyPieces = (int)(sizeof(kPieceWeights) / sizeof(kPieceWeights[0]));
 
 struct HostBuf {
     void *p = nullptr;
@@ -1436,10 +1445,14 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
             VX_CUDA(cudaEventRecord(it->copy_events[0], s));
             VX_CUDA(cudaStreamWaitEvent(it->copy_stream, it->copy_events[0], 0));
         }
-        const uint32_t per_piece = (n + kCopyPieces - 1) / kCopyPieces;
-        for (int k = 0; k < kCopyPieces; ++k) {
-            const uint32_t c0 = k * per_piece, c1 = std::min(n, c0 + per_piece);
-            if (c0 >= c1) break;
+        int weight_total = 0;
+        for (int w : kPieceWeights) weight_total += w;
+        bool first = true;  // the first piece clears the quad memo the later ones share
+        for (int k = 0, acc = 0; k < kCopyPieces; ++k) {
+            const uint32_t c0 = (uint32_t)((uint64_t)n * acc / weight_total);
+            acc += kPieceWeights[k];
+            const uint32_t c1 = (uint32_t)((uint64_t)n * acc / weight_total);
+            if (c0 >= c1) continue;
             VX_CUDA(cudaMemcpyAsync(dg + per * c0, static_cast<const uint8_t *>(grids) + per * c0, per * (c1 - c0),
                                     cudaMemcpyHostToDevice, it->copy_stream));
             VX_CUDA(cudaEventRecord(it->copy_events[k], it->copy_stream));
@@ -1447,12 +1460,13 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
             if (split) {
                 PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
                 VX_CUDA(launch_dense_split(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p, it->num_sms,
-                                           s, memo, k == 0, n, &PhaseSwitch::next, &ps));
+                                           s, memo, first, n, &PhaseSwitch::next, &ps));
             } else {
                 Phase ph(it, VX_PROF_DENSE);
                 VX_CUDA(launch_dense_octants(it->dev, dg + per * c0, dt + c0, c1 - c0, d, dc + c0, it->ws.p,
-                                             it->num_sms, s, memo, k == 0, n));
+                                             it->num_sms, s, memo, first, n));
             }
+            first = false;
         }
         {
             Phase ph(it, VX_PROF_REFCOUNT);
