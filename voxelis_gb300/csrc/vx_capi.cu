@@ -117,10 +117,16 @@ struct DevBuf {
 // a piece's build is latency-bound, so pieces much smaller than a quarter build below the copy rate
 // (8 and 16 equal pieces measured slower than 4).
 #ifndef VX_PIECE_PLAN
-#define VX_PIECE_PLAN 1
+#define VX_PIECE_PLAN 0
 #endif
 #if VX_PIECE_PLAN == 1
 constexpr int kPieceWeights[] = {4, 4, 4, 3, 1};
+#elif VX_PIECE_PLAN == 2
+constexpr int kPieceWeights[] = {2, 2, 2, 1};
+#elif VX_PIECE_PLAN == 3
+constexpr int kPieceWeights[] = {1, 1, 1};
+#elif VX_PIECE_PLAN == 4
+constexpr int kPieceWeights[] = {3, 3, 2};
 #else
 constexpr int kPieceWeights[] = {1, 1, 1, 1};
 #endif
