@@ -114,10 +114,11 @@ struct DevBuf {
 
 // Pieces of a host-memory dense build (the copy of piece k+1 overlaps the build of piece k), as
 // relative sizes. Only the last piece's build is left once the copies end, so it is the smallest;
-// a piece's build is latency-bound, so pieces much smaller than a quarter build below the copy rate
-// (8 and 16 equal pieces measured slower than 4).
+// a piece's build is latency-bound, so small pieces build below the copy rate. Measured on the
+// 4096-chunk dunes (e2e ms): {2,2,2,1} 0.787, equal quarters 0.796, {3,3,2} 0.799, equal thirds
+// 0.804, {4,4,4,3,1} 0.822; 8 and 16 equal pieces were slower still.
 #ifndef VX_PIECE_PLAN
-#define VX_PIECE_PLAN 0
+#define VX_PIECE_PLAN 2
 #endif
 #if VX_PIECE_PLAN == 1
 constexpr int kPieceWeights[] = {4, 4, 4, 3, 1};
