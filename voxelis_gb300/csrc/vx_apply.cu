@@ -1084,6 +1084,25 @@ cudaError_t launch_apply_levels(const DevInterner &I, const ApplyArgs &a, int nu
     return cudaGetLastError();
 }
 
+namespace {
+// rec_item[r] = i for every record r of item i (records of item i: [first[i], first[i+1])), one CTA
+// per item with coalesced stores.
+__global__ void __launch_bounds__(kThreads) expand_items_kernel(const uint32_t *first, uint32_t n,
+                                                               uint32_t *rec_item) {
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t r1 = first[i + 1];
+        for (uint32_t r = first[i] + threadIdx.x; r < r1; r += blockDim.x) rec_item[r] = i;
+    }
+}
+}  // namespace
+
+cudaError_t launch_expand_items(const uint32_t *first, uint32_t n, uint32_t *rec_item, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    count_launches(1);
+    expand_items_kernel<<<n < 65535u ? n : 65535u, kThreads, 0, s>>>(first, n, rec_item);
+    return cudaGetLastError();
+}
+
 size_t apply_single_scan_words(int num_sms) { return (size_t)num_sms * 32 + 64; }
 
 // The whole apply sequence in one cooperative launch: as many CTAs as can be resident at once (the

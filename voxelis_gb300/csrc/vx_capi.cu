@@ -89,7 +89,17 @@ void batch_for_each_touched(const vx_batch *b, F f) {
         std::sort(b->touched.begin(), b->touched.end());
         b->touched_sorted = true;
     }
-    for (uint32_t g : b->touched) f((uint64_t)g);
+    // sparse groups: their mask and value bytes are fetched a few groups ahead of use
+    const size_t m = b->touched.size(), vb = (size_t)b->vbits / 8;
+    for (size_t k = 0; k < m; ++k) {
+        if (k + 16 < m) {
+            const uint64_t gp = b->touched[k + 16];
+            __builtin_prefetch(b->set.data() + gp);
+            __builtin_prefetch(b->clear.data() + gp);
+            __builtin_prefetch(b->vals.data() + 8 * vb * gp);
+        }
+        f((uint64_t)b->touched[k]);
+    }
 }
 
 struct DevBuf {
@@ -418,7 +428,8 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     const size_t need = Carve::need({n * 4 * in_items, n, n * in_items, n * 4 * in_items, n * 8, n * 8, n * 8, n,
                                      n, R * 4 * in_recs, R * 4 * in_recs, R * in_recs, R * in_recs, R * 16 * in_recs,
                                      Rp * 4, Rp * 4, scan_words(it, Rp) * 4, R * 4, R * 4, R * 4,
-                                     R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8});
+                                     R * 4, R * 8, R * 8, R * 4, R * 4, Rp * 4, R * 8, R * 4, n * 8,
+                                     (n + 1) * 4 * in_items});
     VX_CUDA(it->ws.reserve(need));
     Carve c(it->ws.p);
     a.mode = 0;
@@ -460,6 +471,7 @@ int carve_apply(vx_interner *it, uint32_t n, uint64_t R, bool own_inputs, ApplyA
     a.rec_id = c.take<uint64_t>(R);
     a.rec_val = c.take<uint32_t>(R);
     a.release_list = c.take<uint64_t>(n);
+    if (own_inputs) a.it_first = c.take<uint32_t>((size_t)n + 1);
     return VX_OK;
 }
 
@@ -514,13 +526,16 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
             return set_err(it, VX_E_REF_PANIC, "batch apply needs max_depth >= 2 (usize underflow in the reference)");
     if (R >= 0xFFFFFFF0ull) return set_err(it, VX_E_UNSUPPORTED, "too many touched groups in one call");
 
-    // host staging in pinned memory: items, then the touched groups of every batch as records
-    // sorted by (item, group), filled by several threads over balanced record ranges
-    VX_CUDA(it->pinned.reserve(Carve::need({n * 4, n * 4, n, n, R * 4, R * 4, R, R, R * 16})));
+    // host staging in pinned memory: items, then the touched groups of every batch as records sorted
+    // by (item, group). Several threads fill them in record groups; each group's records go to the
+    // device (on the interner's stream) while the threads fill the next one. The record -> item index
+    // is expanded on the device from the items' first records.
+    VX_CUDA(it->pinned.reserve(Carve::need({n * 4, n * 4, n, n, (n + 1) * 4, R * 4, R, R, R * 16})));
     Carve hc(it->pinned.p);
     uint32_t *it_tree = hc.take<uint32_t>(n), *it_fill = hc.take<uint32_t>(n);
     uint8_t *it_depth = hc.take<uint8_t>(n), *it_flags = hc.take<uint8_t>(n);
-    uint32_t *rec_item = hc.take<uint32_t>(R), *rec_group = hc.take<uint32_t>(R);
+    uint32_t *it_off = hc.take<uint32_t>(n + 1);
+    uint32_t *rec_group = hc.take<uint32_t>(R);
     uint8_t *rec_set = hc.take<uint8_t>(R), *rec_clear = hc.take<uint8_t>(R);
     uint16_t *rec_vals = hc.take<uint16_t>(R * 8);
     for (uint32_t i = 0; i < n; ++i) {
@@ -530,7 +545,8 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
         it_flags[i] = (b->has_fill ? 1 : 0) | (b->has_patches ? 2 : 0);
         it_fill[i] = b->fill;
     }
-    auto fill_items = [&](uint32_t i0, uint32_t i1, bool *clear_seen) {
+    for (uint32_t i = 0; i <= n; ++i) it_off[i] = (uint32_t)off[i];
+    auto fill_items = [&](uint32_t i0, uint32_t i1) {
         bool cs = false;
         for (uint32_t i = i0; i < i1; ++i) {
             const vx_batch *b = items[i].batch;
@@ -538,7 +554,6 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
             uint64_t r = off[i];
             const bool wide = b->vbits != 8;
             batch_for_each_touched(b, [&](uint64_t g) {
-                rec_item[r] = i;
                 rec_group[r] = (uint32_t)g;
                 rec_set[r] = b->set[g];
                 rec_clear[r] = b->clear[g];
@@ -551,30 +566,31 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
                 ++r;
             });
         }
-        *clear_seen = cs;
+        return cs;
     };
+    // first item whose records start at or after record r
+    auto item_at = [&](uint64_t r) { return (uint32_t)(std::lower_bound(off.begin(), off.end() - 1, r) - off.begin()); };
     unsigned nt = std::thread::hardware_concurrency();
     nt = std::max(1u, std::min(nt, 16u));
+    const unsigned K = R >= (1u << 20) ? 4 : 1;  // record groups: the copy of one overlaps the fill of the next
     if (R < (1u << 16)) nt = 1;
-    std::vector<uint32_t> bounds(nt + 1, n);
-    bounds[0] = 0;
-    for (unsigned t = 1; t < nt; ++t)  // first item whose records start at or after t/nt of R
-        bounds[t] = (uint32_t)(std::lower_bound(off.begin(), off.end() - 1, R * t / nt) - off.begin());
+    std::vector<uint32_t> gb(K + 1, n);
+    gb[0] = 0;
+    for (unsigned c = 1; c < K; ++c) gb[c] = item_at(R * c / K);
+    std::vector<std::atomic<unsigned>> done(K);
+    for (auto &d : done) d.store(0);
     std::vector<char> clears(nt, 0);
-    if (nt == 1) {
-        bool c0 = false;
-        fill_items(0, n, &c0);
-        clears[0] = c0;
-    } else {
-        std::vector<std::thread> pool;
-        bool cflags[16] = {false};
-        for (unsigned t = 0; t < nt; ++t)
-            pool.emplace_back([&, t] { fill_items(bounds[t], std::max(bounds[t], bounds[t + 1]), &cflags[t]); });
-        for (auto &th : pool) th.join();
-        for (unsigned t = 0; t < nt; ++t) clears[t] = cflags[t];
-    }
-    bool any_clear = false;
-    for (char c : clears) any_clear |= c != 0;
+    auto worker = [&](unsigned t) {  // share t >= 1 of every group
+        bool cs = false;
+        for (unsigned c = 0; c < K; ++c) {
+            const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
+            const uint32_t a0 = t == 0 ? gb[c] : std::max(gb[c], item_at(r0 + (r1 - r0) * t / nt));
+            const uint32_t a1 = t + 1 == nt ? gb[c + 1] : std::min(gb[c + 1], item_at(r0 + (r1 - r0) * (t + 1) / nt));
+            if (a0 < a1) cs |= fill_items(a0, a1);
+            done[c].fetch_add(1, std::memory_order_release);
+        }
+        clears[t] = cs;
+    };
 
     ApplyArgs a{};
     int st0 = carve_apply(it, n, R, true, a);
@@ -586,12 +602,38 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
     VX_CUDA(cudaMemcpyAsync((void *)a.it_flags, it_flags, n, cudaMemcpyHostToDevice, s));
     VX_CUDA(cudaMemcpyAsync((void *)a.it_fill, it_fill, n * 4, cudaMemcpyHostToDevice, s));
     if (R) {
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_item, rec_item, R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_group, rec_group, R * 4, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_set, rec_set, R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_clear, rec_clear, R, cudaMemcpyHostToDevice, s));
-        VX_CUDA(cudaMemcpyAsync((void *)a.rec_vals, rec_vals, R * 16, cudaMemcpyHostToDevice, s));
+        VX_CUDA(cudaMemcpyAsync(a.it_first, it_off, (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        VX_CUDA(launch_expand_items(a.it_first, n, (uint32_t *)a.rec_item, s));
     }
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker, t);
+    // this thread fills share 0 of each group, then queues the group's copies once every share is in
+    cudaError_t copy_err = cudaSuccess;
+    bool cs0 = false;
+    for (unsigned c = 0; c < K; ++c) {
+        {
+            const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
+            const uint32_t a0 = gb[c], a1 = nt == 1 ? gb[c + 1] : std::min(gb[c + 1], item_at(r0 + (r1 - r0) / nt));
+            if (a0 < a1) cs0 |= fill_items(a0, a1);
+        }
+        while (done[c].load(std::memory_order_acquire) + 1 < nt) std::this_thread::yield();
+        if (!R) continue;
+        const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
+        if (r1 == r0 || copy_err != cudaSuccess) continue;
+        const uint64_t m = r1 - r0;
+        cudaError_t e = cudaMemcpyAsync((void *)(a.rec_group + r0), rec_group + r0, m * 4, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync((void *)(a.rec_set + r0), rec_set + r0, m, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((void *)(a.rec_clear + r0), rec_clear + r0, m, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((void *)(a.rec_vals + 8 * r0), rec_vals + 8 * r0, m * 16, cudaMemcpyHostToDevice, s);
+        copy_err = e;
+    }
+    for (auto &th : pool) th.join();
+    clears[0] = cs0;
+    if (copy_err != cudaSuccess) return cuda_fail(it, copy_err, "record copy");
+    bool any_clear = false;
+    for (char c : clears) any_clear |= c != 0;
     int st1 = apply_sequence(it, a, any_clear && (it->flags & VX_PATCH_P4));
     if (st1 != VX_OK) return st1;
     std::vector<uint8_t> ch(n);

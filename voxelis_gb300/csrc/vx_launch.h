@@ -73,6 +73,10 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s);
 cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
 
+// rec_item[r] = i for the records [first[i], first[i+1]) of every item i < n (device memory).
+cudaError_t launch_expand_items(const uint32_t *first, uint32_t n, uint32_t *rec_item, cudaStream_t s);
+
+
 // ---- general batch apply (vx_apply.cu) ---------------------------------------------------------
 struct ApplyArgs {
     int mode;                    // 0: set phase (set_batch_at_depth_iterative); 1: clear pass (P4)
@@ -107,6 +111,7 @@ struct ApplyArgs {
     uint64_t *e_id[2];
     uint32_t *e_val[2];
     uint32_t *p_start;           // [n_records + 1]
+    uint32_t *it_first;           // [n_items + 1] first record of each item (host staging of an apply)
     uint64_t *rec_id;
     uint32_t *rec_val;
     uint64_t *release_list;      // [n_items]
