@@ -572,7 +572,10 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
     auto item_at = [&](uint64_t r) { return (uint32_t)(std::lower_bound(off.begin(), off.end() - 1, r) - off.begin()); };
     unsigned nt = std::thread::hardware_concurrency();
     nt = std::max(1u, std::min(nt, 16u));
-    const unsigned K = R >= (1u << 20) ? 4 : 1;  // record groups: the copy of one overlaps the fill of the next
+#ifndef VX_STAGE_GROUPS
+#define VX_STAGE_GROUPS 4
+#endif
+    const unsigned K = R >= (1u << 20) ? VX_STAGE_GROUPS : 1;  // record groups: the copy of one overlaps the fill of the next
     if (R < (1u << 16)) nt = 1;
     std::vector<uint32_t> gb(K + 1, n);
     gb[0] = 0;
