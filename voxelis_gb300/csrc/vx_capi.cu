@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <thread>
@@ -577,22 +578,43 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
 #endif
     const unsigned K = R >= (1u << 20) ? VX_STAGE_GROUPS : 1;  // record groups: the copy of one overlaps the fill of the next
     if (R < (1u << 16)) nt = 1;
+    // small tasks (item ranges of about R / (16 nt) records) taken from a counter in group order, so a
+    // thread the OS deschedules delays one task, not a fixed share of every group
+    std::vector<uint32_t> task_lo, task_hi;
+    std::vector<unsigned> task_group;
     std::vector<uint32_t> gb(K + 1, n);
     gb[0] = 0;
     for (unsigned c = 1; c < K; ++c) gb[c] = item_at(R * c / K);
-    std::vector<std::atomic<unsigned>> done(K);
-    for (auto &d : done) d.store(0);
-    std::vector<char> clears(nt, 0);
-    auto worker = [&](unsigned t) {  // share t >= 1 of every group
-        bool cs = false;
-        for (unsigned c = 0; c < K; ++c) {
-            const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
-            const uint32_t a0 = t == 0 ? gb[c] : std::max(gb[c], item_at(r0 + (r1 - r0) * t / nt));
-            const uint32_t a1 = t + 1 == nt ? gb[c + 1] : std::min(gb[c + 1], item_at(r0 + (r1 - r0) * (t + 1) / nt));
-            if (a0 < a1) cs |= fill_items(a0, a1);
-            done[c].fetch_add(1, std::memory_order_release);
+    const unsigned per_group = std::max(1u, 16 * nt / K);
+    for (unsigned c = 0; c < K; ++c) {
+        const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
+        uint32_t lo = gb[c];
+        for (unsigned k = 1; k <= per_group; ++k) {
+            const uint32_t hi = k == per_group ? gb[c + 1] : std::min(gb[c + 1], item_at(r0 + (r1 - r0) * k / per_group));
+            if (hi > lo) {
+                task_lo.push_back(lo);
+                task_hi.push_back(hi);
+                task_group.push_back(c);
+                lo = hi;
+            }
         }
-        clears[t] = cs;
+    }
+    const uint32_t n_tasks = (uint32_t)task_lo.size();
+    std::vector<std::atomic<unsigned>> left(K);
+    for (auto &x : left) x.store(0);
+    for (uint32_t t = 0; t < n_tasks; ++t) left[task_group[t]].fetch_add(1);
+    std::atomic<uint32_t> next_task{0};
+    std::vector<char> clears(nt, 0);
+    auto run_tasks = [&](const std::function<void()> &after_task) {
+        bool cs = false;
+        for (;;) {
+            const uint32_t t = next_task.fetch_add(1, std::memory_order_relaxed);
+            if (t >= n_tasks) break;
+            cs |= fill_items(task_lo[t], task_hi[t]);
+            left[task_group[t]].fetch_sub(1, std::memory_order_release);
+            if (after_task) after_task();
+        }
+        return cs;
     };
 
     ApplyArgs a{};
@@ -609,31 +631,31 @@ int run_apply(vx_interner *it, std::vector<Item> items, uint8_t *changed_out) {
         VX_CUDA(launch_expand_items(a.it_first, n, (uint32_t *)a.rec_item, s));
     }
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker, t);
-    // this thread fills share 0 of each group, then queues the group's copies once every share is in
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back([&, t] { clears[t] = run_tasks(nullptr); });
+    // this thread fills tasks too, and queues each record group's copies once its tasks are done
     cudaError_t copy_err = cudaSuccess;
-    bool cs0 = false;
-    for (unsigned c = 0; c < K; ++c) {
-        {
-            const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
-            const uint32_t a0 = gb[c], a1 = nt == 1 ? gb[c + 1] : std::min(gb[c + 1], item_at(r0 + (r1 - r0) / nt));
-            if (a0 < a1) cs0 |= fill_items(a0, a1);
+    unsigned copied = 0;
+    auto copy_ready = [&] {
+        while (copied < K && left[copied].load(std::memory_order_acquire) == 0) {
+            const uint64_t r0 = off[gb[copied]], r1 = off[gb[copied + 1]];
+            ++copied;
+            if (r1 == r0 || copy_err != cudaSuccess) continue;
+            const uint64_t m = r1 - r0;
+            cudaError_t e = cudaMemcpyAsync((void *)(a.rec_group + r0), rec_group + r0, m * 4, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync((void *)(a.rec_set + r0), rec_set + r0, m, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((void *)(a.rec_clear + r0), rec_clear + r0, m, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((void *)(a.rec_vals + 8 * r0), rec_vals + 8 * r0, m * 16, cudaMemcpyHostToDevice, s);
+            copy_err = e;
         }
-        while (done[c].load(std::memory_order_acquire) + 1 < nt) std::this_thread::yield();
-        if (!R) continue;
-        const uint64_t r0 = off[gb[c]], r1 = off[gb[c + 1]];
-        if (r1 == r0 || copy_err != cudaSuccess) continue;
-        const uint64_t m = r1 - r0;
-        cudaError_t e = cudaMemcpyAsync((void *)(a.rec_group + r0), rec_group + r0, m * 4, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync((void *)(a.rec_set + r0), rec_set + r0, m, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync((void *)(a.rec_clear + r0), rec_clear + r0, m, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync((void *)(a.rec_vals + 8 * r0), rec_vals + 8 * r0, m * 16, cudaMemcpyHostToDevice, s);
-        copy_err = e;
+    };
+    clears[0] = run_tasks(copy_ready);
+    while (copied < K) {
+        copy_ready();
+        if (copied < K) std::this_thread::yield();
     }
     for (auto &th : pool) th.join();
-    clears[0] = cs0;
     if (copy_err != cudaSuccess) return cuda_fail(it, copy_err, "record copy");
     bool any_clear = false;
     for (char c : clears) any_clear |= c != 0;
