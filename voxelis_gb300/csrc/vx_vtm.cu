@@ -166,10 +166,8 @@ __global__ void __launch_bounds__(kThreads) vtm_table_kernel(const uint8_t *b, u
 }
 
 // U[g][o] = the kFan child tables of group g applied in turn from entry o (one warp per group).
-__global__ void __launch_bounds__(kThreads) vtm_compose_kernel(const uint8_t *b, uint64_t n, const VtmSections *sec,
-                                                               int kind, uint32_t S, int level, const uint64_t *T,
-                                                               uint64_t *U) {
-    (void)b;
+__global__ void __launch_bounds__(kThreads) vtm_compose_kernel(uint64_t n, const VtmSections *sec, int kind, uint32_t S,
+                                                               int level, const uint64_t *T, uint64_t *U) {
     if (sec->count[kind] == 0) return;
     const Geometry geo = vtm_geometry(sec, kind, n, S);
     const uint32_t n_child = level == 1 ? geo.n0 : geo.n1, n_group = level == 1 ? geo.n1 : geo.n2;
@@ -440,10 +438,8 @@ cudaError_t launch_vtm_parse(const DevInterner &I, const uint8_t *bytes, uint64_
     for (int kind = 0; kind < 3; ++kind) {
         count_launches(5);
         vtm_table_kernel<<<blocks_for(z.n0, kThreads / 32), kThreads, 0, s>>>(bytes, n, sec, kind, vb, z.seg_bytes, T0);
-        vtm_compose_kernel<<<blocks_for(z.n1, kThreads / 32), kThreads, 0, s>>>(bytes, n, sec, kind, z.seg_bytes, 1,
-                                                                                T0, T1);
-        vtm_compose_kernel<<<blocks_for(z.n2, kThreads / 32), kThreads, 0, s>>>(bytes, n, sec, kind, z.seg_bytes, 2,
-                                                                                T1, T2);
+        vtm_compose_kernel<<<blocks_for(z.n1, kThreads / 32), kThreads, 0, s>>>(n, sec, kind, z.seg_bytes, 1, T0, T1);
+        vtm_compose_kernel<<<blocks_for(z.n2, kThreads / 32), kThreads, 0, s>>>(n, sec, kind, z.seg_bytes, 2, T1, T2);
         vtm_down_kernel<<<1, 1024, 0, s>>>(n, sec, kind, z.seg_bytes, T0, T1, T2, E0, E1, E2);
         vtm_emit_kernel<<<(unsigned)((z.n0 + kThreads - 1) / kThreads), kThreads, 0, s>>>(
             I, bytes, n, sec, kind, vb, z.seg_bytes, E0, offs[kind], caps[kind]);
