@@ -28,8 +28,10 @@
 //
 // Refcounts follow from the reference's accounting (interner/mod.rs:712-829): a hash-cons hit gives
 // back the references its children were pre-charged with, so after a build every node's count equals
-// the number of child slots of newly created nodes that name it, plus one per tree root. That sum is
-// computed once per epoch over the allocation log (launch_epoch_refcounts) instead of per lookup.
+// the number of child slots of newly created nodes that name it, plus one per tree root. The split
+// path of 8-bit interners adds it as it creates nodes (the creating lane counts the new node's
+// children; leaf children into per-CTA value counters) and its last kernel closes the epoch; the
+// other builds compute the sum once per epoch over the allocation log (launch_epoch_refcounts).
 #include <cuda.h>
 #include <mutex>
 #include <type_traits>
@@ -361,8 +363,97 @@ __device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64
 
 // One parent from 8 children held by the calling lane: EMPTY, a collapsed leaf, or an interned
 // branch (warp-cooperative; every lane of the warp calls it).
+// One reference per child slot of branch `id`, which the calling lane just created (equal children
+// summed first): leaves of 8-bit interners into the CTA's per-value counters when leaf_cnt is given
+// (added to the leaves by leaf_cnt_flush), everything else by fire-and-forget atomics. The children
+// are read back from the record just written rather than kept live in registers across the insert.
+__device__ __forceinline__ void count_created(const DevInterner &I, uint32_t *leaf_cnt, uint64_t id) {
+    uint64_t c[8];
+    const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(I.children + 8ull * id_index(id));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const ulonglong2 w = src[k];
+        c[2 * k] = w.x;
+        c[2 * k + 1] = w.y;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (c[k] == EMPTY_ID) continue;
+        bool seen = false;
+        uint32_t n = 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < k && c[j] == c[k]) seen = true;
+            if (j > k && c[j] == c[k]) ++n;
+        }
+        if (seen) continue;
+        if (leaf_cnt && id_is_leaf(c[k]))
+            atomicAdd(leaf_cnt + (node_value(I, id_index(c[k])) & 0xFFu), n);
+        else
+            atomicAdd(I.refcount + id_index(c[k]), n);
+    }
+}
+
+// The same from children and values still held in registers (no read-back of the record).
+__device__ __forceinline__ void count_created_regs(const DevInterner &I, uint32_t *leaf_cnt, const uint64_t c[8],
+                                                   const uint32_t cv[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (c[k] == EMPTY_ID) continue;
+        bool seen = false;
+        uint32_t n = 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < k && c[j] == c[k]) seen = true;
+            if (j > k && c[j] == c[k]) ++n;
+        }
+        if (seen) continue;
+        if (leaf_cnt && id_is_leaf(c[k]))
+            atomicAdd(leaf_cnt + (cv[k] & 0xFFu), n);
+        else
+            atomicAdd(I.refcount + id_index(c[k]), n);
+    }
+}
+
+// A created bottom group of an 8-bit interner: its children are the leaves of its nonzero voxel
+// values, so the per-value counters take them straight from the values.
+__device__ __forceinline__ void count_group_leaves(uint32_t *leaf_cnt, const uint32_t v[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (v[k] == 0) continue;
+        bool seen = false;
+        uint32_t n = 1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < k && v[j] == v[k]) seen = true;
+            if (j > k && v[j] == v[k]) ++n;
+        }
+        if (!seen) atomicAdd(leaf_cnt + (v[k] & 0xFFu), n);
+    }
+}
+
+// Adds a CTA's per-value leaf counts to the leaves (every thread of the CTA calls it).
+__device__ __forceinline__ void leaf_cnt_flush(const DevInterner &I, uint32_t *leaf_cnt) {
+    __syncthreads();
+    for (unsigned v = threadIdx.x; v < 256; v += blockDim.x) {
+        const uint32_t n = leaf_cnt[v];
+        if (n == 0) continue;
+        const uint64_t lid = I.leaf_table[v];
+        if (lid > LEAF_BUSY)
+            atomicAdd(I.refcount + id_index(lid), n);
+        else
+            set_error(I, ERR_INTERNAL, 31);
+    }
+}
+
+__device__ __forceinline__ void leaf_cnt_clear(uint32_t *leaf_cnt) {
+    for (unsigned v = threadIdx.x; v < 256; v += blockDim.x) leaf_cnt[v] = 0;
+}
+
+// created (optional): whether this lane created the branch, for callers that count references.
 __device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active, const uint64_t c[8],
-                                              const uint32_t cv[8], uint64_t &out, uint32_t &out_val) {
+                                              const uint32_t cv[8], uint64_t &out, uint32_t &out_val,
+                                              bool *created_out = nullptr) {
     uint32_t types = 0, mask = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -376,6 +467,7 @@ __device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active,
     const uint32_t lod = is_branch ? calc_average8(cv) : 0;
     bool created;
     const uint64_t id = warp_intern_branch(I, is_branch, c, types, mask, lod, &created);
+    if (created_out) *created_out = created;
     if (mask == 0) {
         out = EMPTY_ID;
         out_val = 0;
@@ -415,6 +507,7 @@ struct OctArgs {
     uint32_t memo_mask;              // slots - 1
     uint32_t memo_cap;               // records
     unsigned long long *work;        // octants handed out beyond the first one per warp (nullptr: fixed stride)
+    int count_refs;                  // creators count their children's references (no epoch pass)
 };
 
 constexpr int kOctWarps = 8;
@@ -702,7 +795,8 @@ __device__ __forceinline__ void memo_claim(const OctArgs &a, uint32_t h1, uint32
 // every lane calls it; lanes with active == false only take part in the ballots.
 template <class T, int S>
 __device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache &C, uint64_t *leaf_cache,
-                                            const T *qbase, bool active, uint64_t &qid, uint32_t &qval) {
+                                            const T *qbase, bool active, uint64_t &qid, uint32_t &qval,
+                                            bool count = false) {
     const unsigned lane = threadIdx.x & 31u;
     const bool wide = sizeof(T) == 2;
     uint64_t c3[8];
@@ -747,6 +841,7 @@ __device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache
             for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
             bool created;
             uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+            if (count && created) count_created(I, nullptr, nid);
             nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
             if (lead && nid != EMPTY_ID) kc_insert(C, lo, hi, nid, lod);
             if (need) id = nid;
@@ -762,7 +857,9 @@ __device__ __forceinline__ void quad_groups(const DevInterner &I, const KeyCache
             cv3[k] = lod;
         }
     }
-    reduce_parent(I, active, c3, cv3, qid, qval);
+    bool qc = false;
+    reduce_parent(I, active, c3, cv3, qid, qval, &qc);
+    if (count && qc) count_created(I, nullptr, qid);
 }
 
 template <class T>
@@ -1432,7 +1529,7 @@ __device__ __forceinline__ void quads_of_tile(const DevInterner &I, const OctArg
         if (__any_sync(0xFFFFFFFFu, active)) {
             uint64_t pid;
             uint32_t pval;
-            quad_groups<T, S>(I, C, leaf_cache, qb[p], active, pid, pval);
+            quad_groups<T, S>(I, C, leaf_cache, qb[p], active, pid, pval, a.count_refs != 0);
             if (active) {
                 qidv[p] = pid;
                 qvalv[p] = pval;
@@ -1587,6 +1684,10 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
     for (unsigned k = tid; k < kKeyCache; k += blockDim.x) C.id[k] = 0;
     if (sizeof(T) == 1)
         leaf_cache_warm(I, leaf_cache, tid);
+    __shared__ uint32_t leaf_cnt_s[256];
+    const bool count = sizeof(T) == 1 && a.count_refs != 0;  // 8-bit interners only
+    uint32_t *leaf_cnt = count ? leaf_cnt_s : nullptr;
+    if (leaf_cnt) leaf_cnt_clear(leaf_cnt);
     __syncthreads();
     using W = typename QuadWord<T>::type;
     const bool wide = sizeof(T) == 2;
@@ -1640,6 +1741,12 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
             for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
             bool created;
             uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
+            if (count && created) {
+                if (leaf_cnt)
+                    count_group_leaves(leaf_cnt, v);
+                else
+                    count_created(I, nullptr, nid);
+            }
             nid = __shfl_sync(0xFFFFFFFFu, nid, leader);
             if (lead && nid != EMPTY_ID) kc_insert(C, lo, hi, nid, lod);
             if (need) id = nid;
@@ -1665,16 +1772,20 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
         }
         uint64_t qid;
         uint32_t qval;
-        reduce_parent(I, act && k == 0, c3, cv3, qid, qval);
+        bool qc = false;
+        reduce_parent(I, act && k == 0, c3, cv3, qid, qval, &qc);
+        if (count && qc) count_created_regs(I, leaf_cnt, c3, cv3);
         if (act && k == 0) *tail = make_uint4((uint32_t)qid, (uint32_t)(qid >> 32), qval, 0u);
     }
+    if (leaf_cnt) leaf_cnt_flush(I, leaf_cnt);
 }
 
 // One parent per lane from its 8 children: EMPTY, a collapsed leaf, or the interned branch.
 // Identical parents of the warp (common in repetitive terrain) probe the table once. Warp-collective:
 // every lane calls it; lanes with in == false only take part.
 __device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool in, const uint64_t c[8],
-                                                    const uint32_t cv[8], uint64_t &out, uint32_t &val) {
+                                                    const uint32_t cv[8], uint64_t &out, uint32_t &val,
+                                                    bool *created_out = nullptr) {
     uint32_t types = 0, mask = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -1700,6 +1811,7 @@ __device__ __forceinline__ void reduce_parent_dedup(const DevInterner &I, bool i
     const uint32_t lod = probe ? calc_average8(cv) : 0;
     bool created;
     uint64_t id = warp_intern_branch_inl(I, probe, c, types, mask, lod, &created, h);
+    if (created_out) *created_out = created;
     const uint64_t lead_id = __shfl_sync(0xFFFFFFFFu, id, leader);
     const uint32_t lead_lod = __shfl_sync(0xFFFFFFFFu, lod, leader);
     if (follow) id = lead_id;
@@ -1740,9 +1852,16 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
                                                                const uint32_t *in_vals, uint64_t *out_ids,
                                                                uint32_t *out_vals, uint64_t n_parents, int is_root,
                                                                const uint32_t *trees, uint8_t *changed,
-                                                               PendingView P) {
+                                                               PendingView P, int count_refs) {
     pdl_wait();
     pdl_release();
+    __shared__ uint32_t leaf_cnt_s[256];
+    const bool count = count_refs != 0;
+    uint32_t *leaf_cnt = (count && I.vbits == 8) ? leaf_cnt_s : nullptr;
+    if (leaf_cnt) {
+        leaf_cnt_clear(leaf_cnt);
+        __syncthreads();
+    }
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_parents; base += stride) {
         const uint64_t p = base + threadIdx.x;
@@ -1757,7 +1876,8 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
         }
         uint64_t out;
         uint32_t val;
-        reduce_parent_dedup(I, in, c, cv, out, val);
+        bool created = false;
+        reduce_parent_dedup(I, in, c, cv, out, val, &created);
         if (!in) continue;
         if (is_root) {
             commit_root(I, trees, changed, p, out);
@@ -1765,7 +1885,9 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
             out_ids[p] = out;
             out_vals[p] = val;
         }
+        if (count && created) count_created(I, leaf_cnt, out);
     }
+    if (leaf_cnt) leaf_cnt_flush(I, leaf_cnt);
 }
 
 // The three top levels (depths 2, 1 and 0: 64 + 8 + 1 nodes a chunk) with one warp per chunk and
@@ -1777,50 +1899,66 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
 __global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, const uint64_t *in_ids,
                                                                   const uint32_t *in_vals, uint32_t n_chunks,
                                                                   const uint32_t *trees, uint8_t *changed,
-                                                                  PendingView P) {
+                                                                  PendingView P, int count_refs) {
     pdl_wait();
     pdl_release();
+    __shared__ uint32_t leaf_cnt_s[256];
+    const bool count = count_refs != 0;
+    uint32_t *leaf_cnt = (count && I.vbits == 8) ? leaf_cnt_s : nullptr;
+    if (leaf_cnt) {
+        leaf_cnt_clear(leaf_cnt);
+        __syncthreads();
+    }
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t c = (uint64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-    if (c >= n_chunks) return;  // the whole warp
-    uint64_t d2[2];
-    uint32_t v2[2];
+    if (c < n_chunks) {  // the whole warp
+        uint64_t d2[2];
+        uint32_t v2[2];
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {  // depth 2: parent lane + 32 r of the chunk
-        const uint64_t p = c * 64 + lane + 32u * r;
+        for (int r = 0; r < 2; ++r) {  // depth 2: parent lane + 32 r of the chunk
+            const uint64_t p = c * 64 + lane + 32u * r;
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = in_ids[8 * p + k];
+                cv[k] = in_vals[8 * p + k];
+                resolve_pending(P, ch[k], cv[k]);
+            }
+            bool created = false;
+            reduce_parent_dedup(I, true, ch, cv, d2[r], v2[r], &created);
+            if (count && created) count_created(I, leaf_cnt, d2[r]);
+        }
+        // depth 1: lane q < 8 takes depth-2 nodes 8q .. 8q+7 (pass q >> 2)
         uint64_t ch[8];
         uint32_t cv[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            ch[k] = in_ids[8 * p + k];
-            cv[k] = in_vals[8 * p + k];
-            resolve_pending(P, ch[k], cv[k]);
+            const int src = (8 * lane + k) & 31;
+            const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, d2[0], src), a1 = __shfl_sync(0xFFFFFFFFu, d2[1], src);
+            const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, v2[0], src), b1 = __shfl_sync(0xFFFFFFFFu, v2[1], src);
+            ch[k] = lane < 4 ? a0 : a1;
+            cv[k] = lane < 4 ? b0 : b1;
         }
-        reduce_parent_dedup(I, true, ch, cv, d2[r], v2[r]);
-    }
-    // depth 1: lane q < 8 takes depth-2 nodes 8q .. 8q+7 (pass q >> 2)
-    uint64_t ch[8];
-    uint32_t cv[8];
+        uint64_t d1;
+        uint32_t v1;
+        bool created = false;
+        reduce_parent_dedup(I, lane < 8, ch, cv, d1, v1, &created);
+        if (count && created) count_created(I, leaf_cnt, d1);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int src = (8 * lane + k) & 31;
-        const uint64_t a0 = __shfl_sync(0xFFFFFFFFu, d2[0], src), a1 = __shfl_sync(0xFFFFFFFFu, d2[1], src);
-        const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, v2[0], src), b1 = __shfl_sync(0xFFFFFFFFu, v2[1], src);
-        ch[k] = lane < 4 ? a0 : a1;
-        cv[k] = lane < 4 ? b0 : b1;
+        for (int k = 0; k < 8; ++k) {  // the root from lanes 0-7
+            ch[k] = __shfl_sync(0xFFFFFFFFu, d1, k);
+            cv[k] = __shfl_sync(0xFFFFFFFFu, v1, k);
+        }
+        uint64_t root;
+        uint32_t rv;
+        reduce_parent_dedup(I, lane == 0, ch, cv, root, rv, &created);
+        if (lane == 0) commit_root(I, trees, changed, c, root);
+        if (count && created) count_created(I, leaf_cnt, root);
     }
-    uint64_t d1;
-    uint32_t v1;
-    reduce_parent_dedup(I, lane < 8, ch, cv, d1, v1);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {  // the root from lanes 0-7
-        ch[k] = __shfl_sync(0xFFFFFFFFu, d1, k);
-        cv[k] = __shfl_sync(0xFFFFFFFFu, v1, k);
-    }
-    uint64_t root;
-    uint32_t rv;
-    reduce_parent_dedup(I, lane == 0, ch, cv, root, rv);
-    if (lane == 0) commit_root(I, trees, changed, c, root);
+    if (leaf_cnt) leaf_cnt_flush(I, leaf_cnt);
+    // counting builds: the last CTA closes the epoch (every creation of the build is done by then)
+    if (count && grid_last_cta(&I.ctr->scratch[SC_REF_DONE])) epoch_finalize_body(I);
 }
 
 // Adds one reference per child slot of every node created in this epoch. Leaf references are the hot spots of the in-degree count (a few leaf values are named by most
@@ -2147,12 +2285,23 @@ size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth) {
 
 static cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
                                       uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
-                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P);
+                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P,
+                                      int count_refs);
+
+// The split path's creators add their children's references as they create nodes (8-bit interners,
+// whose leaf references sum in 256 per-CTA counters); the epoch then needs only closing, not the
+// in-degree pass over the allocation log. A creator's child id comes from the child's own creation
+// (shuffle, shared key cache, table) after the child creator's release store, which is issued only
+// once the child's zeroed count is visible, so no count lands before that zero.
+#ifndef VX_SPLIT_REFS
+#define VX_SPLIT_REFS 1
+#endif
+bool dense_split_counts_refs(const DevInterner &I) { return VX_SPLIT_REFS && I.vbits == 8; }
 
 cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
                                bool clear_memo, uint64_t memo_chunks, void (*levels_begin)(void *),
-                               void *levels_ctx) {
+                               void *levels_ctx, bool count_refs) {
     if (n_chunks == 0) return cudaSuccess;
     if (depth < 5 || depth > 10) return cudaErrorInvalidValue;
     OctArgs a{};
@@ -2161,6 +2310,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     a.depth = depth;
     a.changed = changed;
     a.grids = grids;
+    a.count_refs = (count_refs && dense_split_counts_refs(I)) ? 1 : 0;
     if (memo) {
         uint64_t sl, rc;
         memo_geometry(memo_chunks ? memo_chunks : n_chunks, depth, I.memo_shift, &sl, &rc);
@@ -2230,7 +2380,7 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     for (int k = depth - 3; k >= 3; --k) {  // the first pass reads the quads
         const uint64_t np = (uint64_t)n_chunks << (3 * k);
         e = launch_fresh_level(I, ids + off[k + 1], vals + off[k + 1], ids + off[k], vals + off[k], np, false, trees,
-                               changed, s, k == depth - 3 ? P : PendingView{nullptr, 0, 0});
+                               changed, s, k == depth - 3 ? P : PendingView{nullptr, 0, 0}, a.count_refs);
         if (e != cudaSuccess) return e;
     }
     // depths 2, 1 and 0 in one launch
@@ -2238,19 +2388,20 @@ cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const ui
     const unsigned wb = (unsigned)((n_chunks + kThreads / 32 - 1) / (kThreads / 32));
     return launch_pdl(fresh_top_kernel, dim3(wb), dim3(kThreads), 0, s, I, (const uint64_t *)(ids + off[3]),
                       (const uint32_t *)(vals + off[3]), n_chunks, trees, changed,
-                      depth == 5 ? P : PendingView{nullptr, 0, 0});
+                      depth == 5 ? P : PendingView{nullptr, 0, 0}, a.count_refs);
 }
 
 // One level of fresh parents: n_parents = n_chunks * 8^k; children pending in P are resolved first.
 static cudaError_t launch_fresh_level(const DevInterner &I, const uint64_t *in_ids, const uint32_t *in_vals,
                                       uint64_t *out_ids, uint32_t *out_vals, uint64_t n_parents, bool is_root,
-                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P) {
+                                      const uint32_t *trees, uint8_t *changed, cudaStream_t s, PendingView P,
+                                      int count_refs) {
     if (n_parents == 0) return cudaSuccess;
     uint64_t blocks = (n_parents + kThreads - 1) / kThreads;
     if (blocks > 65535) blocks = 65535;
     count_launches(1);
     return launch_pdl(fresh_level_kernel, dim3((unsigned)blocks), dim3(kThreads), 0, s, I, in_ids, in_vals, out_ids,
-                      out_vals, n_parents, is_root ? 1 : 0, trees, changed, P);
+                      out_vals, n_parents, is_root ? 1 : 0, trees, changed, P, count_refs);
 }
 
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s) {

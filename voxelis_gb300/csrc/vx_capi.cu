@@ -713,8 +713,9 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
         const size_t sb = (dense_split_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits, it->dev.memo_shift)));
         PhaseSwitch ps(it, VX_PROF_DENSE, VX_PROF_LEVELS);
+        // one piece: its creators count references (no in-degree pass over the allocation log)
         VX_CUDA(launch_dense_split(it->dev, d_grids, d_trees, n, depth, d_changed, it->ws.p, it->num_sms, s,
-                                   static_cast<char *>(it->ws.p) + sb, true, 0, &PhaseSwitch::next, &ps));
+                                   static_cast<char *>(it->ws.p) + sb, true, 0, &PhaseSwitch::next, &ps, true));
     } else if (depth == 4) {  // one warp per chunk
         const size_t sb = (dense_octant_scratch_bytes(n, depth) + 255) & ~(size_t)255;
         VX_CUDA(it->ws.reserve(sb + dense_octant_memo_bytes(n, depth, it->vbits, it->dev.memo_shift)));
@@ -731,6 +732,7 @@ int dense_fast(vx_interner *it, uint32_t n, const uint32_t *d_trees, const void 
         Phase ph(it, VX_PROF_DENSE);
         VX_CUDA(launch_dense_blocks(it->dev, a, it->num_sms, s));
     }
+    if (depth >= 5 && dense_split_counts_refs(it->dev)) return VX_OK;  // counted and closed by the build
     Phase ph(it, VX_PROF_REFCOUNT);
     VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
     return VX_OK;
@@ -1542,7 +1544,7 @@ int vx_build_dense(vx_interner *it, uint32_t n, const vx_tree *trees, const void
             }
             first = false;
         }
-        {
+        {  // pieces count by one in-degree pass: counting in each piece's kernels measured slower here
             Phase ph(it, VX_PROF_REFCOUNT);
             VX_CUDA(launch_epoch_refcounts(it->dev, it->num_sms, s));
         }

@@ -68,9 +68,13 @@ size_t dense_split_scratch_bytes(uint64_t n_chunks, int depth);
 cudaError_t launch_dense_split(const DevInterner &I, const void *grids, const uint32_t *trees, uint32_t n_chunks,
                                int depth, uint8_t *changed, void *scratch, int num_sms, cudaStream_t s, void *memo,
                                bool clear_memo = true, uint64_t memo_chunks = 0,
-                               void (*levels_begin)(void *) = nullptr, void *levels_ctx = nullptr);
+                               void (*levels_begin)(void *) = nullptr, void *levels_ctx = nullptr,
+                               bool count_refs = false);
 // In-degree refcounts of the nodes created in the current epoch, then closes the epoch.
 cudaError_t launch_epoch_refcounts(const DevInterner &I, int num_sms, cudaStream_t s);
+// Whether launch_dense_split, asked to (count_refs), counts references as it creates nodes and closes
+// the epoch itself; otherwise the caller runs launch_epoch_refcounts after it.
+bool dense_split_counts_refs(const DevInterner &I);
 cudaError_t launch_epoch_finalize(const DevInterner &I, cudaStream_t s);
 
 // rec_item[r] = i for the records [first[i], first[i+1]) of every item i < n (device memory).
