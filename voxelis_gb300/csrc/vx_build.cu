@@ -1890,6 +1890,10 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_level_kernel(DevInterner I,
     if (leaf_cnt) leaf_cnt_flush(I, leaf_cnt);
 }
 
+#ifndef VX_TOP_COMPACT
+#define VX_TOP_COMPACT 1  // fresh_top_kernel packs the depth-2 parents that need an insert into one round
+#endif
+
 // The three top levels (depths 2, 1 and 0: 64 + 8 + 1 nodes a chunk) with one warp per chunk and
 // no CTA barrier: lanes reduce the chunk's 64 depth-2 parents in two passes, lanes 0-7 its 8 depth-1
 // parents from those (shuffles), lane 0 the root. 8 chunks per CTA; a 4096-chunk build is one wave
@@ -1903,6 +1907,13 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, c
     pdl_wait();
     pdl_release();
     __shared__ uint32_t leaf_cnt_s[256];
+#if VX_TOP_COMPACT
+    __shared__ uint64_t top_ch[kThreads * 8];  // per warp: 32 packed depth-2 parents x 8 children
+    __shared__ uint32_t top_cv[kThreads * 8];
+    __shared__ uint64_t top_rid[kThreads * 2];  // per warp: the chunk's 64 depth-2 results
+    __shared__ uint32_t top_rval[kThreads * 2];
+    __shared__ uint8_t top_par[kThreads];       // per warp: the parent of each packed slot
+#endif
     const bool count = count_refs != 0;
     uint32_t *leaf_cnt = (count && I.vbits == 8) ? leaf_cnt_s : nullptr;
     if (leaf_cnt) {
@@ -1912,6 +1923,105 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, c
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t c = (uint64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
     if (c < n_chunks) {  // the whole warp
+#if VX_TOP_COMPACT
+        // depth 2: parent lane + 32 r of the chunk. Parents that are EMPTY or collapse to a leaf are
+        // settled at once; the others (the surface layer, usually at most 32 of the 64) are packed
+        // into the warp's shared slots and interned in one round instead of one per half. Results go
+        // to the warp's shared row of 64, where the depth-1 lanes read them.
+        const unsigned wslot = threadIdx.x >> 5;
+        uint64_t *sch = top_ch + wslot * 32 * 8;
+        uint32_t *scv = top_cv + wslot * 32 * 8;
+        uint64_t *rid = top_rid + wslot * 64;
+        uint32_t *rval = top_rval + wslot * 64;
+        uint8_t *spar = top_par + wslot * 32;
+        unsigned nneed = 0;
+        bool over = false;  // this lane's second-half parent did not get a slot
+#pragma unroll 1
+        for (int r = 0; r < 2; ++r) {
+            const uint64_t p = c * 64 + lane + 32u * r;
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = in_ids[8 * p + k];
+                cv[k] = in_vals[8 * p + k];
+                resolve_pending(P, ch[k], cv[k]);
+            }
+            uint32_t mask = 0;
+            bool same = true;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                mask |= (ch[k] != 0 ? 1u : 0u) << k;
+                same = same && id_is_leaf(ch[k]) && ch[k] == ch[0];
+            }
+            const bool need = mask != 0 && !same;
+            const unsigned b = __ballot_sync(0xFFFFFFFFu, need);
+            const unsigned slot = nneed + __popc(b & ((1u << lane) - 1u));
+            nneed += __popc(b);
+            if (need && slot < 32) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    sch[slot * 8 + k] = ch[k];
+                    scv[slot * 8 + k] = cv[k];
+                }
+                spar[slot] = (uint8_t)(lane + 32u * r);
+            }
+            over = over || (need && slot >= 32);
+            rid[lane + 32u * r] = mask == 0 ? EMPTY_ID : ch[0];
+            rval[lane + 32u * r] = mask == 0 ? 0u : cv[0];
+        }
+        __syncwarp();
+        {
+            const bool in = lane < nneed;
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = in ? sch[lane * 8 + k] : 0ull;
+                cv[k] = in ? scv[lane * 8 + k] : 0u;
+            }
+            uint64_t out;
+            uint32_t val;
+            bool created = false;
+            reduce_parent_dedup(I, in, ch, cv, out, val, &created);
+            if (count && created) count_created(I, leaf_cnt, out);
+            if (in) {
+                const unsigned q = spar[lane];
+                rid[q] = out;
+                rval[q] = val;
+            }
+        }
+        if (__any_sync(0xFFFFFFFFu, over)) {  // second-half parents past the 32 slots: one more round
+            const uint64_t p = c * 64 + lane + 32u;
+            uint64_t ch[8];
+            uint32_t cv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                ch[k] = over ? in_ids[8 * p + k] : 0ull;
+                cv[k] = over ? in_vals[8 * p + k] : 0u;
+                resolve_pending(P, ch[k], cv[k]);
+            }
+            uint64_t out;
+            uint32_t val;
+            bool created = false;
+            reduce_parent_dedup(I, over, ch, cv, out, val, &created);
+            if (count && created) count_created(I, leaf_cnt, out);
+            if (over) {
+                rid[lane + 32u] = out;
+                rval[lane + 32u] = val;
+            }
+        }
+        __syncwarp();
+        // depth 1: lane q < 8 takes depth-2 nodes 8q .. 8q+7
+        uint64_t ch[8];
+        uint32_t cv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const unsigned src = (8 * lane + k) & 63u;
+            ch[k] = rid[src];
+            cv[k] = rval[src];
+        }
+#else
         uint64_t d2[2];
         uint32_t v2[2];
 #pragma unroll
@@ -1940,6 +2050,7 @@ __global__ void __launch_bounds__(kThreads, 4) fresh_top_kernel(DevInterner I, c
             ch[k] = lane < 4 ? a0 : a1;
             cv[k] = lane < 4 ? b0 : b1;
         }
+#endif
         uint64_t d1;
         uint32_t v1;
         bool created = false;
