@@ -291,10 +291,23 @@ __device__ __forceinline__ void epoch_finalize_body(const DevInterner &I) {
     c->alloc_count = 0;
 }
 
-// Writes a new branch record (children, LOD value, fingerprint, live id); rc starts at 0.
+// Slots past next_index have never held a node since the interner was created or reset (the bump
+// allocator hands each out once, recycling only bumps the generation of slots handed out before,
+// and creation, reset and model loading zero the generations), so their generation is 0: a ticket
+// past the free list needs no dependent load of it.
+#ifndef VX_FRESH_GEN
+#define VX_FRESH_GEN 1
+#endif
+__device__ __forceinline__ uint32_t slot_generation(const DevInterner &I, uint32_t idx, bool bumped) {
+    return (VX_FRESH_GEN && bumped) ? 0u : (uint32_t)I.generation[idx];
+}
+
+// Writes a new branch record (children, LOD value, fingerprint, live id); rc starts at 0. bumped: idx
+// came from past the free list (generation 0).
 __device__ __forceinline__ uint64_t write_branch(const DevInterner &I, uint32_t idx, const uint64_t c[8],
-                                                 uint32_t types, uint32_t mask, uint64_t h, uint32_t lod) {
-    uint32_t gen = I.generation[idx];
+                                                 uint32_t types, uint32_t mask, uint64_t h, uint32_t lod,
+                                                 bool bumped = false) {
+    uint32_t gen = slot_generation(I, idx, bumped);
     uint64_t id = make_branch_id(idx, gen, types, mask);
     ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(I.children + 8ull * idx);
     dst[0] = make_ulonglong2(c[0], c[1]);
@@ -403,7 +416,7 @@ __device__ __forceinline__ uint64_t warp_intern_branch_inl(const DevInterner &I,
                     set_error(I, ERR_OOM, 1);
                     atomicExch((unsigned long long *)(I.table + pos), SLOT_TOMB);
                 } else {
-                    result = write_branch(I, idx, c, types, mask, h, lod);
+                    result = write_branch(I, idx, c, types, mask, h, lod, base + rank >= fc);
                     publish_release((unsigned long long *)(I.table + pos), make_slot(tag, idx));
                     *created = true;
                 }
@@ -438,18 +451,20 @@ __device__ __forceinline__ uint64_t intern_leaf(const DevInterner &I, uint32_t v
     unsigned long long *slot = (unsigned long long *)(I.leaf_table + v);
     uint64_t s = ld_volatile(I.leaf_table + v);
     if (s > LEAF_BUSY) return s;
+    // constant during an epoch: loaded before the claim instead of after the ticket
+    const unsigned long long fc = I.ctr->free_count, ni = I.ctr->next_index;
     for (uint32_t spin = 0; spin < I.spin_limit; ++spin) {
         if (s == 0) {  // free (or its creator ran out of memory and backed off): claim it
             const uint64_t prev = atomicCAS(slot, 0ull, LEAF_BUSY);
             if (prev == 0) {
                 const unsigned long long t = atomicAdd(&I.ctr->alloc_count, 1ull);
-                const uint32_t idx = node_for_ticket(I, t);
+                const uint32_t idx = node_for_ticket(I, t, fc, ni);
                 if (idx == NO_NODE) {
                     set_error(I, ERR_OOM, 2);
                     atomicExch(slot, 0ull);
                     return EMPTY_ID;
                 }
-                const uint64_t id = make_leaf_id(idx, I.generation[idx]);
+                const uint64_t id = make_leaf_id(idx, slot_generation(I, idx, t >= fc));
                 set_node_value(I, idx, v);
                 I.hash[idx] = 0;
                 I.refcount[idx] = 0;
