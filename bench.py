@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Benchmark of the batched dense-chunk build (the spec workload) on GB300.
+"""Benchmark of the batched dense-chunk build (4096 perlin-dune chunks of 32^3 u8) on GB300.
 
 Workload (one step): intern 4096 perlin-dune chunks of 32^3 u8 voxels, tiled 64 x 64 in XZ, into one
 device-resident interner with a single batched call (vx_build_dense_async). Inputs are resident in
