@@ -109,6 +109,36 @@ __device__ __forceinline__ uint64_t leaf_of(const DevInterner &I, uint64_t *leaf
     return intern_leaf(I, v, &created);
 }
 
+// leaf_of for 8-bit voxels with one global lookup per CTA and value: the first lane to miss the CTA's
+// cache claims the value in `claim` and finds or creates the leaf; the others wait (bounded) on the
+// shared cache, so a leaf that every warp of the grid needs at once is awaited in shared memory, not
+// by thousands of lanes re-reading one leaf-table word. A claimer that fails marks the value (2) and
+// the waiters go to the table themselves.
+#ifndef VX_LEAF_CLAIM
+#define VX_LEAF_CLAIM 1
+#endif
+__device__ __forceinline__ uint64_t leaf_of_claimed(const DevInterner &I, uint64_t *leaf_cache, uint32_t *claim,
+                                                    uint32_t v) {
+    uint64_t id = *(volatile uint64_t *)(leaf_cache + v);
+    if (id) return id;
+    bool created;
+    if (atomicCAS(claim + v, 0u, 1u) == 0u) {
+        id = intern_leaf(I, v, &created);
+        if (id != EMPTY_ID)
+            *(volatile uint64_t *)(leaf_cache + v) = id;
+        else
+            *(volatile uint32_t *)(claim + v) = 2u;
+        return id;
+    }
+    for (uint32_t spin = 0; spin < (1u << 16); ++spin) {
+        id = *(volatile uint64_t *)(leaf_cache + v);
+        if (id) return id;
+        if (*(volatile uint32_t *)(claim + v) == 2u) break;
+        __nanosleep(32);
+    }
+    return intern_leaf(I, v, &created);
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads) dense_blocks_kernel(DevInterner I, DenseArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1705,6 +1735,9 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
     if (sizeof(T) == 1)
         leaf_cache_warm(I, leaf_cache, tid);
     __shared__ uint32_t leaf_cnt_s[256];
+    __shared__ uint32_t leaf_claim[256];
+    if (sizeof(T) == 1)
+        for (unsigned k = tid; k < 256; k += blockDim.x) leaf_claim[k] = 0;
     const bool count = sizeof(T) == 1 && a.count_refs != 0;  // 8-bit interners only
     uint32_t *leaf_cnt = count ? leaf_cnt_s : nullptr;
     if (leaf_cnt) leaf_cnt_clear(leaf_cnt);
@@ -1758,7 +1791,19 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
             const bool lead = need && leader == (int)lane;
             uint64_t c[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) c[j] = (lead && v[j]) ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+            for (int j = 0; j < 8; ++j) {
+                const bool want = lead && v[j] != 0;
+                if (sizeof(T) == 1 && VX_LEAF_CLAIM) {  // one lookup per warp and value
+                    const unsigned peers = __match_any_sync(0xFFFFFFFFu, want ? v[j] : 0x100u + lane);
+                    const int ldr = __ffs(peers) - 1;
+                    uint64_t lid = 0;
+                    if (want && ldr == (int)lane) lid = leaf_of_claimed(I, leaf_cache, leaf_claim, v[j]);
+                    lid = __shfl_sync(0xFFFFFFFFu, lid, ldr);
+                    c[j] = want ? lid : 0ull;
+                } else {
+                    c[j] = want ? leaf_of<T>(I, leaf_cache, v[j]) : 0ull;
+                }
+            }
             bool created;
             uint64_t nid = warp_intern_branch(I, lead, c, set, set, lod, &created);
             if (count && created) {
@@ -1771,13 +1816,23 @@ __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevI
             if (lead && nid != EMPTY_ID) kc_insert(C, lo, hi, nid, lod);
             if (need) id = nid;
         }
+        const bool gleaf = act && set != 0 && !is_branch;  // a uniform group: its leaf
+        uint64_t glid = 0;
+        if (sizeof(T) == 1 && VX_LEAF_CLAIM) {  // one lookup per warp and value
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, gleaf ? gv0 : 0x100u + lane);
+            const int ldr = __ffs(peers) - 1;
+            if (gleaf && ldr == (int)lane) glid = leaf_of_claimed(I, leaf_cache, leaf_claim, gv0);
+            glid = __shfl_sync(0xFFFFFFFFu, glid, ldr);
+        } else if (gleaf) {
+            glid = leaf_of<T>(I, leaf_cache, gv0);
+        }
         uint64_t gid;
         uint32_t gval;
         if (set == 0) {
             gid = EMPTY_ID;
             gval = 0;
         } else if (!is_branch) {
-            gid = act ? leaf_of<T>(I, leaf_cache, gv0) : 0ull;
+            gid = act ? glid : 0ull;
             gval = gv0;
         } else {
             gid = id;
