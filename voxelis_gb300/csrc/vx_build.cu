@@ -391,8 +391,6 @@ __device__ __forceinline__ void kc_insert(const KeyCache &C, uint64_t lo, uint64
     }
 }
 
-// One parent from 8 children held by the calling lane: EMPTY, a collapsed leaf, or an interned
-// branch (warp-cooperative; every lane of the warp calls it).
 // One reference per child slot of branch `id`, which the calling lane just created (equal children
 // summed first): leaves of 8-bit interners into the CTA's per-value counters when leaf_cnt is given
 // (added to the leaves by leaf_cnt_flush), everything else by fire-and-forget atomics. The children
@@ -480,7 +478,9 @@ __device__ __forceinline__ void leaf_cnt_clear(uint32_t *leaf_cnt) {
     for (unsigned v = threadIdx.x; v < 256; v += blockDim.x) leaf_cnt[v] = 0;
 }
 
-// created (optional): whether this lane created the branch, for callers that count references.
+// One parent from 8 children held by the calling lane: EMPTY, a collapsed leaf, or an interned
+// branch (warp-cooperative; every lane of the warp calls it). created (optional): whether this lane
+// created the branch, for callers that count references.
 __device__ __forceinline__ void reduce_parent(const DevInterner &I, bool active, const uint64_t c[8],
                                               const uint32_t cv[8], uint64_t &out, uint32_t &out_val,
                                               bool *created_out = nullptr) {
@@ -1717,11 +1717,12 @@ __global__ void __launch_bounds__(kQ16Warps * 32, VX_Q16_MINB) dense_quads16_ker
 
 // ---- pending memo records, computed once each ------------------------------------------------------
 //
-// Every record on the live list (claims that won their memo slot, or found none) is a distinct quad of
-// this build; dead claims, about nine in ten on a cold memo, are not walked. Without the list every
-// handed-out record is checked. A warp takes 4 records at a time, 8 lanes each: lane 8m + k reduces bottom group k of the m-th
-// record from the record's row words (the groups, keys and interning of quad_groups), then lane 8m
-// reduces the quad node and writes the record's tail. Group keys go through the CTA's key cache.
+// Every record on the live list (claims that won their memo slot, or found none) is a distinct quad
+// of this build; dead claims, about nine in ten on a cold memo, are not walked. Without the list every
+// handed-out record is checked. A warp takes 4 records at a time, 8 lanes each: lane 8m + k reduces
+// bottom group k of the m-th record from the record's row words (the groups, keys and interning of
+// quad_groups), then lane 8m reduces the quad node and writes the record's tail. Group keys go
+// through the CTA's key cache.
 template <class T>
 __global__ void __launch_bounds__(kQ16Warps * 32) dense_memo_compute_kernel(DevInterner I, OctArgs a) {
     pdl_wait();
